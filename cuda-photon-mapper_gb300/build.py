@@ -1,0 +1,83 @@
+"""Builds libphotonmap.so (the CUDA kernels and the C ABI of include/pm.h)
+in-tree for sm_103a, plus the CPU oracle library used by the tests.
+
+    python cuda-photon-mapper_gb300/build.py          # library + oracle
+"""
+import concurrent.futures as cf
+import glob
+import os
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libphotonmap.so")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle.so")
+REF_DIR = "/root/reference"
+
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s" % (" ".join(cmd), r.stdout))
+    return r.stdout
+
+
+def build_library(force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    objs, jobs = [], []
+    for src in sources:
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        objs.append(obj)
+        if force or _newer(obj, [src] + headers):
+            jobs.append([NVCC] + ARCH + NVFLAGS + ["-c", src, "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        list(ex.map(_run, jobs))
+    if force or jobs or _newer(LIB, objs):
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    return LIB
+
+
+def build_oracle(force=False):
+    sources = sorted(glob.glob(os.path.join(ORACLE_DIR, "*.c")))
+    headers = glob.glob(os.path.join(ORACLE_DIR, "*.h"))
+    if force or _newer(ORACLE_LIB, sources + headers):
+        _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+              "-shared", "-o", ORACLE_LIB] + sources + ["-lm"])
+    return ORACLE_LIB
+
+
+def build_reference():
+    """Compiles the reference's own code into oracle/_ref (needs the checkout)."""
+    if not os.path.isdir(REF_DIR):
+        return None
+    _run(["make", "-s", "-C", ROOT, "-f", "oracle/ref.mk", "REF=" + REF_DIR])
+    return os.path.join(ORACLE_DIR, "_ref", "libpmref.so")
+
+
+def build_all(force=False):
+    build_library(force)
+    build_oracle(force)
+    build_reference()
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv)
+    print("built", LIB, ORACLE_LIB)

@@ -1,0 +1,46 @@
+// radix_sort.cuh -- stable LSD radix sort of (key, uint32 value) pairs and
+// the exclusive scan it is built on.
+//
+// The element count is read from device memory, so a whole pipeline
+// (count -> scan -> sort -> reduce) runs without a host round trip; max_n
+// only sizes the grids. Each 8-bit pass is reduce-then-scan: a per-tile
+// digit histogram, one exclusive scan over all (digit, tile) counts, and a
+// scatter in which every tile ranks its items with warp match masks, so
+// equal keys keep their input order.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+namespace pm {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;
+
+// Number of uint32 words of scratch the sort needs for max_n elements.
+inline size_t radix_sort_hist_words(uint32_t max_n) {
+    uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
+    if (tiles == 0) tiles = 1;
+    return (size_t)256 * tiles;
+}
+
+// Sorts keys[0..n) with their values by bits [begin_bit, end_bit), n read
+// from n_dev. Ping-pongs between (keys, vals) and (keys_tmp, vals_tmp);
+// *out_keys / *out_vals receive whichever pair holds the result.
+// hist must hold radix_sort_hist_words(max_n) words.
+cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp,
+                                 uint32_t *vals_tmp, const uint32_t *n_dev, uint32_t max_n,
+                                 int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
+                                 uint32_t **out_keys, uint32_t **out_vals);
+cudaError_t radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t *keys_tmp,
+                                 uint32_t *vals_tmp, const uint32_t *n_dev, uint32_t max_n,
+                                 int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
+                                 uint64_t **out_keys, uint32_t **out_vals);
+
+// Exclusive prefix sum of in[0..n) into out[0..n) with one CTA; the total
+// goes to *total (device). n is a host value here.
+cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total,
+                               cudaStream_t stream);
+
+}  // namespace pm

@@ -1,0 +1,142 @@
+"""Legacy mode on the GPU against the serial CPU oracle, bit for bit, and
+against the reference's golden digests. Calls go through the C ABI."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+import photonmap  # noqa: E402
+from oracle import LegacyOracle  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "legacy_ref.npz"))
+FLAGS = {(0, 0): 0, (1, 0): 1, (0, 1): 2, (1, 1): 3}
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def render(ctx, w, h, t, flags):
+    img = torch.zeros((h, w, 4), dtype=torch.uint8, device="cuda")
+    rgb = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+    ctx.legacy_render(img.data_ptr(), w, h, t, flags, rgb.data_ptr())
+    torch.cuda.synchronize()
+    return img.cpu().numpy(), rgb.cpu().numpy()
+
+
+@pytest.fixture
+def ctx():
+    c = photonmap.Context(0)
+    yield c
+    c.close()
+
+
+def test_random_table_bit_exact(ctx):
+    o = LegacyOracle()
+    ctx.legacy_init_random()
+    o.init_random()
+    np.testing.assert_array_equal(bits(ctx.legacy_random_numbers()), bits(o.table()))
+    assert sha(ctx.legacy_random_numbers()) == str(GOLD["table_sha"])
+    assert ctx.legacy_rng_draws() == 30000
+
+
+def test_emission_before_random_table(ctx):
+    ctx.legacy_emit(0.0, 0)
+    assert sha(ctx.legacy_grid()) == str(GOLD["pre_init_grid_sha"])
+    img, _ = render(ctx, 512, 512, 0.0, 0)
+    assert sha(img) == str(GOLD["pre_init_img_sha"])
+
+
+def test_frame_sequence_bit_exact(ctx):
+    o = LegacyOracle()
+    ctx.legacy_init_random()
+    o.init_random()
+    for i, (t, interp, media, w, h) in enumerate(GOLD["frames"]):
+        t, interp, media, w, h = float(t), int(interp), int(media), int(w), int(h)
+        flags = FLAGS[(interp, media)]
+        ctx.legacy_emit(t, flags)
+        o.emit(t, interp, media)
+        g = ctx.legacy_grid()
+        np.testing.assert_array_equal(bits(g), bits(o.grid()), err_msg="grid of frame %d" % i)
+        img, rgb = render(ctx, w, h, t, flags)
+        oimg, orgb = o.render(w, h, t, interp, media)
+        np.testing.assert_array_equal(bits(rgb), bits(orgb), err_msg="radiance of frame %d" % i)
+        np.testing.assert_array_equal(img, oimg, err_msg="image of frame %d" % i)
+        if t == 0.0:  # animTime 0 needs no libm call: digests carry across machines
+            assert sha(g) == str(GOLD["f%d_grid_sha" % i])
+            assert sha(img) == str(GOLD["f%d_img_sha" % i])
+
+
+def test_emission_is_deterministic(ctx):
+    ctx.legacy_init_random()
+    ctx.legacy_emit(0.3, 2)
+    a = ctx.legacy_grid()
+    for _ in range(3):
+        ctx.legacy_emit(0.3, 2)
+        np.testing.assert_array_equal(bits(ctx.legacy_grid()), bits(a))
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_many_animated_frames(ctx, seed):
+    rs = np.random.RandomState(seed)
+    o = LegacyOracle()
+    ctx.legacy_init_random()
+    o.init_random()
+    media_frames = 0
+    for _ in range(12):
+        t = float(np.float32(rs.uniform(0, 20)))
+        interp, media = int(rs.randint(2)), int(rs.randint(2))
+        media_frames += media
+        ctx.legacy_emit(t, FLAGS[(interp, media)])
+        o.emit(t, interp, media)
+        np.testing.assert_array_equal(bits(ctx.legacy_grid()), bits(o.grid()))
+    assert ctx.legacy_rng_draws() == 30000 + 90000 * media_frames
+
+
+def test_render_of_arbitrary_grid(ctx):
+    # Random grid contents exercise every window and blend of the gather.
+    rs = np.random.RandomState(7)
+    g = rs.standard_normal((32, 32, 32, 3)).astype(np.float32)
+    o = LegacyOracle()
+    o.set_grid(g)
+    ctx.legacy_set_grid(g)
+    for (interp, media), flags in FLAGS.items():
+        for t in (0.0, 1.25):
+            img, rgb = render(ctx, 256, 192, t, flags)
+            oimg, orgb = o.render(256, 192, t, interp, media)
+            np.testing.assert_array_equal(bits(rgb), bits(orgb))
+            np.testing.assert_array_equal(img, oimg)
+
+
+def test_empty_image(ctx):
+    ctx.legacy_init_random()
+    ctx.legacy_render(0, 0, 0, 0.0, 0)
+    ctx.legacy_render(0, 0, 512, 0.0, 0)
+
+
+def test_reference_exports(ctx):
+    lib = photonmap.load()
+    lib.pm_legacy_set_exit_on_error(0)
+    lib.pm_legacy_release()
+    o = LegacyOracle()
+    img = torch.zeros((512, 512, 4), dtype=torch.uint8, device="cuda")
+    # display() order (callbacksPBO.cpp:47-63) after initCuda's early emission.
+    photonmap.launch_emit_photons_kernel(img.data_ptr(), 512, 512, 0.0, False, False)
+    photonmap.launch_init_random_numbers_kernel()
+    o.init_random()
+    for t, interp, media in [(0.0, False, False), (0.1, True, True), (0.2, False, True)]:
+        photonmap.launch_emit_photons_kernel(img.data_ptr(), 512, 512, t, interp, media)
+        photonmap.launch_photon_mapping_kernel(img.data_ptr(), 512, 512, t, interp, media)
+        assert lib.pm_legacy_last_status() == 0
+        o.emit(t, interp, media)
+        oimg, _ = o.render(512, 512, t, interp, media)
+        np.testing.assert_array_equal(img.cpu().numpy(), oimg)
+    lib.pm_legacy_release()
