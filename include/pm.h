@@ -114,6 +114,111 @@ PM_API pm_status pm_legacy_get_random_numbers(pm_ctx *ctx, float *host_out);
  * 90,000 per emission with participating media). */
 PM_API pm_status pm_legacy_rng_draws(pm_ctx *ctx, unsigned long long *draws);
 
+/* ---- 3. physically based mode --------------------------------------------
+ *
+ * Photon tracing through a Cornell-style box with spheres and a
+ * participating medium, a kd-tree over each photon map and a k-nearest
+ * photon radiance estimate per pixel. The scene keeps the reference's layout
+ * (float4 spheres = centre xyz + radius, float2 planes = axis code + offset,
+ * photonMappingKernel.cu:59-73) and adds a material per object. Photon
+ * records export in the reference's record layout {location, direction,
+ * energy} ("photonMappingKernel - Copy.cu":30-31). */
+
+#define PM_MAX_SPHERES 64
+#define PM_MAX_PLANES 8
+
+enum { PM_MAT_DIFFUSE = 0, PM_MAT_MIRROR = 1, PM_MAT_DIELECTRIC = 2 };
+enum { PM_MAP_SURFACE = 0, PM_MAP_VOLUME = 1 };
+
+typedef struct pm_material {
+    int kind;          /* PM_MAT_* */
+    float albedo[3];   /* diffuse reflectance (diffuse only) */
+    float ior;         /* index of refraction (dielectric only) */
+} pm_material;
+
+typedef struct pm_scene {
+    int num_spheres;
+    float4 spheres[PM_MAX_SPHERES];          /* centre xyz, radius w */
+    pm_material sphere_mat[PM_MAX_SPHERES];
+    int num_planes;
+    float2 planes[PM_MAX_PLANES];            /* axis (0=x,1=y,2=z) as float, offset */
+    pm_material plane_mat[PM_MAX_PLANES];
+    float box_min[3], box_max[3];            /* planes are bounded by this box; the medium fills it */
+    float light[3];                          /* isotropic point light */
+    float light_power;                       /* watts, white */
+    float sigma_s, sigma_a, hg_g;            /* homogeneous medium (sigma_s = 0: none) */
+    int het_res;                             /* >0: sigma_s from a het_res^3 value-noise grid */
+    float het_min, het_max;                  /* range the noise grid is scaled to */
+    float cam_pos[3];                        /* pinhole camera looking +z */
+    float focal;
+} pm_scene;
+
+typedef struct pm_config {
+    uint64_t seed;              /* Philox key (low and high words) */
+    uint32_t scene_id;          /* Philox counter word 3: separates scenes of a batch */
+    uint32_t surface_photons;   /* target size of the surface map */
+    uint32_t volume_photons;    /* target size of the volume map */
+    uint32_t max_paths;         /* cap on emitted paths, 0 = 16 x the larger target */
+    int max_bounces;            /* interactions per path */
+    float rr_survival;          /* Russian-roulette survival probability */
+    int width, height;          /* image */
+    int k;                      /* neighbours per radiance estimate (<= 128) */
+    float radius;               /* gather radius cap */
+    float march_step;           /* volume ray-march step, 0 = no march */
+    int leaf_size;              /* kd-tree leaf size: 32 (one warp) */
+    float exposure;             /* scale applied before the 8-bit conversion */
+} pm_config;
+
+/* The reference's record layout: one photon as three float3. */
+typedef struct pm_photon_record {
+    float location[3];
+    float direction[3];   /* direction of travel when stored */
+    float energy[3];      /* flux, watts per channel */
+} pm_photon_record;
+
+typedef struct pm_frame_stats {
+    uint64_t paths_traced;              /* photon paths emitted this frame */
+    uint32_t map_size[2];               /* records in the surface / volume map */
+    uint32_t map_paths[2];              /* paths that the map's power is normalised by */
+    uint64_t surface_gathers;           /* k-NN queries on the surface map */
+    uint64_t volume_gathers;            /* k-NN queries on the volume map (march steps) */
+    float ms_emit, ms_build, ms_render; /* device time of the last emit / build / render */
+} pm_frame_stats;
+
+/* Fills *scene and *cfg with one of the benchmark presets:
+ * 1 = small box, 2 spheres, 100k photons, 512^2, k=64;
+ * 2 = 8 seeded spheres, 1M surface + 1M volume photons, 1024^2, k=100, step 0.01;
+ * 3 = 64 spheres, heterogeneous medium, 8M + 8M photons, 1920x1080, k=128.
+ * Host only; needs no GPU. */
+PM_API pm_status pm_preset(int preset, uint64_t seed, pm_scene *scene, pm_config *cfg);
+
+/* Installs a scene and configuration (copies both); allocates the maps. */
+PM_API pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg);
+/* Traces photon paths until both maps reach their targets. Synchronises
+ * the stream once to learn the map sizes. */
+PM_API pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream);
+/* Builds the kd-tree of each map (Morton sort + median split + node boxes). */
+PM_API pm_status pm_build(pm_ctx *ctx, cudaStream_t stream);
+/* Renders one frame: eye rays, specular chains, the volume march and the
+ * surface radiance estimate. radiance (nullable, device): width*height
+ * float4 (rgb, alpha = 1); rgba (nullable, device): width*height uchar4. */
+PM_API pm_status pm_render(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStream_t stream);
+/* k nearest photons of map `map` for nq query points (device float4
+ * xyz), within radius; idx_out / d2_out (device, nq*k) receive photon
+ * indices and squared distances sorted by (distance, index); missing
+ * neighbours are 0xFFFFFFFF / radius^2. Needs pm_build. */
+PM_API pm_status pm_knn(pm_ctx *ctx, int map, const float4 *queries, uint32_t nq, int k,
+                        float radius, uint32_t *idx_out, float *d2_out, cudaStream_t stream);
+/* Synchronous copy of a map in index order, in the reference's record
+ * layout (cap records at most); *count receives the map size. */
+PM_API pm_status pm_get_photons(pm_ctx *ctx, int map, pm_photon_record *out, uint32_t cap,
+                                uint32_t *count);
+/* Synchronous copy of a map's raw SoA records in index order: pos = xyz +
+ * index bits, pow = rgb flux + octahedral direction bits. */
+PM_API pm_status pm_get_photons_soa(pm_ctx *ctx, int map, float4 *pos, float4 *pow,
+                                    uint32_t cap, uint32_t *count);
+PM_API pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

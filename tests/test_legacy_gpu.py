@@ -76,12 +76,26 @@ def test_frame_sequence_bit_exact(ctx):
 
 
 def test_emission_is_deterministic(ctx):
+    # Without media the generator is untouched: repeated emissions agree.
     ctx.legacy_init_random()
-    ctx.legacy_emit(0.3, 2)
+    ctx.legacy_emit(0.3, 1)
     a = ctx.legacy_grid()
     for _ in range(3):
-        ctx.legacy_emit(0.3, 2)
+        ctx.legacy_emit(0.3, 1)
         np.testing.assert_array_equal(bits(ctx.legacy_grid()), bits(a))
+    # With media each emission advances the shared generator by 90,000
+    # draws, as the reference's does; two contexts replaying the same calls
+    # agree bit for bit.
+    grids = []
+    for _ in range(2):
+        c = photonmap.Context(0)
+        c.legacy_init_random()
+        c.legacy_emit(0.3, 2)
+        c.legacy_emit(0.3, 2)
+        grids.append(c.legacy_grid())
+        assert c.legacy_rng_draws() == 30000 + 2 * 90000
+        c.close()
+    np.testing.assert_array_equal(bits(grids[0]), bits(grids[1]))
 
 
 @pytest.mark.parametrize("seed", [0, 1])
