@@ -59,7 +59,7 @@ def build_oracle(force=False):
     sources = sorted(glob.glob(os.path.join(ORACLE_DIR, "*.c")))
     headers = glob.glob(os.path.join(ORACLE_DIR, "*.h"))
     if force or _newer(ORACLE_LIB, sources + headers):
-        _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+        _run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
               "-shared", "-o", ORACLE_LIB] + sources + ["-lm"])
     return ORACLE_LIB
 

@@ -1,0 +1,363 @@
+// gather.cu -- warp-cooperative k-nearest-photon search, radiance estimates
+// and the frame render (eye rays, specular chains, volume march).
+//
+// One warp answers one query. The k best candidates so far live in
+// registers as a list sorted by (squared distance, photon index), spread
+// across the warp: lane l holds list positions l*S .. l*S+S-1 (S = k/32
+// rounded up). Inserting a candidate is one shuffle from the previous lane
+// plus S compare-selects per lane. The tree is walked 32 children at a time:
+// the implicit layout puts the descendants five levels below node n at
+// n*32 .. n*32+31, so each lane tests one child box with one coalesced
+// load; surviving children are pushed far-to-near onto a per-warp stack in
+// shared memory. Leaves are 32 consecutive records, one per lane.
+//
+// A node is skipped only when its box is strictly farther than the current
+// k-th candidate, so a photon at exactly that distance with a smaller index
+// is still found: the result equals a brute-force sort by (distance, index).
+#include "gather.cuh"
+
+namespace pm {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kStackCap = 192;     // 32 entries per wide level, 6 levels: depth <= 29
+constexpr int kWarpsPerBlock = 4;
+constexpr int kMaxSpecular = 8;
+constexpr uint32_t kEyeSalt = 0xE7E5A17Bu;
+
+__device__ __forceinline__ uint64_t make_key(float d2, uint32_t idx) {
+    return ((uint64_t)__float_as_uint(d2) << 32) | idx;
+}
+__device__ __forceinline__ float key_d2(uint64_t k) { return __uint_as_float((uint32_t)(k >> 32)); }
+
+template <int S>
+struct Knn {
+    uint64_t key[S];
+    uint32_t at[S];  // tree position of the record
+    uint64_t worst;
+    int k;
+
+    __device__ __forceinline__ void reset(uint64_t cap, int kk) {
+        k = kk;
+#pragma unroll
+        for (int s = 0; s < S; ++s) { key[s] = cap; at[s] = 0xffffffffu; }
+        worst = cap;
+    }
+    __device__ __forceinline__ void update_worst() {
+        const int kl = (k - 1) / S, ks = (k - 1) % S;
+        uint64_t w = key[0];
+#pragma unroll
+        for (int s = 1; s < S; ++s)
+            if (s == ks) w = key[s];
+        worst = __shfl_sync(kFull, w, kl);
+    }
+    // Inserts x (< worst) keeping the list sorted.
+    __device__ __forceinline__ void insert(uint64_t x, uint32_t xa, int lane) {
+        uint64_t pk = __shfl_up_sync(kFull, key[S - 1], 1);
+        uint32_t pa = __shfl_up_sync(kFull, at[S - 1], 1);
+#pragma unroll
+        for (int s = S - 1; s >= 0; --s) {
+            uint64_t below = s > 0 ? key[s - 1] : pk;
+            uint32_t below_at = s > 0 ? at[s - 1] : pa;
+            bool first = (s == 0) && (lane == 0);
+            if (key[s] >= x) {
+                if (first || below < x) { key[s] = x; at[s] = xa; }
+                else { key[s] = below; at[s] = below_at; }
+            }
+        }
+        update_worst();
+    }
+};
+
+__device__ __forceinline__ float box_d2(float4 lo, float4 hi, v3 q) {
+    float dx = fmaxf(fmaxf(lo.x - q.x, q.x - hi.x), 0.0f);
+    float dy = fmaxf(fmaxf(lo.y - q.y, q.y - hi.y), 0.0f);
+    float dz = fmaxf(fmaxf(lo.z - q.z, q.z - hi.z), 0.0f);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+template <int S>
+__device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, uint32_t *st_node, float *st_d2,
+                           int lane) {
+    if (m.n == 0) return;
+    const uint32_t first_leaf = 1u << m.depth;
+    int top = 1;
+    if (lane == 0) { st_node[0] = 1u; st_d2[0] = 0.0f; }
+    __syncwarp();
+    while (top > 0) {
+        --top;
+        const uint32_t node = st_node[top];
+        const float nd2 = st_d2[top];
+        __syncwarp();
+        const float wd2 = key_d2(kn.worst);
+        if (nd2 > wd2) continue;
+        const int dn = 31 - __clz(node);
+        if (dn == m.depth) {
+            const uint32_t base = (node - first_leaf) * 32u;
+            const uint32_t r = base + lane;
+            uint64_t key = ~0ull;
+            if (r < m.n) {
+                float4 p = __ldg(&m.pos[r]);
+                float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                key = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
+            }
+            unsigned mask = __ballot_sync(kFull, key < kn.worst);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                uint64_t x = __shfl_sync(kFull, key, src);
+                kn.insert(x, base + src, lane);
+                mask &= mask - 1;
+                mask &= __ballot_sync(kFull, key < kn.worst);
+            }
+        } else {
+            int w = (m.depth - dn) % 5;
+            if (w == 0) w = 5;
+            const int nc = 1 << w;
+            const uint32_t child = (node << w) + lane;
+            float bd2 = __int_as_float(0x7f800000);
+            if (lane < nc) bd2 = box_d2(__ldg(&m.lo[child]), __ldg(&m.hi[child]), q);
+            const bool ok = (lane < nc) && (bd2 <= wd2);
+            const unsigned mask = __ballot_sync(kFull, ok);
+            // Far-to-near: rank = survivors farther than this lane (ties: higher lane farther).
+            int rank = 0;
+            for (unsigned mm = mask; mm; mm &= mm - 1) {
+                const int j = __ffs(mm) - 1;
+                float o = __shfl_sync(kFull, bd2, j);
+                rank += (o > bd2 || (o == bd2 && j > lane)) ? 1 : 0;
+            }
+            if (ok && top + rank < kStackCap) {
+                st_node[top + rank] = child;
+                st_d2[top + rank] = bd2;
+            }
+            top = min(top + __popc(mask), kStackCap);
+            __syncwarp();
+        }
+    }
+}
+
+// Kahan sum within a lane, then a compensated butterfly across the warp:
+// every lane ends with the same value.
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
+    float y = x - comp;
+    float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+__device__ __forceinline__ float warp_csum(float sum, float comp) {
+    float s = sum, e = -comp;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        float s2 = __shfl_xor_sync(kFull, s, off);
+        float e2 = __shfl_xor_sync(kFull, e, off);
+        float t = s + s2;
+        float bb = t - s;
+        float err = (s - (t - bb)) + (s2 - bb);
+        e = (e + e2) + err;
+        s = t;
+    }
+    return s + e;
+}
+
+// Radiance-estimate numerator: sum of photon flux times weight over the
+// k-NN list. mode 0: surface (weight 1 for photons arriving on the side nf
+// faces, else 0); mode 1: volume (HG phase toward wo). Returns found count
+// and the squared radius in *r2.
+template <int S>
+__device__ v3 flux_sum(const Knn<S> &kn, const MapView &m, int lane, int mode, v3 dirv, float g,
+                       uint64_t cap, float r2cap, int *found, float *r2) {
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    int cnt = 0;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int j = lane * S + s;
+        if (j < kn.k && kn.key[s] != cap) {
+            ++cnt;
+            float4 pw = __ldg(&m.pow[kn.at[s]]);
+            v3 dir = oct_decode(__float_as_uint(pw.w));
+            float w;
+            if (mode == 0) w = dot(dirv, dir) < 0.0f ? 1.0f : 0.0f;
+            else w = hg_phase(g, dot(dir, dirv));
+            kahan_add(sx, cx, pw.x * w);
+            kahan_add(sy, cy, pw.y * w);
+            kahan_add(sz, cz, pw.z * w);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) cnt += __shfl_xor_sync(kFull, cnt, off);
+    *found = cnt;
+    *r2 = cnt == kn.k ? key_d2(kn.worst) : r2cap;
+    return mk3(warp_csum(sx, cx), warp_csum(sy, cy), warp_csum(sz, cz));
+}
+
+template <int S>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) knn_kernel(MapView m, const float4 *q,
+                                                                  uint32_t nq, int k, float r2cap,
+                                                                  uint32_t *idx_out, float *d2_out) {
+    __shared__ uint32_t st_node[kWarpsPerBlock][kStackCap];
+    __shared__ float st_d2[kWarpsPerBlock][kStackCap];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t qi = blockIdx.x * kWarpsPerBlock + wib;
+    if (qi >= nq) return;
+    float4 qq = q[qi];
+    const uint64_t cap = make_key(r2cap, 0xffffffffu);
+    Knn<S> kn;
+    kn.reset(cap, k);
+    knn_search<S>(m, mk3(qq.x, qq.y, qq.z), kn, st_node[wib], st_d2[wib], lane);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int j = lane * S + s;
+        if (j < k) {
+            idx_out[(size_t)qi * k + j] = (uint32_t)kn.key[s];
+            d2_out[(size_t)qi * k + j] = key_d2(kn.key[s]);
+        }
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, MapView surf,
+                                                                     MapView vol, RenderParams R,
+                                                                     float4 *rad, uchar4 *rgba) {
+    __shared__ uint32_t st_node[kWarpsPerBlock][kStackCap];
+    __shared__ float st_d2[kWarpsPerBlock][kStackCap];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t pix = blockIdx.x * kWarpsPerBlock + wib;
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
+    if (pix >= npix) return;
+    const uint32_t px = pix % (uint32_t)R.width, py = pix / (uint32_t)R.width;
+    const float u = ((float)px / (float)R.width - 0.5f) * R.aspect;
+    const float v = -((float)py / (float)R.height - 0.5f);
+    v3 o = mk3(Sc.cam[0], Sc.cam[1], Sc.cam[2]);
+    v3 d = normalize(mk3(u, v, Sc.focal));
+    const uint64_t cap = make_key(R.r2cap, 0xffffffffu);
+    v3 L = mk3(0.f, 0.f, 0.f);
+    float tau = 0.0f;
+    bool glass = false;
+    uint32_t nsurf = 0, nvol = 0;
+    for (int depth = 0; depth < kMaxSpecular; ++depth) {
+        PHit h = intersect(Sc, o, d, 3.0e38f);
+        const float tend = h.obj != kNone ? h.t : 3.0e38f;
+        if (R.step > 0.0f && Sc.sigma_max > 0.0f && !glass) {
+            float t0, t1;
+            box_span(Sc, o, d, &t0, &t1);
+            t1 = fminf(t1, tend);
+            if (t0 < t1) {
+                const int nst = (int)ceilf((t1 - t0) / R.step);
+                const v3 wo = d * -1.0f;
+                for (int j = 0; j < nst; ++j) {
+                    const float ta = t0 + (float)j * R.step;
+                    const float tb = fminf(t0 + (float)(j + 1) * R.step, t1);
+                    const float dt = tb - ta;
+                    const float tm = 0.5f * (ta + tb);
+                    const v3 x = o + d * tm;
+                    const float ss = Sc.het_res > 0 ? sigma_s_at(Sc, x) : Sc.sigma_s;
+                    const float st = ss + Sc.sigma_a;
+                    const float tau_mid = tau + st * (0.5f * dt);
+                    if (vol.n > 0) {
+                        Knn<S> kn;
+                        kn.reset(cap, R.k);
+                        knn_search<S>(vol, x, kn, st_node[wib], st_d2[wib], lane);
+                        int found;
+                        float r2;
+                        v3 e = flux_sum<S>(kn, vol, lane, 1, wo, Sc.g, cap, R.r2cap, &found, &r2);
+                        ++nvol;
+                        if (found > 0) {
+                            const float scale = pm_expf(-tau_mid) * dt * (1.0f / (4.18879020f * r2 * sqrtf(r2)));
+                            L = L + e * scale;
+                        }
+                    }
+                    tau = tau + st * dt;
+                }
+            }
+        }
+        if (h.obj == kNone) break;
+        const v3 hp = o + d * h.t;
+        const v3 n = outward_normal(Sc, h.obj, hp);
+        const int kind = material_kind(Sc, h.obj);
+        const float dn = dot(n, d);
+        const v3 nf = dn < 0.0f ? n : n * -1.0f;
+        if (kind == PM_MAT_DIFFUSE) {
+            if (surf.n > 0) {
+                Knn<S> kn;
+                kn.reset(cap, R.k);
+                knn_search<S>(surf, hp, kn, st_node[wib], st_d2[wib], lane);
+                int found;
+                float r2;
+                v3 e = flux_sum<S>(kn, surf, lane, 0, nf, 0.0f, cap, R.r2cap, &found, &r2);
+                ++nsurf;
+                if (found > 0) {
+                    const v3 a = material_albedo(Sc, h.obj);
+                    const float scale = pm_expf(-tau) * (1.0f / (3.14159265f * r2)) * 0.318309886f;
+                    L = L + mk3(a.x * (e.x * scale), a.y * (e.y * scale), a.z * (e.z * scale));
+                }
+            }
+            break;
+        }
+        if (kind == PM_MAT_MIRROR) {
+            d = normalize(d - n * (2.0f * dn));
+            o = hp + nf * kOffset;
+        } else {
+            float ci = -dn;
+            const bool entering = ci > 0.0f;
+            const float ior = material_ior(Sc, h.obj);
+            const float eta = entering ? 1.0f / ior : ior;
+            const v3 nn = entering ? n : n * -1.0f;
+            ci = fabsf(ci);
+            float ct;
+            const float F = fresnel(ci, eta, &ct);
+            pm_u32x4 r = philox(R.seed, pix, (uint32_t)depth, kEyeSalt, R.scene_id);
+            if (pm_u01(r.v[0]) < F) {
+                d = normalize(d + nn * (2.0f * ci));
+                o = hp + nn * kOffset;
+            } else {
+                d = normalize(d * eta + nn * (eta * ci - ct));
+                o = hp - nn * kOffset;
+                glass = entering;
+            }
+        }
+    }
+    if (lane == 0) {
+        if (rad) rad[pix] = make_float4(L.x, L.y, L.z, 1.0f);
+        if (rgba)
+            rgba[pix] = make_uchar4(to_u8_sat((double)(L.x * R.exposure) * 255.0),
+                                    to_u8_sat((double)(L.y * R.exposure) * 255.0),
+                                    to_u8_sat((double)(L.z * R.exposure) * 255.0), 255);
+        if (R.counters) {
+            if (nsurf) atomicAdd(&R.counters[0], (unsigned long long)nsurf);
+            if (nvol) atomicAdd(&R.counters[1], (unsigned long long)nvol);
+        }
+    }
+}
+
+int slots_for(int k) { return (k + 31) / 32; }
+
+}  // namespace
+
+cudaError_t knn_query(const MapView &m, const float4 *q, uint32_t nq, int k, float radius,
+                      uint32_t *idx, float *d2, cudaStream_t s) {
+    if (nq == 0) return cudaSuccess;
+    const float r2 = radius * radius;
+    const dim3 grid((nq + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
+    switch (slots_for(k)) {
+        case 1: knn_kernel<1><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
+        case 2: knn_kernel<2><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
+        case 3: knn_kernel<3><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
+        default: knn_kernel<4><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vol,
+                         const RenderParams &R, float4 *rad, uchar4 *rgba, cudaStream_t s) {
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
+    if (npix == 0) return cudaSuccess;
+    const dim3 grid((npix + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
+    switch (slots_for(R.k)) {
+        case 1: render_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
+        case 2: render_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
+        case 3: render_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
+        default: render_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace pm

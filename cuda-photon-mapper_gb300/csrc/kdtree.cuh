@@ -1,0 +1,27 @@
+// kdtree.cuh -- Morton-ordered implicit kd-tree over a photon map.
+#pragma once
+#include "phys_common.cuh"
+
+namespace pm {
+
+// Depth D of the tree over n records (leaves of 32 at depth D, 2^D leaf slots).
+int tree_depth(uint32_t n);
+// Node array length (index 0 unused, root at 1): 2^(D+1).
+size_t tree_nodes(uint32_t n);
+
+struct KdBuildArgs {
+    uint32_t n;                 // records
+    const uint32_t *n_dev;      // the same count in device memory
+    float3 lo, hi;              // Morton quantisation box
+    const float4 *pos_in, *pow_in;   // records in index order
+    float4 *pos_out, *pow_out;       // records in tree order
+    float4 *node_lo, *node_hi;       // tree_nodes(n) boxes
+    uint64_t *keys, *keys_tmp;       // n each
+    uint32_t *vals, *vals_tmp;       // n each
+    uint32_t *hist;                  // radix_sort_hist_words(n)
+    uint32_t *order_out;             // nullable: tree position -> record index
+};
+
+cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s);
+
+}  // namespace pm

@@ -57,6 +57,45 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(const uint32_t *in, 
     if (threadIdx.x == 0 && total_out) *total_out = total;
 }
 
+// Per-tile sums for the large scan (tile = kSortTile elements).
+__global__ void __launch_bounds__(kSortThreads) tile_sum_kernel(const uint32_t *in, uint32_t n,
+                                                                uint32_t *sums) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    const uint32_t base = blockIdx.x * kSortTile + threadIdx.x * kSortItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        uint32_t idx = base + i;
+        if (idx < n) s += in[idx];
+    }
+    block_exclusive_scan(s, warp_sums, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kSortThreads) tile_scan_kernel(const uint32_t *in, uint32_t *out,
+                                                                 uint32_t n,
+                                                                 const uint32_t *offs) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t total;
+    const uint32_t base = blockIdx.x * kSortTile + threadIdx.x * kSortItems;
+    uint32_t v[kSortItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        uint32_t idx = base + i;
+        v[i] = idx < n ? in[idx] : 0u;
+        s += v[i];
+    }
+    uint32_t run = block_exclusive_scan(s, warp_sums, &total) + offs[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        uint32_t idx = base + i;
+        if (idx < n) out[idx] = run;
+        run += v[i];
+    }
+}
+
 template <typename K>
 __global__ void __launch_bounds__(kSortThreads) hist_kernel(const K *keys, const uint32_t *n_dev,
                                                             int shift, uint32_t *hist,
@@ -150,6 +189,21 @@ cudaError_t radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t *keys_
                                  uint64_t **out_keys, uint32_t **out_vals) {
     return sort_pairs<uint64_t>(keys, vals, keys_tmp, vals_tmp, n_dev, max_n, begin_bit, end_bit,
                                 hist, stream, out_keys, out_vals);
+}
+
+uint32_t scan_tile_count(uint32_t n) {
+    uint32_t t = (n + kSortTile - 1) / kSortTile;
+    return t == 0 ? 1 : t;
+}
+
+cudaError_t exclusive_scan_u32_large(const uint32_t *in, uint32_t *out, uint32_t n,
+                                     uint32_t *total, uint32_t *tmp, cudaStream_t stream) {
+    if (n <= 65536) return exclusive_scan_u32(in, out, n, total, stream);
+    uint32_t tiles = scan_tile_count(n);
+    tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(in, n, tmp);
+    scan_kernel<<<1, kScanThreads, 0, stream>>>(tmp, tmp, tiles, total);
+    tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(in, out, n, tmp);
+    return cudaGetLastError();
 }
 
 cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total,

@@ -43,4 +43,11 @@ cudaError_t radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t *keys_
 cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total,
                                cudaStream_t stream);
 
+// Exclusive prefix sum of in[0..n) for large n: per-tile sums, one scan of
+// the tile sums, then per-tile scans. tmp must hold scan_tile_count(n) + 1
+// words. *total (device) receives the sum.
+uint32_t scan_tile_count(uint32_t n);
+cudaError_t exclusive_scan_u32_large(const uint32_t *in, uint32_t *out, uint32_t n,
+                                     uint32_t *total, uint32_t *tmp, cudaStream_t stream);
+
 }  // namespace pm

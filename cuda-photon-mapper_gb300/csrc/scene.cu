@@ -48,7 +48,7 @@ void base_box(pm_scene &s) {
     set_mat(s.plane_mat[4], PM_MAT_DIFFUSE, 0.75f, 0.75f, 0.75f, 1.0f);
     s.light[0] = 0.0f; s.light[1] = 0.95f; s.light[2] = 0.0f;
     s.light_power = 1.0f;
-    s.cam[0] = 0.0f; s.cam[1] = 0.5f; s.cam[2] = -1.5f;
+    s.cam_pos[0] = 0.0f; s.cam_pos[1] = 0.5f; s.cam_pos[2] = -1.5f;
     s.focal = 1.0f;
 }
 

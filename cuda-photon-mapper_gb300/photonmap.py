@@ -20,6 +20,60 @@ LEGACY_GRID = 32
 LEGACY_PHOTONS = 10000
 
 _c = ctypes
+
+
+class Material(_c.Structure):
+    _fields_ = [("kind", _c.c_int), ("albedo", _c.c_float * 3), ("ior", _c.c_float)]
+
+
+class Scene(_c.Structure):
+    """pm_scene (include/pm.h); padding mirrors float4/float2 alignment."""
+    _fields_ = [
+        ("num_spheres", _c.c_int), ("_pad0", _c.c_byte * 12),
+        ("spheres", (_c.c_float * 4) * 64),
+        ("sphere_mat", Material * 64),
+        ("num_planes", _c.c_int), ("_pad1", _c.c_byte * 4),
+        ("planes", (_c.c_float * 2) * 8),
+        ("plane_mat", Material * 8),
+        ("box_min", _c.c_float * 3), ("box_max", _c.c_float * 3),
+        ("light", _c.c_float * 3), ("light_power", _c.c_float),
+        ("sigma_s", _c.c_float), ("sigma_a", _c.c_float), ("hg_g", _c.c_float),
+        ("het_res", _c.c_int), ("het_min", _c.c_float), ("het_max", _c.c_float),
+        ("cam_pos", _c.c_float * 3), ("focal", _c.c_float),
+        ("_pad2", _c.c_byte * 8),
+    ]
+
+
+class Config(_c.Structure):
+    _fields_ = [
+        ("seed", _c.c_uint64), ("scene_id", _c.c_uint32),
+        ("surface_photons", _c.c_uint32), ("volume_photons", _c.c_uint32),
+        ("max_paths", _c.c_uint32), ("max_bounces", _c.c_int), ("rr_survival", _c.c_float),
+        ("width", _c.c_int), ("height", _c.c_int), ("k", _c.c_int), ("radius", _c.c_float),
+        ("march_step", _c.c_float), ("leaf_size", _c.c_int), ("exposure", _c.c_float),
+        ("_pad", _c.c_byte * 4),
+    ]
+
+
+class PhotonRecord(_c.Structure):
+    _fields_ = [("location", _c.c_float * 3), ("direction", _c.c_float * 3),
+                ("energy", _c.c_float * 3)]
+
+
+class FrameStats(_c.Structure):
+    _fields_ = [
+        ("paths_traced", _c.c_uint64), ("map_size", _c.c_uint32 * 2),
+        ("map_paths", _c.c_uint32 * 2), ("surface_gathers", _c.c_uint64),
+        ("volume_gathers", _c.c_uint64), ("ms_emit", _c.c_float), ("ms_build", _c.c_float),
+        ("ms_render", _c.c_float), ("_pad", _c.c_byte * 4),
+    ]
+
+
+MAP_SURFACE = 0
+MAP_VOLUME = 1
+MAT_DIFFUSE, MAT_MIRROR, MAT_DIELECTRIC = 0, 1, 2
+NOISE_SEED_SALT = 0x6E6F697365
+
 _vp = _c.c_void_p
 _u = _c.c_uint
 _f = _c.c_float
@@ -45,6 +99,17 @@ PROTOTYPES = {
     "pm_legacy_set_grid": (_i, [_vp, _vp]),
     "pm_legacy_get_random_numbers": (_i, [_vp, _vp]),
     "pm_legacy_rng_draws": (_i, [_vp, _c.POINTER(_c.c_ulonglong)]),
+    "pm_preset": (_i, [_i, _c.c_uint64, _c.POINTER(Scene), _c.POINTER(Config)]),
+    "pm_set_scene": (_i, [_vp, _c.POINTER(Scene), _c.POINTER(Config)]),
+    "pm_emit": (_i, [_vp, _vp]),
+    "pm_build": (_i, [_vp, _vp]),
+    "pm_render": (_i, [_vp, _vp, _vp, _vp]),
+    "pm_knn": (_i, [_vp, _i, _vp, _c.c_uint32, _i, _f, _vp, _vp, _vp]),
+    "pm_get_photons": (_i, [_vp, _i, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
+    "pm_get_photons_soa": (_i, [_vp, _i, _vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
+    "pm_get_stats": (_i, [_vp, _c.POINTER(FrameStats)]),
+    "pm_abi_struct_size": (_c.c_size_t, [_i]),
+    "pm_set_photons": (_i, [_vp, _i, _vp, _vp, _c.c_uint32]),
 }
 
 _lib = None
@@ -133,6 +198,67 @@ class Context:
         n = _c.c_ulonglong()
         self._check(self.lib.pm_legacy_rng_draws(self.h, _c.byref(n)), "pm_legacy_rng_draws")
         return n.value
+
+
+    # physically based mode --------------------------------------------------
+    def set_scene(self, scene, cfg):
+        self.scene, self.cfg = scene, cfg
+        self._check(self.lib.pm_set_scene(self.h, _c.byref(scene), _c.byref(cfg)), "pm_set_scene")
+
+    def emit(self, stream=0):
+        self._check(self.lib.pm_emit(self.h, stream), "pm_emit")
+
+    def build(self, stream=0):
+        self._check(self.lib.pm_build(self.h, stream), "pm_build")
+
+    def render(self, radiance=None, rgba=None, stream=0):
+        self._check(self.lib.pm_render(self.h, radiance, rgba, stream), "pm_render")
+
+    def knn(self, map_id, queries, nq, k, radius, idx, d2, stream=0):
+        self._check(self.lib.pm_knn(self.h, map_id, queries, nq, k, radius, idx, d2, stream),
+                    "pm_knn")
+
+    def photons_soa(self, map_id):
+        """Map `map_id` in index order: (pos float32[n,4], pow float32[n,4])."""
+        n = _c.c_uint32()
+        self._check(self.lib.pm_get_photons_soa(self.h, map_id, None, None, 0, _c.byref(n)),
+                    "pm_get_photons_soa")
+        pos = np.zeros((n.value, 4), np.float32)
+        pw = np.zeros((n.value, 4), np.float32)
+        self._check(self.lib.pm_get_photons_soa(self.h, map_id, pos.ctypes.data, pw.ctypes.data,
+                                                n.value, _c.byref(n)), "pm_get_photons_soa")
+        return pos, pw
+
+    def photon_records(self, map_id):
+        """Map `map_id` in the reference's record layout, float32[n, 9]
+        (location, direction, energy)."""
+        n = _c.c_uint32()
+        self._check(self.lib.pm_get_photons(self.h, map_id, None, 0, _c.byref(n)), "pm_get_photons")
+        out = np.zeros((n.value, 9), np.float32)
+        self._check(self.lib.pm_get_photons(self.h, map_id, out.ctypes.data, n.value, _c.byref(n)),
+                    "pm_get_photons")
+        return out
+
+    def set_photons(self, map_id, pos, pw):
+        pos = np.ascontiguousarray(pos, np.float32)
+        pw = np.ascontiguousarray(pw, np.float32)
+        assert pos.shape == pw.shape and pos.shape[1] == 4
+        self._check(self.lib.pm_set_photons(self.h, map_id, pos.ctypes.data, pw.ctypes.data,
+                                            len(pos)), "pm_set_photons")
+
+    def stats(self):
+        st = FrameStats()
+        self._check(self.lib.pm_get_stats(self.h, _c.byref(st)), "pm_get_stats")
+        return st
+
+
+def preset(which, seed=0x5EED0000):
+    """Benchmark preset `which` (1, 2, 3): returns (Scene, Config)."""
+    sc, cf = Scene(), Config()
+    s = load().pm_preset(which, seed, _c.byref(sc), _c.byref(cf))
+    if s != PM_OK:
+        raise PMError("pm_preset(%d): %s" % (which, load().pm_status_string(s).decode()))
+    return sc, cf
 
 
 # The reference's three exports (photonMappingKernel.cu:1523,1549,1569).

@@ -218,6 +218,17 @@ PM_API pm_status pm_get_photons(pm_ctx *ctx, int map, pm_photon_record *out, uin
 PM_API pm_status pm_get_photons_soa(pm_ctx *ctx, int map, float4 *pos, float4 *pow,
                                     uint32_t cap, uint32_t *count);
 PM_API pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out);
+/* Replaces map `map` with n host records in the SoA layout of
+ * pm_get_photons_soa (pos.w is overwritten with the record index); used to
+ * load a saved map or to query an arbitrary point set. Needs pm_set_scene
+ * (its box bounds the Morton codes); follow with pm_build. */
+PM_API pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *pow,
+                                uint32_t n);
+
+/* sizeof of the ABI structs as this library was compiled (0 = pm_scene,
+ * 1 = pm_config, 2 = pm_photon_record, 3 = pm_frame_stats), for bindings
+ * in other languages to check their struct layouts against. */
+PM_API size_t pm_abi_struct_size(int which);
 
 #ifdef __cplusplus
 }

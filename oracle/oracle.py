@@ -81,3 +81,120 @@ class LegacyOracle:
         r = np.zeros(2, np.uint32)
         self.lib.pmo_legacy_get_rng(self.h, r.ctypes.data)
         return r
+
+
+# ---- physically based mode ---------------------------------------------------
+
+def _phys_protos(lib):
+    vp, u32, i, f = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_float
+    lib.pmo_emit.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.pmo_emit.restype = i
+    lib.pmo_knn.argtypes = [vp, u32, vp, u32, i, f, vp, vp]
+    lib.pmo_knn.restype = None
+    lib.pmo_render.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp]
+    lib.pmo_render.restype = None
+    lib.pmo_noise_grid.argtypes = [vp, i, ctypes.c_uint64, f, f]
+    lib.pmo_noise_grid.restype = None
+    lib.pmo_philox.argtypes = [ctypes.c_uint64, vp, vp]
+    lib.pmo_philox.restype = None
+    lib.pmo_logf.argtypes = [f]
+    lib.pmo_logf.restype = f
+    lib.pmo_expf.argtypes = [f]
+    lib.pmo_expf.restype = f
+    lib.pmo_sincos2pi.argtypes = [f, vp, vp]
+    lib.pmo_sincos2pi.restype = None
+    lib.pmo_oct_encode.argtypes = [vp]
+    lib.pmo_oct_encode.restype = u32
+    lib.pmo_oct_decode.argtypes = [u32, vp]
+    lib.pmo_oct_decode.restype = None
+    lib.pmo_sizeof_scene.restype = ctypes.c_size_t
+    lib.pmo_sizeof_config.restype = ctypes.c_size_t
+    lib.pmo64_emit.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.pmo64_emit.restype = i
+    lib.pmo64_render.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32, vp, u32, vp]
+    lib.pmo64_render.restype = None
+    lib.pmo_trace_path.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]
+    lib.pmo_trace_path.restype = None
+
+
+def phys_lib():
+    lib = load()
+    if not getattr(lib, "_phys_ready", False):
+        _phys_protos(lib)
+        lib._phys_ready = True
+    return lib
+
+
+NOISE_SEED_SALT = 0x6E6F697365
+
+
+def noise_grid(scene, cfg):
+    """The heterogeneous medium's sigma_s grid (None for a homogeneous one)."""
+    if scene.het_res <= 0:
+        return None
+    r = scene.het_res
+    g = np.zeros(r * r * r, np.float32)
+    phys_lib().pmo_noise_grid(g.ctypes.data, r, (cfg.seed ^ NOISE_SEED_SALT) & (2 ** 64 - 1),
+                              scene.het_min, scene.het_max)
+    return g
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class PhysicalMaps:
+    def __init__(self, spos, spow, vpos, vpow, sizes, paths):
+        self.spos, self.spow, self.vpos, self.vpow = spos, spow, vpos, vpow
+        self.sizes, self.paths = sizes, paths
+
+
+def emit(scene, cfg, het=None, double=False):
+    """Photon maps as the GPU compacts them (float32) or their float64
+    counterpart (pos [n,4], pow [n,6] with the direction in pow[:,3:])."""
+    lib = phys_lib()
+    ns, nv = cfg.surface_photons, cfg.volume_photons
+    dt, w = (np.float64, 6) if double else (np.float32, 4)
+    spos = np.zeros((max(ns, 1), 4), dt)
+    spow = np.zeros((max(ns, 1), w), dt)
+    vpos = np.zeros((max(nv, 1), 4), dt)
+    vpow = np.zeros((max(nv, 1), w), dt)
+    sizes = np.zeros(2, np.uint32)
+    paths = np.zeros(2, np.uint32)
+    fn = lib.pmo64_emit if double else lib.pmo_emit
+    fn(ctypes.byref(scene), ctypes.byref(cfg), _ptr(het), spos.ctypes.data, spow.ctypes.data,
+       vpos.ctypes.data, vpow.ctypes.data, sizes.ctypes.data, paths.ctypes.data)
+    return PhysicalMaps(spos[:sizes[0]], spow[:sizes[0]], vpos[:sizes[1]], vpow[:sizes[1]], sizes,
+                        paths)
+
+
+def knn(pos, queries, k, radius):
+    pos = np.ascontiguousarray(pos, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    idx = np.zeros((len(q), k), np.uint32)
+    d2 = np.zeros((len(q), k), np.float32)
+    phys_lib().pmo_knn(pos.ctypes.data, len(pos), q.ctypes.data, len(q), k, radius,
+                       idx.ctypes.data, d2.ctypes.data)
+    return idx, d2
+
+
+def render(scene, cfg, het, maps, pixels=None, double=False):
+    """Radiance float[npix, 4] for the given pixel indices (all by default)."""
+    lib = phys_lib()
+    if pixels is None:
+        pixels = np.arange(cfg.width * cfg.height, dtype=np.uint32)
+    pixels = np.ascontiguousarray(pixels, np.uint32)
+    if double:
+        out = np.zeros((len(pixels), 4), np.float64)
+        lib.pmo64_render(ctypes.byref(scene), ctypes.byref(cfg), _ptr(het), maps.spos.ctypes.data,
+                         maps.spow.ctypes.data, len(maps.spos), maps.vpos.ctypes.data,
+                         maps.vpow.ctypes.data, len(maps.vpos), pixels.ctypes.data, len(pixels),
+                         out.ctypes.data)
+        return out
+    out = np.zeros((len(pixels), 4), np.float32)
+    gathers = np.zeros(2, np.uint64)
+    lib.pmo_render(ctypes.byref(scene), ctypes.byref(cfg), _ptr(het), maps.spos.ctypes.data,
+                   maps.spow.ctypes.data, len(maps.spos), maps.vpos.ctypes.data,
+                   maps.vpow.ctypes.data, len(maps.vpos), pixels.ctypes.data, len(pixels),
+                   out.ctypes.data, gathers.ctypes.data)
+    return out

@@ -1,0 +1,204 @@
+"""Physically based mode on the GPU against the single-precision CPU oracle
+(bit for bit) and the double-precision oracle (relative RMSE), through the
+C ABI."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+import photonmap  # noqa: E402
+import oracle  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def small(preset, surface=20000, volume=20000, size=(48, 40), k=None, radius=None, seed=0x5EED0001):
+    sc, cf = photonmap.preset(preset, seed)
+    cf.surface_photons, cf.volume_photons = surface, volume
+    cf.width, cf.height = size
+    if k is not None:
+        cf.k = k
+    if radius is not None:
+        cf.radius = radius
+    return sc, cf
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.fixture
+def ctx():
+    c = photonmap.Context(0)
+    yield c
+    c.close()
+
+
+def gpu_frame(ctx, sc, cf):
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    ctx.build()
+    rad = torch.zeros((cf.height * cf.width, 4), dtype=torch.float32, device="cuda")
+    rgba = torch.zeros((cf.height * cf.width, 4), dtype=torch.uint8, device="cuda")
+    ctx.render(rad.data_ptr(), rgba.data_ptr())
+    torch.cuda.synchronize()
+    return rad.cpu().numpy(), rgba.cpu().numpy()
+
+
+@pytest.mark.parametrize("preset", [1, 2, 3])
+def test_emission_bit_exact(ctx, preset):
+    sc, cf = small(preset, 30000, 30000)
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    het = oracle.noise_grid(sc, cf)
+    m = oracle.emit(sc, cf, het)
+    st = ctx.stats()
+    assert list(st.map_size) == list(m.sizes)
+    assert list(st.map_paths) == list(m.paths)
+    for mid, (op, ow) in enumerate([(m.spos, m.spow), (m.vpos, m.vpow)]):
+        pos, pw = ctx.photons_soa(mid)
+        np.testing.assert_array_equal(bits(pos), bits(op))
+        np.testing.assert_array_equal(bits(pw), bits(ow))
+
+
+def test_emission_close_to_float64(ctx):
+    sc, cf = small(2, 30000, 30000)
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    m64 = oracle.emit(sc, cf, None, double=True)
+    pos, pw = ctx.photons_soa(0)
+    assert len(pos) == len(m64.spos)
+    rel = np.abs(pos[:, :3] - m64.spos[:, :3]) / np.maximum(np.abs(m64.spos[:, :3]), 1e-3)
+    # Paths that take a different branch in float32 (a grazing hit or a
+    # threshold draw) diverge; all others agree to 1e-5 relative.
+    ok = (rel < 1e-5).all(axis=1)
+    assert ok.mean() > 0.97, ok.mean()
+    prel = np.abs(pw[:, :3] - m64.spow[:, :3]) / np.abs(m64.spow[:, :3])
+    assert np.median(prel) < 1e-5
+
+
+@pytest.mark.parametrize("k,radius", [(1, 0.05), (17, 0.08), (32, 0.1), (64, 0.1), (100, 0.05),
+                                      (128, 0.2)])
+def test_knn_bit_exact(ctx, k, radius):
+    sc, cf = small(1, 40000, 10000)
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    ctx.build()
+    rs = np.random.RandomState(k)
+    q = np.zeros((3000, 4), np.float32)
+    q[:, 0] = rs.uniform(-0.55, 0.55, 3000)
+    q[:, 1] = rs.uniform(-0.05, 1.05, 3000)
+    q[:, 2] = rs.uniform(-0.55, 0.55, 3000)
+    for mid in (0, 1):
+        pos, _ = ctx.photons_soa(mid)
+        qd = torch.from_numpy(q).cuda()
+        idx = torch.zeros((3000, k), dtype=torch.int32, device="cuda")
+        d2 = torch.zeros((3000, k), dtype=torch.float32, device="cuda")
+        ctx.knn(mid, qd.data_ptr(), 3000, k, radius, idx.data_ptr(), d2.data_ptr())
+        torch.cuda.synchronize()
+        oi, od = oracle.knn(pos, q, k, radius)
+        np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32), oi)
+        np.testing.assert_array_equal(bits(d2.cpu().numpy()), bits(od))
+
+
+def test_knn_ties_broken_by_index(ctx):
+    # A lattice with every point repeated three times: many neighbours at
+    # exactly equal distance; the answer must follow the photon index.
+    sc, cf = small(1, 1000, 1000)
+    ctx.set_scene(sc, cf)
+    g = np.stack(np.meshgrid(np.arange(-0.5, 0.51, 0.05), np.arange(0.0, 1.01, 0.05),
+                             np.arange(-0.5, 0.51, 0.05), indexing="ij"), -1).reshape(-1, 3)
+    g = np.repeat(g, 3, axis=0).astype(np.float32)
+    rs = np.random.RandomState(3)
+    perm = rs.permutation(len(g))
+    pos = np.zeros((len(g), 4), np.float32)
+    pos[:, :3] = g[perm]
+    pw = np.ones((len(g), 4), np.float32)
+    ctx.set_photons(0, pos, pw)
+    ctx.build()
+    q = np.zeros((500, 4), np.float32)
+    q[:, :3] = g[rs.randint(0, len(g), 500)]
+    q[250:, 0] += 0.025  # midway between lattice planes: equal distances to both
+    for k in (7, 27, 64, 128):
+        qd = torch.from_numpy(q).cuda()
+        idx = torch.zeros((500, k), dtype=torch.int32, device="cuda")
+        d2 = torch.zeros((500, k), dtype=torch.float32, device="cuda")
+        ctx.knn(0, qd.data_ptr(), 500, k, 0.12, idx.data_ptr(), d2.data_ptr())
+        torch.cuda.synchronize()
+        oi, od = oracle.knn(pos, q, k, 0.12)
+        np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32), oi)
+        np.testing.assert_array_equal(bits(d2.cpu().numpy()), bits(od))
+
+
+def test_knn_empty_and_tiny_maps(ctx):
+    sc, cf = small(1, 1000, 1000)
+    ctx.set_scene(sc, cf)
+    q = torch.zeros((4, 4), dtype=torch.float32, device="cuda")
+    idx = torch.zeros((4, 8), dtype=torch.int32, device="cuda")
+    d2 = torch.zeros((4, 8), dtype=torch.float32, device="cuda")
+    for n in (0, 1, 5, 33):
+        pos = np.zeros((n, 4), np.float32)
+        pos[:, 0] = np.linspace(-0.1, 0.1, n)
+        ctx.set_photons(1, pos, np.ones((n, 4), np.float32))
+        ctx.build()
+        ctx.knn(1, q.data_ptr(), 4, 8, 0.5, idx.data_ptr(), d2.data_ptr())
+        torch.cuda.synchronize()
+        oi, od = oracle.knn(pos, np.zeros((4, 4), np.float32), 8, 0.5)
+        np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32), oi)
+        np.testing.assert_array_equal(bits(d2.cpu().numpy()), bits(od))
+
+
+@pytest.mark.parametrize("preset,size", [(1, (48, 40)), (2, (40, 40)), (3, (64, 36))])
+def test_render_bit_exact(ctx, preset, size):
+    sc, cf = small(preset, 20000, 20000, size)
+    rad, rgba = gpu_frame(ctx, sc, cf)
+    het = oracle.noise_grid(sc, cf)
+    m = oracle.emit(sc, cf, het)
+    orad = oracle.render(sc, cf, het, m)
+    np.testing.assert_array_equal(bits(rad), bits(orad))
+    assert rad[:, :3].max() > 0.0
+    st = ctx.stats()
+    assert st.surface_gathers > 0 and st.volume_gathers > 0
+
+
+def test_render_against_float64(ctx):
+    sc, cf = small(2, 30000, 30000, (40, 40))
+    rad, _ = gpu_frame(ctx, sc, cf)
+    m64 = oracle.emit(sc, cf, None, double=True)
+    r64 = oracle.render(sc, cf, None, m64, double=True)
+    err = np.sqrt(np.mean((rad[:, :3] - r64[:, :3]) ** 2)) / np.sqrt(np.mean(r64[:, :3] ** 2))
+    # tolerance: float32 trajectories and neighbour sets vs float64 ones
+    assert err < 2e-2, err
+
+
+def test_emit_build_render_repeatable(ctx):
+    sc, cf = small(1, 20000, 20000, (32, 32))
+    a, _ = gpu_frame(ctx, sc, cf)
+    ctx.emit()
+    ctx.build()
+    rad = torch.zeros((32 * 32, 4), dtype=torch.float32, device="cuda")
+    ctx.render(rad.data_ptr(), None)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(rad.cpu().numpy()), bits(a))
+
+
+def test_record_layout_export(ctx):
+    sc, cf = small(1, 5000, 5000)
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    rec = ctx.photon_records(0)
+    pos, pw = ctx.photons_soa(0)
+    np.testing.assert_array_equal(rec[:, 0:3], pos[:, :3])
+    np.testing.assert_array_equal(rec[:, 6:9], pw[:, :3])
+    nrm = np.linalg.norm(rec[:, 3:6], axis=1)
+    np.testing.assert_allclose(nrm, 1.0, atol=1e-5)
+
+
+def test_state_errors(ctx):
+    lib = photonmap.load()
+    assert lib.pm_emit(ctx.h, None) == 4
+    sc, cf = small(1, 1000, 1000)
+    ctx.set_scene(sc, cf)
+    assert lib.pm_render(ctx.h, None, None, None) == 4
+    cf.k = 0
+    with pytest.raises(photonmap.PMError):
+        ctx.set_scene(sc, cf)
