@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Frame benchmark of the GB300 photon mapper.
+
+One step = one frame of the physically based pipeline on benchmark preset 2
+(8 seeded spheres in the box, 1M surface + 1M volume photons, a kd-tree over
+each map, 1024x1024 eye rays with specular chains, a k=100 nearest-photon
+surface estimate and a volume march of step 0.01 with a k=100 volume
+estimate per step): pm_emit + pm_build + pm_render through the C ABI.
+
+Prints one JSON line. `value` is k-NN gathers (surface + volume radiance
+estimates) per second of whole-frame device time; photon throughput and the
+per-phase times are reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank renders its own replica of the scene on its GPU
+(replicas only: the path has no exchange step); value = all ranks' gathers
+over the slowest rank's time. --impl reference times the CPU restatement of
+the same path (the reference has no physically based tracer of its own) on
+this host's cores, on a bounded sample of the same frame.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cuda-photon-mapper_gb300")
+sys.path.insert(0, PKG)
+
+PRESET_DESC = {
+    1: "box with 2 spheres, 100k surface + 100k volume photons, 512x512, k=64, r<=0.1, march 0.01",
+    2: "box with 8 seeded spheres, 1M surface + 1M volume photons, kd-tree per map, 1024x1024, "
+       "k=100, r<=0.05, volume march step 0.01",
+    3: "box with 64 spheres, heterogeneous 128^3 medium, 8M + 8M photons, 1920x1080, k=128, "
+       "r<=0.05, march 0.01",
+}
+L2_FLUSH_BYTES = 256 << 20
+CPU_SAMPLE_PIXELS = 2048
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--preset", type=int, default=2)
+    ap.add_argument("--seed", type=lambda s: int(s, 0), default=0x5EED0002)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+def dist_info():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(preset):
+    """DRAM bytes per render launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "render_kernel_preset%d_traffic.txt" % preset)
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_frame_sample(scene, cfg, pixels, seed=1234):
+    """The CPU restatement on a bounded sample of one frame: full photon
+    emission, neighbour grids over both maps, `pixels` random pixels shaded
+    with all host threads. Returns frame-equivalent numbers."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+    het = oracle.noise_grid(scene, cfg)
+    t0 = time.perf_counter()
+    maps = oracle.emit(scene, cfg, het)
+    t_emit = time.perf_counter() - t0
+    npix = cfg.width * cfg.height
+    rs = np.random.RandomState(seed)
+    pix = np.sort(rs.choice(npix, size=min(pixels, npix), replace=False)).astype(np.uint32)
+    _, gathers, secs = oracle.render_timed(scene, cfg, het, maps, pix)
+    scale = npix / float(len(pix))
+    g_frame = float(gathers.sum()) * scale
+    t_frame = t_emit + secs[0] + secs[1] * scale
+    return {
+        "gathers_per_s": g_frame / t_frame,
+        "frame_s": t_frame,
+        "emit_s": t_emit,
+        "grid_s": float(secs[0]),
+        "shade_sample_s": float(secs[1]),
+        "sample_pixels": int(len(pix)),
+        "paths": int(max(maps.paths)),
+        "cores": os.cpu_count(),
+    }
+
+
+def run_reference(args):
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    import photonmap
+    scene, cfg = photonmap.preset(args.preset, args.seed)
+    threads = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    for _ in range(args.warmup):
+        cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
+    vals, frames = [], []
+    for i in range(args.steps):
+        r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS, seed=1234 + i)
+        vals.append(r["gathers_per_s"])
+        frames.append(r["frame_s"])
+    value = statistics.mean(vals)
+    sample = ("per step: full CPU photon emission (%d paths, 1 thread), neighbour grids, "
+              "%d random pixels of %dx%d shaded on %d threads; frame time extrapolated to all "
+              "pixels" % (r["paths"], CPU_SAMPLE_PIXELS, cfg.width, cfg.height, threads))
+    line = {
+        "impl": "reference",
+        "metric": "gathers/s", "value": value, "unit": "gathers/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(frames), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "preset %d: %s" % (args.preset, PRESET_DESC[args.preset]),
+                   "preset": args.preset},
+        "cpu_baseline": {"value": value, "unit": "gathers/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "gathers/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import photonmap
+
+    world, rank, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    lib = photonmap.load()
+    scene, cfg = photonmap.preset(args.preset, args.seed)
+    cfg.scene_id = rank  # each replica traces its own photon streams
+    ctx = photonmap.Context(local)
+    ctx.set_scene(scene, cfg)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    npix = cfg.width * cfg.height
+    rad = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
+    rgba = torch.empty((npix, 4), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def frame():
+        ctx.emit(sh)
+        ctx.build(sh)
+        ctx.render(rad.data_ptr(), rgba.data_ptr(), sh)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            frame()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        l0 = lib.pm_kernel_launches()
+        frame_ms, emit_ms, build_ms, render_ms = [], [], [], []
+        gathers = surf = vol = paths = 0
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between frames, before the start event
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            frame()
+            ev1.record(stream)
+            ev1.synchronize()
+            st = ctx.stats()
+            frame_ms.append(ev0.elapsed_time(ev1))
+            emit_ms.append(st.ms_emit)
+            build_ms.append(st.ms_build)
+            render_ms.append(st.ms_render)
+            surf += st.surface_gathers
+            vol += st.volume_gathers
+            paths += st.paths_traced
+        launches = lib.pm_kernel_launches() - l0
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        map_sizes = list(st.map_size)
+    gathers = surf + vol
+    t_total = sum(frame_ms) / 1e3
+    t_render = sum(render_ms) / 1e3
+
+    # end to end through the C ABI: per step the scene goes in from host
+    # memory (pm_update_scene), the frame's radiance and 8-bit image come
+    # back to pinned host buffers.
+    host_rad = torch.empty((npix, 4), dtype=torch.float32).pin_memory()
+    host_rgba = torch.empty((npix, 4), dtype=torch.uint8).pin_memory()
+    e2e_g = 0
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(args.e2e_steps):
+            ctx.update_scene(scene)
+            frame()
+            host_rad.copy_(rad, non_blocking=True)
+            host_rgba.copy_(rgba, non_blocking=True)
+            stream.synchronize()
+            st = ctx.stats()
+            e2e_g += st.surface_gathers + st.volume_gathers
+    t_e2e = time.perf_counter() - t0
+    barrier()
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_total, t_e2e], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        g = torch.tensor([gathers, e2e_g, paths, launches], dtype=torch.float64, device="cuda")
+        dist.all_reduce(g, op=dist.ReduceOp.SUM)
+        t_total, t_e2e = t.tolist()
+        gathers, e2e_g, paths, launches = [int(x) for x in g.tolist()]
+    if rank != 0:
+        return 0
+
+    peak, peak_kind = load_peaks()
+    k = cfg.k
+    render_s = t_render / args.steps
+    q_per_frame = (surf + vol) / args.steps
+    alg_bytes = q_per_frame * 32.0 * k + npix * 16.0
+    achieved = alg_bytes / render_s / 1e9
+    traffic = load_traffic(args.preset)
+    line = {
+        "metric": "gathers/s",
+        "value": gathers / t_total,
+        "unit": "gathers/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": "preset %d: %s" % (args.preset, PRESET_DESC[args.preset]),
+            "preset": args.preset, "seed": args.seed, "resolution": [cfg.width, cfg.height],
+            "photons": [cfg.surface_photons, cfg.volume_photons], "k": k,
+            "radius": cfg.radius, "march_step": cfg.march_step,
+            "l2": "flushed between timed frames (256 MiB write, outside the timed events)",
+            "parallelism": "replicas x%d" % world,
+        },
+        "phases": {
+            "emit_ms": statistics.mean(emit_ms), "build_ms": statistics.mean(build_ms),
+            "render_ms": statistics.mean(render_ms), "frame_ms": statistics.mean(frame_ms),
+            "paths_per_frame": paths / args.steps / world,
+            "photons_per_s": paths / (sum(emit_ms) / 1e3) / world,
+            "records_per_s": sum(map_sizes) * args.steps / (sum(emit_ms) / 1e3),
+            "map_sizes": map_sizes,
+            "surface_gathers_per_frame": surf / args.steps,
+            "volume_gathers_per_frame": vol / args.steps,
+        },
+        "e2e": {"value": e2e_g / t_e2e, "unit": "gathers/s",
+                "h2d_bytes_per_step": int(photonmap.ctypes.sizeof(photonmap.Scene)),
+                "d2h_bytes_per_step": int(npix * (16 + 4)),
+                "steps": args.e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": "render_kernel", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind,
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "formula": "gathers x 32 B x k + pixels x 16 B, over the render "
+                                "kernel's CUDA-event time"},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
+        line["cpu_baseline"] = {
+            "value": r["gathers_per_s"], "unit": "gathers/s", "cores": r["cores"], "kind": "port",
+            "sample": "full CPU photon emission (%d paths, 1 thread) + neighbour grids + %d "
+                      "random pixels shaded on %d threads, frame time extrapolated to %dx%d"
+                      % (r["paths"], r["sample_pixels"], r["cores"], cfg.width, cfg.height),
+            "frame_s": r["frame_s"],
+        }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

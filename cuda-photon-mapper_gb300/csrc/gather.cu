@@ -14,6 +14,7 @@
 // A node is skipped only when its box is strictly farther than the current
 // k-th candidate, so a photon at exactly that distance with a smaller index
 // is still found: the result equals a brute-force sort by (distance, index).
+#include "launch_count.cuh"
 #include "gather.cuh"
 
 namespace pm {
@@ -24,6 +25,7 @@ constexpr int kStackCap = 192;     // 32 entries per wide level, 6 levels: depth
 constexpr int kWarpsPerBlock = 4;
 constexpr int kMaxSpecular = 8;
 constexpr uint32_t kEyeSalt = 0xE7E5A17Bu;
+constexpr int kMaxMarchSteps = 1 << 16;  // per segment
 
 __device__ __forceinline__ uint64_t make_key(float d2, uint32_t idx) {
     return ((uint64_t)__float_as_uint(d2) << 32) | idx;
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
             box_span(Sc, o, d, &t0, &t1);
             t1 = fminf(t1, tend);
             if (t0 < t1) {
-                const int nst = (int)ceilf((t1 - t0) / R.step);
+                const int nst = (int)fminf(ceilf((t1 - t0) / R.step), (float)kMaxMarchSteps);
                 const v3 wo = d * -1.0f;
                 for (int j = 0; j < nst; ++j) {
                     const float ta = t0 + (float)j * R.step;
@@ -338,10 +340,10 @@ cudaError_t knn_query(const MapView &m, const float4 *q, uint32_t nq, int k, flo
     const float r2 = radius * radius;
     const dim3 grid((nq + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
     switch (slots_for(k)) {
-        case 1: knn_kernel<1><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
-        case 2: knn_kernel<2><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
-        case 3: knn_kernel<3><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
-        default: knn_kernel<4><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); break;
+        case 1: knn_kernel<1><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); note_launch(); break;
+        case 2: knn_kernel<2><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); note_launch(); break;
+        case 3: knn_kernel<3><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); note_launch(); break;
+        default: knn_kernel<4><<<grid, block, 0, s>>>(m, q, nq, k, r2, idx, d2); note_launch(); break;
     }
     return cudaGetLastError();
 }
@@ -352,10 +354,10 @@ cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vo
     if (npix == 0) return cudaSuccess;
     const dim3 grid((npix + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
     switch (slots_for(R.k)) {
-        case 1: render_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
-        case 2: render_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
-        case 3: render_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
-        default: render_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); break;
+        case 1: render_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); note_launch(); break;
+        case 2: render_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); note_launch(); break;
+        case 3: render_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); note_launch(); break;
+        default: render_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); note_launch(); break;
     }
     return cudaGetLastError();
 }

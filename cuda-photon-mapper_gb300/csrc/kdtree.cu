@@ -9,6 +9,7 @@
 //    load), node i has children 2i and 2i+1 and leaves sit at depth D. Each
 //    node stores the bounding box of its records (lo, hi), built bottom-up,
 //    so a query can bound the distance to everything below a node.
+#include "launch_count.cuh"
 #include "kdtree.cuh"
 #include "radix_sort.cuh"
 
@@ -104,24 +105,27 @@ size_t tree_nodes(uint32_t n) { return (size_t)2 << tree_depth(n); }
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     const uint32_t n = a.n;
     if (n == 0) return cudaSuccess;
-    morton_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.pos_in, n, a.lo, a.hi, a.keys, a.vals);
+    morton_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.pos_in, n, a.lo, a.hi, a.keys, a.vals); note_launch();
     uint64_t *sk = nullptr;
     uint32_t *sv = nullptr;
     cudaError_t e = radix_sort_pairs_u64(a.keys, a.vals, a.keys_tmp, a.vals_tmp, a.n_dev, n, 0, 64,
                                          a.hist, s, &sk, &sv);
     if (e != cudaSuccess) return e;
-    permute_kernel<<<(n + 255) / 256, 256, 0, s>>>(sv, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out);
+    permute_kernel<<<(n + 255) / 256, 256, 0, s>>>(sv, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out); note_launch();
     const int D = tree_depth(n);
     const uint32_t first_leaf = 1u << D;
     leaf_box_kernel<<<(first_leaf * 32 + 255) / 256, 256, 0, s>>>(a.pos_out, n, first_leaf, first_leaf,
-                                                                 a.node_lo, a.node_hi);
+                                                                 a.node_lo, a.node_hi); note_launch();
     // Wide levels one launch each; the top 10 levels in a single CTA.
     int l = D - 1;
     for (; l >= 10; --l) {
         uint32_t first = 1u << l;
-        inner_box_kernel<<<(first + 255) / 256, 256, 0, s>>>(first, first, a.node_lo, a.node_hi);
+        inner_box_kernel<<<(first + 255) / 256, 256, 0, s>>>(first, first, a.node_lo, a.node_hi); note_launch();
     }
-    if (l >= 0) top_box_kernel<<<1, 1024, 0, s>>>((uint32_t)(l + 1), a.node_lo, a.node_hi);
+    if (l >= 0) {
+        top_box_kernel<<<1, 1024, 0, s>>>((uint32_t)(l + 1), a.node_lo, a.node_hi);
+        note_launch();
+    }
     if (a.order_out) {
         e = cudaMemcpyAsync(a.order_out, sv, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return e;

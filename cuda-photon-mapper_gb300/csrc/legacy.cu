@@ -8,6 +8,7 @@
 // sphere animation is computed once on the host instead of by every
 // thread, the random table is filled in parallel by jumping the generator
 // ahead, and grid accumulation is a deterministic sort + ordered sum.
+#include "launch_count.cuh"
 #include "legacy.cuh"
 #include "pm_vec.cuh"
 #include "radix_sort.cuh"
@@ -550,7 +551,7 @@ void legacy_free(LegacyState &st) {
 cudaError_t legacy_init_random(LegacyState &st, cudaStream_t s) {
     uint32_t z0 = mwc_jump_host(kMwcSeedZ, kMwcAz, kMwcMz, st.rng_draws);
     uint32_t w0 = mwc_jump_host(kMwcSeedW, kMwcAw, kMwcMw, st.rng_draws);
-    table_kernel<<<(kLegacyPhotons + 255) / 256, 256, 0, s>>>(st.table, z0, w0);
+    table_kernel<<<(kLegacyPhotons + 255) / 256, 256, 0, s>>>(st.table, z0, w0); note_launch();
     st.rng_draws += 3ull * kLegacyPhotons;
     st.table_written = true;
     return cudaGetLastError();
@@ -563,17 +564,17 @@ cudaError_t legacy_emit(LegacyState &st, float anim_time, int flags, cudaStream_
     uint32_t w0 = mwc_jump_host(kMwcSeedW, kMwcAw, kMwcMw, st.rng_draws);
     const int blocks = (kLegacyPhotons + 255) / 256;
     emit_kernel<<<blocks, 256, 0, s>>>(sc, st.table, media, z0, w0, st.counts, nullptr, nullptr,
-                                       nullptr, nullptr);
+                                       nullptr, nullptr); note_launch();
     cudaError_t e = exclusive_scan_u32(st.counts, st.offsets, kLegacyPhotons, st.total, s);
     if (e != cudaSuccess) return e;
     emit_kernel<<<blocks, 256, 0, s>>>(sc, st.table, media, z0, w0, st.counts, st.offsets, st.keys,
-                                       st.idx, st.dep);
+                                       st.idx, st.dep); note_launch();
     uint32_t *sk = nullptr, *si = nullptr;
     e = radix_sort_pairs_u32(st.keys, st.idx, st.keys_tmp, st.idx_tmp, st.total, kLegacyMaxDeposits,
                              0, 16, st.hist, s, &sk, &si);
     if (e != cudaSuccess) return e;
     reduce_kernel<<<(kLegacyVoxels + 255) / 256, 256, 0, s>>>(sk, si, st.dep, st.total, st.grid3,
-                                                             st.grid4);
+                                                             st.grid4); note_launch();
     if (media) st.rng_draws += 9ull * kLegacyPhotons;
     return cudaGetLastError();
 }
@@ -585,7 +586,7 @@ cudaError_t legacy_render(const LegacyState &st, uchar4 *out, unsigned width, un
     if (n == 0) return cudaSuccess;
     render_kernel<<<(n + 255) / 256, 256, 0, s>>>(sc, st.grid4, out, width, height,
                                                   (flags & kLegacyInterpolate) != 0,
-                                                  (flags & kLegacyMedia) != 0, rgb_out);
+                                                  (flags & kLegacyMedia) != 0, rgb_out); note_launch();
     return cudaGetLastError();
 }
 
@@ -593,7 +594,7 @@ cudaError_t legacy_upload_grid(LegacyState &st, const float *host_grid3, cudaStr
     cudaError_t e = cudaMemcpyAsync(st.grid3, host_grid3, sizeof(float) * 3 * kLegacyVoxels,
                                     cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
-    grid_from_host_kernel<<<(kLegacyVoxels + 255) / 256, 256, 0, s>>>(st.grid3, st.grid4);
+    grid_from_host_kernel<<<(kLegacyVoxels + 255) / 256, 256, 0, s>>>(st.grid3, st.grid4); note_launch();
     return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 // installation, photon emission, kd-tree build, render and queries.
 #include "gather.cuh"
 #include "kdtree.cuh"
+#include "launch_count.cuh"
 #include "pm_ctx.cuh"
 #include "radix_sort.cuh"
 #include "scene.cuh"
@@ -18,9 +19,9 @@ struct PhysicalState {
     float *het = nullptr;
     uint32_t path_cap = 0;
     int mb = 0;
-    float4 *slot[4] = {nullptr, nullptr, nullptr, nullptr};  // spos, spow, vpos, vpow
-    uint32_t *cnt[2] = {nullptr, nullptr};
-    uint32_t *off = nullptr, *scan_tmp = nullptr;
+    uint32_t *cnt[2] = {nullptr, nullptr};  // records per path, per map
+    uint32_t *off[2] = {nullptr, nullptr};  // exclusive scans of cnt
+    uint32_t *scan_tmp = nullptr;
     uint32_t *words = nullptr;  // [0] path counter [1] stored_s [2] stored_v [3] total [4..7] extents
     struct Map {
         float4 *pos = nullptr, *pow = nullptr, *tpos = nullptr, *tpow = nullptr;
@@ -54,9 +55,8 @@ cudaError_t dalloc(T **p, size_t count) {
 void free_state(PhysicalState *st) {
     if (!st) return;
     cudaFree(st->het);
-    for (auto &p : st->slot) cudaFree(p);
     for (auto &p : st->cnt) cudaFree(p);
-    cudaFree(st->off);
+    for (auto &p : st->off) cudaFree(p);
     cudaFree(st->scan_tmp);
     cudaFree(st->words);
     for (auto &m : st->map) {
@@ -109,18 +109,16 @@ pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg)
     memset(&st->stats, 0, sizeof(st->stats));
     cudaDeviceGetAttribute(&st->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
     const uint32_t tmax = std::max(cfg->surface_photons, cfg->volume_photons);
-    uint64_t cap = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 8u;
+    uint64_t cap = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 16u;
     cap = std::max<uint64_t>(cap, 1024);
-    if (cap * (uint64_t)cfg->max_bounces > 0xFFFFFFFFull) return fail(ctx, PM_ERR_LIMIT, "too many photon slots");
+    if (cap > 0xFFFFFFFFull) return fail(ctx, PM_ERR_LIMIT, "path cap above 2^32");
     if (tmax > (1u << 28)) return fail(ctx, PM_ERR_LIMIT, "map target above 2^28 records");
     st->path_cap = (uint32_t)cap;
     st->mb = cfg->max_bounces;
-    const size_t slots = (size_t)st->path_cap * st->mb;
     cudaError_t e = cudaSuccess;
 #define PM_TRY(x) do { e = (x); if (e != cudaSuccess) { physical_free(ctx); return check_cuda(ctx, e, #x); } } while (0)
-    for (auto &p : st->slot) PM_TRY(dalloc(&p, slots));
     for (auto &p : st->cnt) PM_TRY(dalloc(&p, st->path_cap));
-    PM_TRY(dalloc(&st->off, st->path_cap));
+    for (auto &p : st->off) PM_TRY(dalloc(&p, st->path_cap));
     PM_TRY(dalloc(&st->scan_tmp, scan_tile_count(st->path_cap) + 1));
     PM_TRY(dalloc(&st->words, 16));
     PM_TRY(cudaMemset(st->words, 0, 16 * sizeof(uint32_t)));
@@ -155,6 +153,28 @@ pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg)
     return PM_OK;
 }
 
+pm_status pm_update_scene(pm_ctx *ctx, const pm_scene *scene) {
+    if (!ctx || !scene) return PM_ERR_INVALID;
+    PhysicalState *st = ctx->phys;
+    if (!st) return fail(ctx, PM_ERR_STATE, "pm_update_scene before pm_set_scene");
+    std::string why;
+    pm_status s = validate(*scene, st->cfg, &why);
+    if (s != PM_OK) return fail(ctx, s, why);
+    if (scene->het_res != st->scene.het_res)
+        return fail(ctx, PM_ERR_INVALID, "het_res differs from the installed scene");
+    DeviceGuard g(ctx->device);
+    const bool regen = scene->het_res > 0 &&
+                       (scene->het_min != st->scene.het_min || scene->het_max != st->scene.het_max);
+    st->scene = *scene;
+    if (regen) {
+        cudaError_t e = make_noise_grid(st->het, scene->het_res, st->cfg.seed ^ 0x6E6F697365ull,
+                                        scene->het_min, scene->het_max, 0);
+        if (e != cudaSuccess) return check_cuda(ctx, e, "make_noise_grid");
+    }
+    st->dscene = to_device_scene(*scene, st->het);
+    return PM_OK;
+}
+
 pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream) {
     if (!ctx) return PM_ERR_INVALID;
     PhysicalState *st = ctx->phys;
@@ -163,10 +183,9 @@ pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream) {
     cudaError_t e;
 #define PM_TRY(x) do { e = (x); if (e != cudaSuccess) return check_cuda(ctx, e, #x); } while (0)
     PM_TRY(cudaEventRecord(st->ev[0], stream));
-    PM_TRY(cudaMemsetAsync(st->cnt[0], 0, sizeof(uint32_t) * st->path_cap, stream));
-    PM_TRY(cudaMemsetAsync(st->cnt[1], 0, sizeof(uint32_t) * st->path_cap, stream));
     PM_TRY(cudaMemsetAsync(st->words, 0, 16 * sizeof(uint32_t), stream));
     TraceParams P;
+    memset(&P, 0, sizeof(P));
     P.seed = st->cfg.seed;
     P.scene_id = st->cfg.scene_id;
     P.max_bounces = st->mb;
@@ -177,21 +196,30 @@ pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream) {
     P.path_counter = st->words + 0;
     P.stored_s = st->words + 1;
     P.stored_v = st->words + 2;
-    P.spos = st->slot[0]; P.spow = st->slot[1];
-    P.vpos = st->slot[2]; P.vpow = st->slot[3];
-    P.cnt_s = st->cnt[0]; P.cnt_v = st->cnt[1];
+    P.cnt_s = st->cnt[0];
+    P.cnt_v = st->cnt[1];
+    // counting pass: every issued path writes its two counts
     PM_TRY(trace_photons(st->dscene, P, st->sm_count, stream));
     uint32_t counter = 0;
     PM_TRY(cudaMemcpyAsync(&counter, st->words, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
     PM_TRY(cudaStreamSynchronize(stream));
     const uint32_t issued = std::min(counter, st->path_cap);
     for (int m = 0; m < 2; ++m) {
-        auto &mp = st->map[m];
         const uint32_t target = m == 0 ? st->cfg.surface_photons : st->cfg.volume_photons;
-        PM_TRY(compact_map(issued, st->cnt[m], st->off, st->words + 3, st->scan_tmp, target,
-                           st->words + 4 + 2 * m, st->slot[2 * m], st->slot[2 * m + 1], st->mb,
-                           st->scene.light_power, mp.pos, mp.pow, stream));
+        PM_TRY(map_extent(issued, st->cnt[m], st->off[m], st->words + 3, st->scan_tmp, target,
+                          st->words + 4 + 2 * m, stream));
     }
+    // writing pass over the paths the maps need
+    PM_TRY(cudaMemsetAsync(st->words, 0, sizeof(uint32_t), stream));
+    P.store = 1;
+    P.off_s = st->off[0];
+    P.off_v = st->off[1];
+    P.ext_s = st->words + 4;
+    P.ext_v = st->words + 6;
+    P.power = st->scene.light_power;
+    P.spos = st->map[0].pos; P.spow = st->map[0].pow;
+    P.vpos = st->map[1].pos; P.vpow = st->map[1].pow;
+    PM_TRY(trace_photons(st->dscene, P, st->sm_count, stream));
     uint32_t ext[4];
     PM_TRY(cudaMemcpyAsync(ext, st->words + 4, sizeof(ext), cudaMemcpyDeviceToHost, stream));
     PM_TRY(cudaEventRecord(st->ev[1], stream));
@@ -385,6 +413,8 @@ pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *
     st->emitted = true;
     return PM_OK;
 }
+
+unsigned long long pm_kernel_launches(void) { return launch_counter().load(); }
 
 size_t pm_abi_struct_size(int which) {
     switch (which) {

@@ -1,4 +1,5 @@
 // radix_sort.cu -- stable LSD radix sort and single-CTA exclusive scan.
+#include "launch_count.cuh"
 #include "radix_sort.cuh"
 
 namespace pm {
@@ -161,10 +162,10 @@ cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
     uint32_t ntiles = (max_n + kSortTile - 1) / kSortTile;
     if (ntiles == 0) ntiles = 1;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        hist_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, n_dev, shift, hist, ntiles);
-        scan_kernel<<<1, kScanThreads, 0, stream>>>(hist, hist, 256u * ntiles, nullptr);
+        hist_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, n_dev, shift, hist, ntiles); note_launch();
+        scan_kernel<<<1, kScanThreads, 0, stream>>>(hist, hist, 256u * ntiles, nullptr); note_launch();
         scatter_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n_dev, shift,
-                                                               hist, ntiles);
+                                                               hist, ntiles); note_launch();
         K *tk = kin; kin = kout; kout = tk;
         uint32_t *tv = vin; vin = vout; vout = tv;
     }
@@ -200,15 +201,15 @@ cudaError_t exclusive_scan_u32_large(const uint32_t *in, uint32_t *out, uint32_t
                                      uint32_t *total, uint32_t *tmp, cudaStream_t stream) {
     if (n <= 65536) return exclusive_scan_u32(in, out, n, total, stream);
     uint32_t tiles = scan_tile_count(n);
-    tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(in, n, tmp);
-    scan_kernel<<<1, kScanThreads, 0, stream>>>(tmp, tmp, tiles, total);
-    tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(in, out, n, tmp);
+    tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(in, n, tmp); note_launch();
+    scan_kernel<<<1, kScanThreads, 0, stream>>>(tmp, tmp, tiles, total); note_launch();
+    tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(in, out, n, tmp); note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total,
                                cudaStream_t stream) {
-    scan_kernel<<<1, kScanThreads, 0, stream>>>(in, out, n, total);
+    scan_kernel<<<1, kScanThreads, 0, stream>>>(in, out, n, total); note_launch();
     return cudaGetLastError();
 }
 

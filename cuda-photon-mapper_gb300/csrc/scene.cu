@@ -1,5 +1,6 @@
 // scene.cu -- benchmark scene presets (host) and the heterogeneous-medium
 // noise grid (device).
+#include "launch_count.cuh"
 #include "pm.h"
 #include "phys_common.cuh"
 #include "scene.cuh"
@@ -249,7 +250,7 @@ __global__ void noise_kernel(float *grid, int res, uint64_t seed, float lo, floa
 cudaError_t make_noise_grid(float *grid, int res, uint64_t seed, float lo, float hi,
                             cudaStream_t s) {
     int n = res * res * res;
-    noise_kernel<<<(n + 255) / 256, 256, 0, s>>>(grid, res, seed, lo, hi);
+    noise_kernel<<<(n + 255) / 256, 256, 0, s>>>(grid, res, seed, lo, hi); note_launch();
     return cudaGetLastError();
 }
 

@@ -9,10 +9,14 @@
 // (seed) and counted by (path, event, slot, scene), so a path's trajectory
 // does not depend on which warp or lane traced it.
 //
-// Records go to fixed per-path slots (path * max_bounces + k). Compaction
-// then scans the per-path counts and copies, in path order, exactly the
-// map's target number of records into SoA float4 arrays, scaling power by
-// the number of paths the map drew from.
+// Two passes over the same deterministic paths: the counting pass stores
+// nothing and stops issuing paths once both maps are full; a scan of the
+// per-path counts then fixes every record's final index (records in path
+// order, cut at the map's target), and the writing pass retraces exactly
+// the paths the maps need and writes each record straight into the SoA
+// float4 map arrays, its power scaled by the number of paths the map drew
+// from. No per-path staging memory, no compaction copy.
+#include "launch_count.cuh"
 #include "trace.cuh"
 #include "radix_sort.cuh"
 
@@ -43,13 +47,20 @@ __device__ __forceinline__ void start_path(const TraceParams &P, uint32_t id, Pa
     p.nv = 0;
 }
 
-__device__ __forceinline__ void store(float4 *pos, float4 *pw, uint32_t slot, v3 x, v3 thr, v3 d) {
-    pos[slot] = make_float4(x.x, x.y, x.z, 0.0f);
-    pw[slot] = make_float4(thr.x, thr.y, thr.z, __uint_as_float(oct_encode(d)));
+__device__ __forceinline__ void store(float4 *pos, float4 *pw, uint32_t j, v3 x, v3 thr, v3 d,
+                                      float scale) {
+    pos[j] = make_float4(x.x, x.y, x.z, __uint_as_float(j));
+    pw[j] = make_float4(thr.x * scale, thr.y * scale, thr.z * scale, __uint_as_float(oct_encode(d)));
 }
 
+struct MapOut {
+    uint32_t n, paths;
+    float scale;
+};
+
 // One interaction of path p; returns false when the path ends.
-__device__ bool step_path(const PScene &S, const TraceParams &P, Path &p) {
+__device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const MapOut &ms,
+                          const MapOut &mv) {
     p.ev += 1;
     pm_u32x4 r = philox(P.seed, p.id, (uint32_t)p.ev, 0u, P.scene_id);
     float u0 = pm_u01(r.v[0]), u1 = pm_u01(r.v[1]), u2 = pm_u01(r.v[2]), u3 = pm_u01(r.v[3]);
@@ -90,8 +101,10 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p) {
         }
     }
     if (vol) {
-        if (p.nv < (uint32_t)P.max_bounces)
-            store(P.vpos, P.vpow, p.id * (uint32_t)P.max_bounces + p.nv, x, p.thr, p.d);
+        if (P.store) {
+            uint32_t j = P.off_v[p.id] + p.nv;
+            if (j < mv.n) store(P.vpos, P.vpow, j, x, p.thr, p.d, mv.scale);
+        }
         p.nv += 1;
         if (!(u1 < P.rr)) return false;
         float f = (ss / st) / P.rr;
@@ -107,8 +120,10 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p) {
     float dn = dot(n, p.d);
     v3 nf = dn < 0.0f ? n : n * -1.0f;
     if (kind == PM_MAT_DIFFUSE) {
-        if (p.ns < (uint32_t)P.max_bounces)
-            store(P.spos, P.spow, p.id * (uint32_t)P.max_bounces + p.ns, hp, p.thr, p.d);
+        if (P.store) {
+            uint32_t j = P.off_s[p.id] + p.ns;
+            if (j < ms.n) store(P.spos, P.spow, j, hp, p.thr, p.d, ms.scale);
+        }
         p.ns += 1;
         if (!(u1 < P.rr)) return false;
         v3 a = material_albedo(S, h.obj);
@@ -141,22 +156,31 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p) {
 
 __global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) {
     const int lane = threadIdx.x & 31;
+    MapOut ms = {0u, 0u, 0.0f}, mv = {0u, 0u, 0.0f};
+    uint32_t cap = P.path_cap;
+    if (P.store) {
+        ms.n = P.ext_s[0]; ms.paths = P.ext_s[1];
+        mv.n = P.ext_v[0]; mv.paths = P.ext_v[1];
+        ms.scale = ms.paths ? P.power / (float)ms.paths : 0.0f;
+        mv.scale = mv.paths ? P.power / (float)mv.paths : 0.0f;
+        cap = max(ms.paths, mv.paths);
+    }
     Path p;
     bool live = false;
     for (;;) {
         unsigned empty = __ballot_sync(0xffffffffu, !live);
         if (empty) {
             const int leader = __ffs(empty) - 1;
-            uint32_t base = P.path_cap;
+            uint32_t base = cap;
             if (lane == leader) {
-                bool full = *((volatile uint32_t *)P.stored_s) >= P.target_s &&
+                bool full = !P.store && *((volatile uint32_t *)P.stored_s) >= P.target_s &&
                             *((volatile uint32_t *)P.stored_v) >= P.target_v;
                 if (!full) base = atomicAdd(P.path_counter, (uint32_t)__popc(empty));
             }
             base = __shfl_sync(0xffffffffu, base, leader);
             if (!live) {
                 uint32_t id = base + (uint32_t)__popc(empty & lanemask_lt());
-                if (base < P.path_cap && id < P.path_cap) {
+                if (base < cap && id < cap) {
                     start_path(P, id, p, S);
                     live = true;
                 }
@@ -164,12 +188,15 @@ __global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) {
         }
         if (!__any_sync(0xffffffffu, live)) break;
         if (live) {
-            if (!step_path(S, P, p)) {
-                uint32_t ns = min(p.ns, (uint32_t)P.max_bounces), nv = min(p.nv, (uint32_t)P.max_bounces);
-                P.cnt_s[p.id] = ns;
-                P.cnt_v[p.id] = nv;
-                if (ns) atomicAdd(P.stored_s, ns);
-                if (nv) atomicAdd(P.stored_v, nv);
+            if (!step_path(S, P, p, ms, mv)) {
+                if (!P.store) {
+                    uint32_t ns = min(p.ns, (uint32_t)P.max_bounces);
+                    uint32_t nv = min(p.nv, (uint32_t)P.max_bounces);
+                    P.cnt_s[p.id] = ns;
+                    P.cnt_v[p.id] = nv;
+                    if (ns) atomicAdd(P.stored_s, ns);
+                    if (nv) atomicAdd(P.stored_v, nv);
+                }
                 live = false;
             }
         }
@@ -199,42 +226,20 @@ __global__ void map_extent_kernel(const uint32_t *off, const uint32_t *cnt, uint
     extent[1] = lo + 1;
 }
 
-__global__ void compact_kernel(const uint32_t *off, const uint32_t *cnt, const uint32_t *extent,
-                               const float4 *spos, const float4 *spow, int mb, float power,
-                               float4 *pos, float4 *pw) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t n = extent[0], paths = extent[1];
-    if (p >= paths) return;
-    float scale = power / (float)paths;
-    uint32_t o = off[p], c = cnt[p];
-    for (uint32_t k = 0; k < c; ++k) {
-        uint32_t j = o + k;
-        if (j >= n) break;
-        float4 a = spos[(size_t)p * mb + k];
-        float4 b = spow[(size_t)p * mb + k];
-        pos[j] = make_float4(a.x, a.y, a.z, __uint_as_float(j));
-        pw[j] = make_float4(b.x * scale, b.y * scale, b.z * scale, b.w);
-    }
-}
-
 }  // namespace
 
 cudaError_t trace_photons(const PScene &S, const TraceParams &P, int sm_count, cudaStream_t s) {
     // 4 warps per CTA, enough CTAs to fill every SM several times over.
-    trace_kernel<<<sm_count * 8, 128, 0, s>>>(S, P);
+    trace_kernel<<<sm_count * 8, 128, 0, s>>>(S, P); note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t compact_map(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint32_t *total,
-                        uint32_t *scan_tmp, uint32_t target, uint32_t *extent, const float4 *spos,
-                        const float4 *spow, int mb, float power, float4 *pos, float4 *pw,
-                        cudaStream_t s) {
+cudaError_t map_extent(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint32_t *total,
+                       uint32_t *scan_tmp, uint32_t target, uint32_t *extent, cudaStream_t s) {
     if (issued == 0) return cudaMemsetAsync(extent, 0, 2 * sizeof(uint32_t), s);
     cudaError_t e = exclusive_scan_u32_large(cnt, off, issued, total, scan_tmp, s);
     if (e != cudaSuccess) return e;
-    map_extent_kernel<<<1, 1, 0, s>>>(off, cnt, issued, total, target, extent);
-    compact_kernel<<<(issued + 255) / 256, 256, 0, s>>>(off, cnt, extent, spos, spow, mb, power,
-                                                        pos, pw);
+    map_extent_kernel<<<1, 1, 0, s>>>(off, cnt, issued, total, target, extent); note_launch();
     return cudaGetLastError();
 }
 

@@ -12,24 +12,28 @@ struct TraceParams {
     uint32_t scene_id;
     int max_bounces;
     float rr;                     // Russian-roulette survival probability
-    uint32_t target_s, target_v;  // map targets: stop issuing paths once both are reached
-    uint32_t path_cap;            // slots exist for this many paths
-    uint32_t *path_counter;       // next path id
+    uint32_t target_s, target_v;  // map targets: counting stops issuing paths once both are met
+    uint32_t path_cap;            // counting pass: most paths that may be issued
+    uint32_t *path_counter;       // next path id (zeroed before each pass)
     uint32_t *stored_s, *stored_v;
-    float4 *spos, *spow;          // surface slots [path_cap * max_bounces]
-    float4 *vpos, *vpow;          // volume slots
-    uint32_t *cnt_s, *cnt_v;      // records per path (zeroed before the launch)
+    uint32_t *cnt_s, *cnt_v;      // records per path (zeroed before the counting pass)
+    // Writing pass (store != 0): paths [0, max(ext_s[1], ext_v[1])) again,
+    // each record written straight to map index off[p] + k when below the
+    // map size ext[0], power scaled by power / ext[1].
+    int store;
+    const uint32_t *off_s, *off_v;
+    const uint32_t *ext_s, *ext_v;
+    float power;
+    float4 *spos, *spow, *vpos, *vpow;
 };
 
+// One persistent launch over the photon paths (counting or writing pass).
 cudaError_t trace_photons(const PScene &S, const TraceParams &P, int sm_count, cudaStream_t s);
 
-// Scans the per-path counts of the first `issued` paths, finds how many
-// paths reach `target` records (extent[0] = records, extent[1] = paths, on
-// the device) and copies those records in path order to pos/pw, with the
-// record index in pos.w and power scaled by power / paths.
-cudaError_t compact_map(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint32_t *total,
-                        uint32_t *scan_tmp, uint32_t target, uint32_t *extent, const float4 *spos,
-                        const float4 *spow, int mb, float power, float4 *pos, float4 *pw,
-                        cudaStream_t s);
+// Scans the per-path counts of the first `issued` paths into off and finds
+// how many paths reach `target` records: extent[0] = records, extent[1] =
+// paths (device).
+cudaError_t map_extent(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint32_t *total,
+                       uint32_t *scan_tmp, uint32_t target, uint32_t *extent, cudaStream_t s);
 
 }  // namespace pm

@@ -101,6 +101,7 @@ PROTOTYPES = {
     "pm_legacy_rng_draws": (_i, [_vp, _c.POINTER(_c.c_ulonglong)]),
     "pm_preset": (_i, [_i, _c.c_uint64, _c.POINTER(Scene), _c.POINTER(Config)]),
     "pm_set_scene": (_i, [_vp, _c.POINTER(Scene), _c.POINTER(Config)]),
+    "pm_update_scene": (_i, [_vp, _c.POINTER(Scene)]),
     "pm_emit": (_i, [_vp, _vp]),
     "pm_build": (_i, [_vp, _vp]),
     "pm_render": (_i, [_vp, _vp, _vp, _vp]),
@@ -110,6 +111,7 @@ PROTOTYPES = {
     "pm_get_stats": (_i, [_vp, _c.POINTER(FrameStats)]),
     "pm_abi_struct_size": (_c.c_size_t, [_i]),
     "pm_set_photons": (_i, [_vp, _i, _vp, _vp, _c.c_uint32]),
+    "pm_kernel_launches": (_c.c_ulonglong, []),
 }
 
 _lib = None
@@ -204,6 +206,10 @@ class Context:
     def set_scene(self, scene, cfg):
         self.scene, self.cfg = scene, cfg
         self._check(self.lib.pm_set_scene(self.h, _c.byref(scene), _c.byref(cfg)), "pm_set_scene")
+
+    def update_scene(self, scene):
+        self.scene = scene
+        self._check(self.lib.pm_update_scene(self.h, _c.byref(scene)), "pm_update_scene")
 
     def emit(self, stream=0):
         self._check(self.lib.pm_emit(self.h, stream), "pm_emit")

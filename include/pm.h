@@ -194,6 +194,11 @@ PM_API pm_status pm_preset(int preset, uint64_t seed, pm_scene *scene, pm_config
 
 /* Installs a scene and configuration (copies both); allocates the maps. */
 PM_API pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg);
+/* Replaces the scene of the next frame (geometry, materials, light, medium
+ * coefficients, camera) without reallocating: sphere and plane counts may
+ * change, het_res may not. The per-frame counterpart of the reference's
+ * positionObjects(animTime) (photonMappingKernel.cu:1380-1404). */
+PM_API pm_status pm_update_scene(pm_ctx *ctx, const pm_scene *scene);
 /* Traces photon paths until both maps reach their targets. Synchronises
  * the stream once to learn the map sizes. */
 PM_API pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream);
@@ -224,6 +229,9 @@ PM_API pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out);
  * (its box bounds the Morton codes); follow with pm_build. */
 PM_API pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *pow,
                                 uint32_t n);
+
+/* Kernels this library has launched since it was loaded (all contexts). */
+PM_API unsigned long long pm_kernel_launches(void);
 
 /* sizeof of the ABI structs as this library was compiled (0 = pm_scene,
  * 1 = pm_config, 2 = pm_photon_record, 3 = pm_frame_stats), for bindings

@@ -93,6 +93,8 @@ def _phys_protos(lib):
     lib.pmo_knn.restype = None
     lib.pmo_render.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp]
     lib.pmo_render.restype = None
+    lib.pmo_render_timed.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp, vp]
+    lib.pmo_render_timed.restype = None
     lib.pmo_noise_grid.argtypes = [vp, i, ctypes.c_uint64, f, f]
     lib.pmo_noise_grid.restype = None
     lib.pmo_philox.argtypes = [ctypes.c_uint64, vp, vp]
@@ -176,6 +178,21 @@ def knn(pos, queries, k, radius):
     phys_lib().pmo_knn(pos.ctypes.data, len(pos), q.ctypes.data, len(q), k, radius,
                        idx.ctypes.data, d2.ctypes.data)
     return idx, d2
+
+
+def render_timed(scene, cfg, het, maps, pixels):
+    """float32 render of `pixels`; returns (radiance, gathers[2], seconds[2]
+    = neighbour-grid build, shading)."""
+    pixels = np.ascontiguousarray(pixels, np.uint32)
+    out = np.zeros((len(pixels), 4), np.float32)
+    gathers = np.zeros(2, np.uint64)
+    secs = np.zeros(2, np.float64)
+    phys_lib().pmo_render_timed(ctypes.byref(scene), ctypes.byref(cfg), _ptr(het),
+                                maps.spos.ctypes.data, maps.spow.ctypes.data, len(maps.spos),
+                                maps.vpos.ctypes.data, maps.vpow.ctypes.data, len(maps.vpos),
+                                pixels.ctypes.data, len(pixels), out.ctypes.data,
+                                gathers.ctypes.data, secs.ctypes.data)
+    return out, gathers, secs
 
 
 def render(scene, cfg, het, maps, pixels=None, double=False):

@@ -21,6 +21,7 @@
 #include "physical_oracle.h"
 
 #include <math.h>
+#include <omp.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -370,7 +371,7 @@ int pmo_emit(const pmo_scene *scene, const pmo_config *cfg, const float *het, fl
     uint32_t n[2] = {0, 0}, np[2] = {0, 0};
     int done[2] = {targets[0] == 0, targets[1] == 0};
     uint32_t tmax = targets[0] > targets[1] ? targets[0] : targets[1];
-    uint64_t cap64 = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 8u;
+    uint64_t cap64 = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 16u;
     if (cap64 < 1024) cap64 = 1024;
     uint32_t cap = (uint32_t)cap64;
     for (uint32_t id = 0; id < cap && !(done[0] && done[1]); ++id) {
@@ -609,7 +610,7 @@ static v3 shade(const render_ctx *R, uint32_t pix, uint64_t *counts) {
             box_span(s, o, d, &t0, &t1);
             t1 = fminf(t1, tend);
             if (t0 < t1) {
-                int nst = (int)ceilf((t1 - t0) / c->march_step);
+                int nst = (int)fminf(ceilf((t1 - t0) / c->march_step), 65536.0f);
                 v3 wo = scl(d, -1.0f);
                 for (int j = 0; j < nst; ++j) {
                     float ta = t0 + (float)j * c->march_step;
@@ -687,6 +688,15 @@ void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,
                 const float (*spos)[4], const float (*spow)[4], uint32_t ns,
                 const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
                 const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers) {
+    pmo_render_timed(scene, cfg, het, spos, spow, ns, vpos, vpow, nv, pixels, npix, out, gathers, NULL);
+}
+
+void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                      const float (*spos)[4], const float (*spow)[4], uint32_t ns,
+                      const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
+                      const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers,
+                      double *seconds) {
+    double t0 = omp_get_wtime();
     render_ctx R;
     R.s = scene;
     R.c = cfg;
@@ -695,6 +705,7 @@ void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,
     R.ns = ns; R.nv = nv;
     R.gs = pmo_grid_build(spos, ns, cfg->radius);
     R.gv = pmo_grid_build(vpos, nv, cfg->radius);
+    double t1 = omp_get_wtime();
     uint64_t total[2] = {0, 0};
 #pragma omp parallel
     {
@@ -708,6 +719,7 @@ void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,
         { total[0] += local[0]; total[1] += local[1]; }
     }
     if (gathers) { gathers[0] = total[0]; gathers[1] = total[1]; }
+    if (seconds) { seconds[0] = t1 - t0; seconds[1] = omp_get_wtime() - t1; }
     pmo_grid_free(R.gs);
     pmo_grid_free(R.gv);
 }

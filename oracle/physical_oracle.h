@@ -72,6 +72,13 @@ void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,
                 const float (*spos)[4], const float (*spow)[4], uint32_t ns,
                 const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
                 const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers);
+/* pmo_render with seconds[0] = neighbour-grid build time, seconds[1] =
+ * shading time (all threads). */
+void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                      const float (*spos)[4], const float (*spow)[4], uint32_t ns,
+                      const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
+                      const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers,
+                      double *seconds);
 void pmo_noise_grid(float *grid, int res, uint64_t seed, float lo, float hi);
 void pmo_philox(uint64_t seed, const uint32_t *ctr, uint32_t *out);
 float pmo_logf(float x);

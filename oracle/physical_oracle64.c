@@ -280,7 +280,7 @@ int pmo64_emit(const pmo_scene *scene, const pmo_config *cfg, const float *het, 
     uint32_t n[2] = {0, 0}, np[2] = {0, 0};
     int done[2] = {targets[0] == 0, targets[1] == 0};
     uint32_t tmax = targets[0] > targets[1] ? targets[0] : targets[1];
-    uint64_t cap = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 8u;
+    uint64_t cap = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 16u;
     if (cap < 1024) cap = 1024;
     for (uint32_t id = 0; id < cap && !(done[0] && done[1]); ++id) {
         uint32_t cs, cv;
@@ -402,7 +402,7 @@ static d3 shade(const pmo_scene *s, const pmo_config *c, const float *het, const
             box_span(s, o, d, &t0, &t1);
             t1 = fmin(t1, tend);
             if (t0 < t1) {
-                int nst = (int)ceil((t1 - t0) / c->march_step);
+                int nst = (int)fmin(ceil((t1 - t0) / c->march_step), 65536.0);
                 for (int j = 0; j < nst; ++j) {
                     double ta = t0 + (double)j * c->march_step;
                     double tb = fmin(t0 + (double)(j + 1) * c->march_step, t1);

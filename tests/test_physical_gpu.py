@@ -112,6 +112,7 @@ def test_knn_ties_broken_by_index(ctx):
     perm = rs.permutation(len(g))
     pos = np.zeros((len(g), 4), np.float32)
     pos[:, :3] = g[perm]
+    pos[:, 3] = np.arange(len(g), dtype=np.uint32).view(np.float32)  # record index bits
     pw = np.ones((len(g), 4), np.float32)
     ctx.set_photons(0, pos, pw)
     ctx.build()
@@ -138,6 +139,7 @@ def test_knn_empty_and_tiny_maps(ctx):
     for n in (0, 1, 5, 33):
         pos = np.zeros((n, 4), np.float32)
         pos[:, 0] = np.linspace(-0.1, 0.1, n)
+        pos[:, 3] = np.arange(n, dtype=np.uint32).view(np.float32)
         ctx.set_photons(1, pos, np.ones((n, 4), np.float32))
         ctx.build()
         ctx.knn(1, q.data_ptr(), 4, 8, 0.5, idx.data_ptr(), d2.data_ptr())
