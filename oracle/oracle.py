@@ -117,6 +117,12 @@ def _phys_protos(lib):
     lib.pmo64_render.restype = None
     lib.pmo_trace_path.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]
     lib.pmo_trace_path.restype = None
+    lib.pmo_sample.argtypes = [i, vp, f, f, f, vp]
+    lib.pmo_sample.restype = None
+    lib.pmo_fresnel.argtypes = [f, f]
+    lib.pmo_fresnel.restype = f
+    lib.pmo_hg_phase.argtypes = [f, f]
+    lib.pmo_hg_phase.restype = f
 
 
 def phys_lib():
@@ -214,4 +220,19 @@ def render(scene, cfg, het, maps, pixels=None, double=False):
                    maps.spow.ctypes.data, len(maps.spos), maps.vpos.ctypes.data,
                    maps.vpow.ctypes.data, len(maps.vpos), pixels.ctypes.data, len(pixels),
                    out.ctypes.data, gathers.ctypes.data)
+    return out
+
+
+def sample(which, n, g=0.0, direction=(0.0, 0.0, 1.0), seed=0):
+    """n directions from sampler `which` (0 sphere, 1 cosine, 2 HG) with
+    uniforms from a seeded numpy stream."""
+    lib = phys_lib()
+    rs = np.random.RandomState(seed)
+    u = rs.randint(0, 1 << 24, size=(n, 2)).astype(np.float64) / float(1 << 24)
+    d = np.asarray(direction, np.float32)
+    out = np.zeros((n, 3), np.float32)
+    o = np.zeros(3, np.float32)
+    for i in range(n):
+        lib.pmo_sample(which, d.ctypes.data, g, float(u[i, 0]), float(u[i, 1]), o.ctypes.data)
+        out[i] = o
     return out

@@ -771,3 +771,19 @@ uint32_t pmo_oct_encode(const float *d) { return oct_encode(mk(d[0], d[1], d[2])
 void pmo_oct_decode(uint32_t e, float *d) { v3 v = oct_decode(e); d[0] = v.x; d[1] = v.y; d[2] = v.z; }
 size_t pmo_sizeof_scene(void) { return sizeof(pmo_scene); }
 size_t pmo_sizeof_config(void) { return sizeof(pmo_config); }
+
+/* Samplers exposed for distribution tests. */
+void pmo_sample(int which, const float *dir, float g, float u1, float u2, float *out) {
+    v3 r;
+    if (which == 0) r = sample_sphere(u1, u2);
+    else if (which == 1) r = sample_cosine(mk(dir[0], dir[1], dir[2]), u1, u2);
+    else r = sample_hg(mk(dir[0], dir[1], dir[2]), g, u1, u2);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
+float pmo_fresnel(float ci, float eta) {
+    float ct;
+    return fresnel(ci, eta, &ct);
+}
+
+float pmo_hg_phase(float g, float c) { return hg_phase(g, c); }

@@ -86,6 +86,10 @@ float pmo_expf(float x);
 void pmo_sincos2pi(float u, float *s, float *c);
 uint32_t pmo_oct_encode(const float *d);
 void pmo_oct_decode(uint32_t e, float *d);
+/* which: 0 uniform sphere, 1 cosine hemisphere around dir, 2 HG(g) around dir */
+void pmo_sample(int which, const float *dir, float g, float u1, float u2, float *out);
+float pmo_fresnel(float ci, float eta);
+float pmo_hg_phase(float g, float c);
 size_t pmo_sizeof_scene(void);
 size_t pmo_sizeof_config(void);
 
