@@ -17,9 +17,13 @@ namespace pm {
 namespace {
 
 __global__ void morton_kernel(const float4 *__restrict__ pos, uint32_t n, float3 lo, float3 hi,
-                              uint64_t *keys, uint32_t *vals) {
+                              const float *box_dev, uint64_t *keys, uint32_t *vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (box_dev) {
+        lo = make_float3(box_dev[0], box_dev[1], box_dev[2]);
+        hi = make_float3(box_dev[3], box_dev[4], box_dev[5]);
+    }
     float4 p = pos[i];
     uint64_t c = spread21(quantize21(p.x, lo.x, hi.x)) |
                  (spread21(quantize21(p.y, lo.y, hi.y)) << 1) |
@@ -35,7 +39,7 @@ __global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
     if (i >= n) return;
     uint32_t s = order[i];
     pos_out[i] = pos_in[s];
-    pow_out[i] = pow_in[s];
+    if (pow_in) pow_out[i] = pow_in[s];
 }
 
 // One warp per leaf slot: box of its (up to) 32 records.
@@ -105,7 +109,8 @@ size_t tree_nodes(uint32_t n) { return (size_t)2 << tree_depth(n); }
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     const uint32_t n = a.n;
     if (n == 0) return cudaSuccess;
-    morton_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.pos_in, n, a.lo, a.hi, a.keys, a.vals); note_launch();
+    morton_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.pos_in, n, a.lo, a.hi, a.box_dev, a.keys,
+                                                   a.vals); note_launch();
     uint64_t *sk = nullptr;
     uint32_t *sv = nullptr;
     cudaError_t e = radix_sort_pairs_u64(a.keys, a.vals, a.keys_tmp, a.vals_tmp, a.n_dev, n, 0, 64,

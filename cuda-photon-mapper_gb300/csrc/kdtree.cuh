@@ -13,8 +13,9 @@ struct KdBuildArgs {
     uint32_t n;                 // records
     const uint32_t *n_dev;      // the same count in device memory
     float3 lo, hi;              // Morton quantisation box
-    const float4 *pos_in, *pow_in;   // records in index order
-    float4 *pos_out, *pow_out;       // records in tree order
+    const float *box_dev;       // nullable: lo/hi read from device memory (6 floats)
+    const float4 *pos_in, *pow_in;   // records in index order (pow_in nullable)
+    float4 *pos_out, *pow_out;       // records in tree order (pow_out nullable)
     float4 *node_lo, *node_hi;       // tree_nodes(n) boxes
     uint64_t *keys, *keys_tmp;       // n each
     uint32_t *vals, *vals_tmp;       // n each

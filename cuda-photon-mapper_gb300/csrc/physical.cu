@@ -252,6 +252,7 @@ pm_status pm_build(pm_ctx *ctx, cudaStream_t stream) {
         if (mp.n == 0) { mp.built = true; continue; }
         if (mp.depth > 29) return fail(ctx, PM_ERR_LIMIT, "photon map too large for the tree");
         KdBuildArgs a;
+        a.box_dev = nullptr;
         a.n = mp.n;
         a.n_dev = st->words + 4 + 2 * m;
         a.lo = make_float3(st->scene.box_min[0], st->scene.box_min[1], st->scene.box_min[2]);

@@ -112,6 +112,7 @@ PROTOTYPES = {
     "pm_abi_struct_size": (_c.c_size_t, [_i]),
     "pm_set_photons": (_i, [_vp, _i, _vp, _vp, _c.c_uint32]),
     "pm_kernel_launches": (_c.c_ulonglong, []),
+    "pm_knn_noalloc": (_i, [_vp, _c.c_uint32, _vp, _c.c_uint32, _i, _f, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -230,6 +230,33 @@ PM_API pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out);
 PM_API pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *pow,
                                 uint32_t n);
 
+/* ---- 4. allocation-free k-NN ------------------------------------------------
+ *
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory -- code running inside another framework's memory pool or
+ * stream-ordered allocator, plug-ins whose host forbids device allocation
+ * after start-up, real-time loops that must not risk an allocation stall or
+ * failure -- pm_knn_noalloc answers the same queries as pm_set_photons +
+ * pm_build + pm_knn over n caller-provided points (device float4, xyz; the
+ * point's position in the array is its index for ties and in idx_out) and
+ * calls no cudaMalloc, cudaFree or other allocating routine. Its temporary
+ * memory is one fixed file-scope device array of
+ * PM_KNN_NOALLOC_SCRATCH_BYTES (about 7.3 MiB) that every GPU loading the
+ * library holds until the process exits; n above PM_KNN_NOALLOC_MAX_POINTS
+ * returns PM_ERR_LIMIT.
+ *
+ * The first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call
+ * before any stream capture. All calls share the array and it keeps the
+ * last call's contents, so calls that overlap on the GPU (other streams,
+ * other host threads on the same device) race and must be serialised by the
+ * caller. Needs no pm_ctx. */
+#define PM_KNN_NOALLOC_MAX_POINTS (1u << 17)
+#define PM_KNN_NOALLOC_SCRATCH_BYTES 7635200u
+PM_API pm_status pm_knn_noalloc(const float4 *points, uint32_t n, const float4 *queries,
+                                uint32_t nq, int k, float radius, uint32_t *idx_out,
+                                float *d2_out, cudaStream_t stream);
+
 /* Kernels this library has launched since it was loaded (all contexts). */
 PM_API unsigned long long pm_kernel_launches(void);
 
