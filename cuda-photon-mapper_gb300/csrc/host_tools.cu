@@ -1,0 +1,173 @@
+// host_tools.cu -- host-side utilities around the photon mapper: photon-map
+// files, PPM image output and a headless frame driver with the reference's
+// display()/keyboard() semantics.
+#include "pm.h"
+#include "pm_ctx.cuh"
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+const char kMapMagic[] = "{\"format\": \"pm-photon-map\", \"version\": 1";
+
+}  // namespace
+
+extern "C" {
+
+// File = one JSON header line, then `records` float4 pos followed by
+// `records` float4 pow (the SoA layout of pm_get_photons_soa).
+pm_status pm_save_map(pm_ctx *ctx, int map, const char *path) {
+    if (!ctx || !path || map < 0 || map > 1) return PM_ERR_INVALID;
+    uint32_t n = 0;
+    pm_status s = pm_get_photons_soa(ctx, map, nullptr, nullptr, 0, &n);
+    if (s != PM_OK) return s;
+    std::vector<float4> pos(n), pw(n);
+    s = pm_get_photons_soa(ctx, map, pos.data(), pw.data(), n, &n);
+    if (s != PM_OK) return s;
+    pm_frame_stats st;
+    if (pm_get_stats(ctx, &st) != PM_OK) memset(&st, 0, sizeof(st));
+    FILE *f = fopen(path, "wb");
+    if (!f) return pm::fail(ctx, PM_ERR_INVALID, std::string("cannot open ") + path);
+    fprintf(f,
+            "%s, \"map\": \"%s\", \"records\": %u, \"paths\": %u, \"layout\": \"float4 pos (xyz, "
+            "index bits) x records, float4 pow (rgb flux, octahedral 16:16 direction) x records\"}\n",
+            kMapMagic, map == 0 ? "surface" : "volume", n, st.map_paths[map]);
+    bool ok = fwrite(pos.data(), sizeof(float4), n, f) == n && fwrite(pw.data(), sizeof(float4), n, f) == n;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? PM_OK : pm::fail(ctx, PM_ERR_INVALID, "short write");
+}
+
+pm_status pm_load_map(pm_ctx *ctx, int map, const char *path) {
+    if (!ctx || !path || map < 0 || map > 1) return PM_ERR_INVALID;
+    FILE *f = fopen(path, "rb");
+    if (!f) return pm::fail(ctx, PM_ERR_INVALID, std::string("cannot open ") + path);
+    char line[1024];
+    if (!fgets(line, sizeof(line), f) || strncmp(line, kMapMagic, strlen(kMapMagic)) != 0) {
+        fclose(f);
+        return pm::fail(ctx, PM_ERR_INVALID, "not a photon-map file");
+    }
+    const char *r = strstr(line, "\"records\": ");
+    unsigned n = 0;
+    if (!r || sscanf(r + 11, "%u", &n) != 1) {
+        fclose(f);
+        return pm::fail(ctx, PM_ERR_INVALID, "header without a record count");
+    }
+    std::vector<float4> pos(n), pw(n);
+    bool ok = fread(pos.data(), sizeof(float4), n, f) == n && fread(pw.data(), sizeof(float4), n, f) == n;
+    fclose(f);
+    if (!ok) return pm::fail(ctx, PM_ERR_INVALID, "truncated photon-map file");
+    return pm_set_photons(ctx, map, pos.data(), pw.data(), n);
+}
+
+pm_status pm_write_ppm(const char *path, const uchar4 *rgba, unsigned width, unsigned height) {
+    if (!path || (!rgba && width && height)) return PM_ERR_INVALID;
+    FILE *f = fopen(path, "wb");
+    if (!f) return PM_ERR_INVALID;
+    fprintf(f, "P6\n%u %u\n255\n", width, height);
+    std::vector<unsigned char> row(3 * (size_t)width);
+    bool ok = true;
+    for (unsigned y = 0; y < height && ok; ++y) {
+        for (unsigned x = 0; x < width; ++x) {
+            const uchar4 &p = rgba[(size_t)y * width + x];
+            row[3 * x] = p.x;
+            row[3 * x + 1] = p.y;
+            row[3 * x + 2] = p.z;
+        }
+        ok = fwrite(row.data(), 1, row.size(), f) == row.size();
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? PM_OK : PM_ERR_INVALID;
+}
+
+// ---- headless frame driver (callbacksPBO.cpp:19-27, 47-101, 104-143) --------
+
+struct pm_viewer {
+    pm_viewer_state s;
+    pm_ctx *ctx;
+    bool started;
+};
+
+pm_status pm_viewer_create(pm_viewer **out, unsigned width, unsigned height) {
+    if (!out) return PM_ERR_INVALID;
+    pm_viewer *v = new pm_viewer();
+    memset(&v->s, 0, sizeof(v->s));
+    v->s.width = width;
+    v->s.height = height;
+    v->s.anim_flag = 0;       // animFlag
+    v->s.emit_flag = 1;       // emitFlag
+    v->s.interpolate = 0;     // interpolateFlag
+    v->s.media = 0;           // participatingMediaFlag
+    v->s.iter = 0;
+    v->s.anim_time = 0.0f;
+    v->s.anim_inc = 0.1f;
+    v->ctx = nullptr;
+    v->started = false;
+    *out = v;
+    return PM_OK;
+}
+
+void pm_viewer_destroy(pm_viewer *v) {
+    if (!v) return;
+    pm_destroy(v->ctx);
+    delete v;
+}
+
+void pm_viewer_key(pm_viewer *v, unsigned char key) {
+    if (!v) return;
+    pm_viewer_state &s = v->s;
+    switch (key) {
+        case 27: s.quit = 1; break;  // the reference exits the process here
+        case 'a': case 'A': s.anim_flag = s.anim_flag ? 0 : 1; break;
+        case 'e': case 'E': s.emit_flag = s.emit_flag ? 0 : 1; break;
+        case 'i': case 'I': s.interpolate = !s.interpolate; break;
+        case 'p': case 'P': s.media = !s.media; break;
+        case '-': s.anim_inc = (float)((double)s.anim_inc - 0.01); break;
+        case '+': s.anim_inc = (float)((double)s.anim_inc + 0.01); break;
+        case 'r': s.anim_inc = 0.01f; break;
+        default: break;
+    }
+}
+
+pm_status pm_viewer_state_get(const pm_viewer *v, pm_viewer_state *out) {
+    if (!v || !out) return PM_ERR_INVALID;
+    *out = v->s;
+    return PM_OK;
+}
+
+pm_status pm_viewer_display(pm_viewer *v, uchar4 *pos) {
+    if (!v) return PM_ERR_INVALID;
+    pm_status st;
+    if (!v->started) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) {
+            cudaGetLastError();
+            return PM_ERR_CUDA;
+        }
+        if ((st = pm_create(&v->ctx, dev)) != PM_OK) return st;
+        // initCuda runs one emission before the first display
+        // (simplePBO.cpp:203), before the random table exists.
+        if ((st = pm_legacy_emit(v->ctx, v->s.anim_time, 0, 0)) != PM_OK) return st;
+        v->started = true;
+    }
+    pm_viewer_state &s = v->s;
+    const int flags = (s.interpolate ? PM_LEGACY_INTERPOLATE : 0) | (s.media ? PM_LEGACY_MEDIA : 0);
+    if (s.iter == 0) {
+        if ((st = pm_legacy_init_random(v->ctx, 0)) != PM_OK) return st;
+        s.iter++;
+    }
+    if (s.emit_flag && (st = pm_legacy_emit(v->ctx, s.anim_time, flags, 0)) != PM_OK) return st;
+    if ((st = pm_legacy_render(v->ctx, pos, s.width, s.height, s.anim_time, flags, nullptr, 0)) != PM_OK)
+        return st;
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return PM_ERR_CUDA;
+    }
+    s.frames++;
+    if (s.anim_flag) s.anim_time += s.anim_inc;
+    return PM_OK;
+}
+
+}  // extern "C"

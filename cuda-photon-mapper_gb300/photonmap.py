@@ -69,6 +69,13 @@ class FrameStats(_c.Structure):
     ]
 
 
+class ViewerState(_c.Structure):
+    _fields_ = [("width", _c.c_uint), ("height", _c.c_uint), ("anim_flag", _c.c_int),
+                ("emit_flag", _c.c_int), ("interpolate", _c.c_int), ("media", _c.c_int),
+                ("iter", _c.c_int), ("quit", _c.c_int), ("anim_time", _c.c_float),
+                ("anim_inc", _c.c_float), ("frames", _c.c_ulonglong)]
+
+
 MAP_SURFACE = 0
 MAP_VOLUME = 1
 MAT_DIFFUSE, MAT_MIRROR, MAT_DIELECTRIC = 0, 1, 2
@@ -113,6 +120,14 @@ PROTOTYPES = {
     "pm_set_photons": (_i, [_vp, _i, _vp, _vp, _c.c_uint32]),
     "pm_kernel_launches": (_c.c_ulonglong, []),
     "pm_knn_noalloc": (_i, [_vp, _c.c_uint32, _vp, _c.c_uint32, _i, _f, _vp, _vp, _vp]),
+    "pm_save_map": (_i, [_vp, _i, _c.c_char_p]),
+    "pm_load_map": (_i, [_vp, _i, _c.c_char_p]),
+    "pm_write_ppm": (_i, [_c.c_char_p, _vp, _u, _u]),
+    "pm_viewer_create": (_i, [_c.POINTER(_vp), _u, _u]),
+    "pm_viewer_destroy": (None, [_vp]),
+    "pm_viewer_key": (None, [_vp, _c.c_ubyte]),
+    "pm_viewer_state_get": (_i, [_vp, _c.POINTER(ViewerState)]),
+    "pm_viewer_display": (_i, [_vp, _vp]),
 }
 
 _lib = None
@@ -253,10 +268,59 @@ class Context:
         self._check(self.lib.pm_set_photons(self.h, map_id, pos.ctypes.data, pw.ctypes.data,
                                             len(pos)), "pm_set_photons")
 
+    def save_map(self, map_id, path):
+        self._check(self.lib.pm_save_map(self.h, map_id, path.encode()), "pm_save_map")
+
+    def load_map(self, map_id, path):
+        self._check(self.lib.pm_load_map(self.h, map_id, path.encode()), "pm_load_map")
+
     def stats(self):
         st = FrameStats()
         self._check(self.lib.pm_get_stats(self.h, _c.byref(st)), "pm_get_stats")
         return st
+
+
+class Viewer:
+    """Headless frame driver (pm_viewer_*): the reference's display()/keyboard()."""
+
+    def __init__(self, width=512, height=512):
+        self.lib = load()
+        h = _vp()
+        if self.lib.pm_viewer_create(_c.byref(h), width, height) != PM_OK:
+            raise PMError("pm_viewer_create")
+        self.h = h
+
+    def key(self, k):
+        self.lib.pm_viewer_key(self.h, ord(k) if isinstance(k, str) else int(k))
+
+    def state(self):
+        st = ViewerState()
+        self.lib.pm_viewer_state_get(self.h, _c.byref(st))
+        return st
+
+    def display(self, pos):
+        s = self.lib.pm_viewer_display(self.h, pos)
+        if s != PM_OK:
+            raise PMError("pm_viewer_display: %s" % self.lib.pm_status_string(s).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.pm_viewer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_ppm(path, rgba):
+    """rgba: uint8 [h, w, 4] host array."""
+    a = np.ascontiguousarray(rgba, np.uint8)
+    s = load().pm_write_ppm(path.encode(), a.ctypes.data, a.shape[1], a.shape[0])
+    if s != PM_OK:
+        raise PMError("pm_write_ppm(%s)" % path)
 
 
 def preset(which, seed=0x5EED0000):

@@ -257,6 +257,39 @@ PM_API pm_status pm_knn_noalloc(const float4 *points, uint32_t n, const float4 *
                                 uint32_t nq, int k, float radius, uint32_t *idx_out,
                                 float *d2_out, cudaStream_t stream);
 
+/* ---- 5. host utilities ------------------------------------------------------- */
+
+/* Saves map `map` in index order: one JSON header line, then the records'
+ * float4 pos array and float4 pow array (the layout of pm_get_photons_soa). */
+PM_API pm_status pm_save_map(pm_ctx *ctx, int map, const char *path);
+/* Loads a file written by pm_save_map into map `map` (as pm_set_photons;
+ * follow with pm_build). */
+PM_API pm_status pm_load_map(pm_ctx *ctx, int map, const char *path);
+/* Writes width*height host RGBA8 pixels as a binary PPM (RGB, row 0 on top):
+ * the headless stand-in for the reference's GL blit (callbacksPBO.cpp:65-92). */
+PM_API pm_status pm_write_ppm(const char *path, const uchar4 *rgba, unsigned width,
+                              unsigned height);
+
+/* Headless frame driver with the reference's frame loop and keys
+ * (callbacksPBO.cpp:19-27 state, :47-101 display, :104-143 keyboard): the
+ * first display runs initCuda's early emission, then the random table; each
+ * display emits when emit_flag is set, renders into `pos` (device,
+ * width*height uchar4), and advances anim_time by anim_inc when anim_flag is
+ * set. Key 27 sets quit instead of exiting the process. */
+typedef struct pm_viewer pm_viewer;
+typedef struct pm_viewer_state {
+    unsigned width, height;
+    int anim_flag, emit_flag, interpolate, media;
+    int iter, quit;
+    float anim_time, anim_inc;
+    unsigned long long frames;
+} pm_viewer_state;
+PM_API pm_status pm_viewer_create(pm_viewer **out, unsigned width, unsigned height);
+PM_API void pm_viewer_destroy(pm_viewer *v);
+PM_API void pm_viewer_key(pm_viewer *v, unsigned char key);
+PM_API pm_status pm_viewer_state_get(const pm_viewer *v, pm_viewer_state *out);
+PM_API pm_status pm_viewer_display(pm_viewer *v, uchar4 *pos);
+
 /* Kernels this library has launched since it was loaded (all contexts). */
 PM_API unsigned long long pm_kernel_launches(void);
 
