@@ -27,6 +27,20 @@ constexpr int kMaxSpecular = 8;
 constexpr uint32_t kEyeSalt = 0xE7E5A17Bu;
 constexpr int kMaxMarchSteps = 1 << 16;  // per segment
 
+constexpr int kMergeMin = 4;        // leaf candidates at or above which insertion is a merge
+
+// Per-warp shared memory: the traversal stack and the staging areas of the
+// bulk merge (the k-list and the sorted leaf candidates).
+struct WarpScratch {
+    uint32_t st_node[kStackCap];
+    float st_d2[kStackCap];
+    uint64_t lk[128];
+    uint32_t la[128];
+    uint64_t ck[32];
+    uint32_t ca[32];
+};
+
+
 __device__ __forceinline__ uint64_t make_key(float d2, uint32_t idx) {
     return ((uint64_t)__float_as_uint(d2) << 32) | idx;
 }
@@ -69,6 +83,90 @@ struct Knn {
         }
         update_worst();
     }
+    // Merges the candidates of the lanes in `mask` (each lane's `x` / `xa`,
+    // all below worst) into the list at once: every list entry moves up by
+    // the number of candidates below it, every candidate lands at its rank
+    // among the candidates plus the number of list entries below it. Keys
+    // are unique (photon indices), so the new positions are a permutation.
+    __device__ __forceinline__ void merge(uint64_t x, uint32_t xa, unsigned mask, int lane,
+                                          WarpScratch &w, bool dedup) {
+        constexpr int K = 32 * S;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            w.lk[lane * S + s] = key[s];
+            w.la[lane * S + s] = at[s];
+        }
+        if (dedup) {  // drop candidates already in the list
+            __syncwarp();
+            bool dup = false;
+            if ((mask >> lane) & 1u) {
+                int lo = 0, hi = K;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (w.lk[mid] < x) lo = mid + 1; else hi = mid;
+                }
+                dup = lo < K && w.lk[lo] == x;
+            }
+            mask &= ~__ballot_sync(kFull, dup);
+            if (!mask) {
+                __syncwarp();
+                return;
+            }
+        }
+        const int n = __popc(mask);
+        int rc = 0;
+        for (unsigned mm = mask; mm; mm &= mm - 1) {
+            const int j = __ffs(mm) - 1;
+            rc += __shfl_sync(kFull, x, j) < x ? 1 : 0;
+        }
+        if ((mask >> lane) & 1u) {
+            w.ck[rc] = x;
+            w.ca[rc] = xa;
+        }
+        __syncwarp();
+        int lpos[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            int lo = 0, hi = n;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (w.ck[mid] < key[s]) lo = mid + 1; else hi = mid;
+            }
+            lpos[s] = lane * S + s + lo;
+        }
+        int cpos = K;
+        uint64_t cv = 0;
+        uint32_t cav = 0;
+        if (lane < n) {
+            cv = w.ck[lane];
+            cav = w.ca[lane];
+            int lo = 0, hi = K;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (w.lk[mid] < cv) lo = mid + 1; else hi = mid;
+            }
+            cpos = lane + lo;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+            if (lpos[s] < K) {
+                w.lk[lpos[s]] = key[s];
+                w.la[lpos[s]] = at[s];
+            }
+        if (cpos < K) {
+            w.lk[cpos] = cv;
+            w.la[cpos] = cav;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            key[s] = w.lk[lane * S + s];
+            at[s] = w.la[lane * S + s];
+        }
+        __syncwarp();
+        update_worst();
+    }
 };
 
 __device__ __forceinline__ float box_d2(float4 lo, float4 hi, v3 q) {
@@ -78,11 +176,70 @@ __device__ __forceinline__ float box_d2(float4 lo, float4 hi, v3 q) {
     return dx * dx + dy * dy + dz * dz;
 }
 
+// Sorts lk/la[0..P) ascending by key (bitonic network over shared memory);
+// P is a power of two in [32, 128].
+__device__ __forceinline__ void warp_sort_smem(WarpScratch &w, int P, int lane) {
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < (P >> 1); t += 32) {
+                const int i = 2 * stride * (t / stride) + (t % stride);
+                const int j = i + stride;
+                const bool up = (i & size) == 0;
+                const uint64_t a = w.lk[i], b = w.lk[j];
+                if ((a > b) == up) {
+                    w.lk[i] = b;
+                    w.lk[j] = a;
+                    const uint32_t x = w.la[i];
+                    w.la[i] = w.la[j];
+                    w.la[j] = x;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Sorts the `count` collected candidates (count <= 128) in lk/la and loads
+// the first 32*S of them into the k-list; empty slots hold cap.
 template <int S>
-__device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, uint32_t *st_node, float *st_d2,
-                           int lane) {
+__device__ __forceinline__ void load_sorted(Knn<S> &kn, WarpScratch &w, int count, uint64_t cap,
+                                            int lane) {
+    int P = 32;
+    while (P < count) P <<= 1;
+    for (int i = count + lane; i < P; i += 32) {
+        w.lk[i] = cap;
+        w.la[i] = 0xffffffffu;
+    }
+    __syncwarp();
+    warp_sort_smem(w, P, lane);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int j = lane * S + s;
+        kn.key[s] = j < P ? w.lk[j] : cap;
+        kn.at[s] = j < P ? w.la[j] : 0xffffffffu;
+    }
+    __syncwarp();
+    kn.update_worst();
+}
+
+// k nearest records of q, sorted by (squared distance, index), within the
+// radius cap held in kn.worst at entry. The walk starts in collect mode:
+// every record within the cap is appended to a shared buffer, children are
+// pushed in any order and nothing is kept sorted. If more than 128 records
+// turn up, the buffer is sorted into the k-list and the walk continues in
+// list mode, pruning with the current k-th distance and inserting (bulk
+// merge or one at a time). A walk that stays in collect mode sorts its
+// buffer once at the end. Both modes produce the same exact list.
+template <int S>
+__device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, int lane,
+                           uint64_t cap, bool warm = false) {
     if (m.n == 0) return;
+    constexpr int kCollectMax = 128;
+    uint32_t *st_node = ws.st_node;
+    float *st_d2 = ws.st_d2;
     const uint32_t first_leaf = 1u << m.depth;
+    bool collect = !warm;
+    int count = 0;
     int top = 1;
     if (lane == 0) { st_node[0] = 1u; st_d2[0] = 0.0f; }
     __syncwarp();
@@ -104,12 +261,39 @@ __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, uint32_t *st_node
                 key = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
             }
             unsigned mask = __ballot_sync(kFull, key < kn.worst);
-            while (mask) {
-                const int src = __ffs(mask) - 1;
-                uint64_t x = __shfl_sync(kFull, key, src);
-                kn.insert(x, base + src, lane);
-                mask &= mask - 1;
-                mask &= __ballot_sync(kFull, key < kn.worst);
+            if (!mask) continue;
+            if (collect) {
+                const int add = __popc(mask);
+                if (count + add <= kCollectMax) {
+                    if ((mask >> lane) & 1u) {
+                        const int at = count + __popc(mask & ((1u << lane) - 1u));
+                        ws.lk[at] = key;
+                        ws.la[at] = r;
+                    }
+                    count += add;
+                    __syncwarp();
+                    continue;
+                }
+                load_sorted<S>(kn, ws, count, cap, lane);
+                collect = false;
+                mask = __ballot_sync(kFull, key < kn.worst);
+            }
+            if (__popc(mask) >= kMergeMin) {
+                kn.merge(key, r, mask, lane, ws, warm);
+            } else {
+                while (mask) {
+                    const int src = __ffs(mask) - 1;
+                    uint64_t x = __shfl_sync(kFull, key, src);
+                    bool dup = false;
+                    if (warm) {
+#pragma unroll
+                        for (int s = 0; s < S; ++s) dup |= kn.key[s] == x;
+                        dup = __any_sync(kFull, dup);
+                    }
+                    if (!dup) kn.insert(x, base + src, lane);
+                    mask &= mask - 1;
+                    mask &= __ballot_sync(kFull, key < kn.worst);
+                }
             }
         } else {
             int w = (m.depth - dn) % 5;
@@ -120,12 +304,17 @@ __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, uint32_t *st_node
             if (lane < nc) bd2 = box_d2(__ldg(&m.lo[child]), __ldg(&m.hi[child]), q);
             const bool ok = (lane < nc) && (bd2 <= wd2);
             const unsigned mask = __ballot_sync(kFull, ok);
-            // Far-to-near: rank = survivors farther than this lane (ties: higher lane farther).
-            int rank = 0;
-            for (unsigned mm = mask; mm; mm &= mm - 1) {
-                const int j = __ffs(mm) - 1;
-                float o = __shfl_sync(kFull, bd2, j);
-                rank += (o > bd2 || (o == bd2 && j > lane)) ? 1 : 0;
+            int rank;
+            if (collect) {
+                rank = __popc(mask & ((1u << lane) - 1u));  // visiting order is free
+            } else {
+                // far-to-near: survivors farther than this lane (ties: higher lane farther)
+                rank = 0;
+                for (unsigned mm = mask; mm; mm &= mm - 1) {
+                    const int j = __ffs(mm) - 1;
+                    float o = __shfl_sync(kFull, bd2, j);
+                    rank += (o > bd2 || (o == bd2 && j > lane)) ? 1 : 0;
+                }
             }
             if (ok && top + rank < kStackCap) {
                 st_node[top + rank] = child;
@@ -135,6 +324,47 @@ __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, uint32_t *st_node
             __syncwarp();
         }
     }
+    if (collect) load_sorted<S>(kn, ws, count, cap, lane);
+}
+
+// Warm start for the next sample of a march: the list of the previous
+// sample, re-scored at q (entries beyond the cap dropped) and sorted. The
+// search that follows only has to find records closer than its k-th entry.
+template <int S>
+__device__ void rescore(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, uint64_t cap,
+                        int lane) {
+    constexpr int K = 32 * S;
+    constexpr int P = K <= 32 ? 32 : (K <= 64 ? 64 : 128);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int j = lane * S + s;
+        uint64_t nk = cap;
+        uint32_t na = 0xffffffffu;
+        if (kn.at[s] != 0xffffffffu) {
+            const float4 p = __ldg(&m.pos[kn.at[s]]);
+            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const uint64_t k2 = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
+            if (k2 < cap) {
+                nk = k2;
+                na = kn.at[s];
+            }
+        }
+        ws.lk[j] = nk;
+        ws.la[j] = na;
+    }
+    for (int i = K + lane; i < P; i += 32) {
+        ws.lk[i] = cap;
+        ws.la[i] = 0xffffffffu;
+    }
+    __syncwarp();
+    warp_sort_smem(ws, P, lane);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        kn.key[s] = ws.lk[lane * S + s];
+        kn.at[s] = ws.la[lane * S + s];
+    }
+    __syncwarp();
+    kn.update_worst();
 }
 
 // Kahan sum within a lane, then a compensated butterfly across the warp:
@@ -195,8 +425,7 @@ template <int S>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) knn_kernel(MapView m, const float4 *q,
                                                                   uint32_t nq, int k, float r2cap,
                                                                   uint32_t *idx_out, float *d2_out) {
-    __shared__ uint32_t st_node[kWarpsPerBlock][kStackCap];
-    __shared__ float st_d2[kWarpsPerBlock][kStackCap];
+    __shared__ WarpScratch ws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t qi = blockIdx.x * kWarpsPerBlock + wib;
     if (qi >= nq) return;
@@ -204,7 +433,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) knn_kernel(MapView m, con
     const uint64_t cap = make_key(r2cap, 0xffffffffu);
     Knn<S> kn;
     kn.reset(cap, k);
-    knn_search<S>(m, mk3(qq.x, qq.y, qq.z), kn, st_node[wib], st_d2[wib], lane);
+    knn_search<S>(m, mk3(qq.x, qq.y, qq.z), kn, ws[wib], lane, cap);
 #pragma unroll
     for (int s = 0; s < S; ++s) {
         const int j = lane * S + s;
@@ -219,8 +448,7 @@ template <int S>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, MapView surf,
                                                                      MapView vol, RenderParams R,
                                                                      float4 *rad, uchar4 *rgba) {
-    __shared__ uint32_t st_node[kWarpsPerBlock][kStackCap];
-    __shared__ float st_d2[kWarpsPerBlock][kStackCap];
+    __shared__ WarpScratch ws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t pix = blockIdx.x * kWarpsPerBlock + wib;
     const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
@@ -245,6 +473,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
             if (t0 < t1) {
                 const int nst = (int)fminf(ceilf((t1 - t0) / R.step), (float)kMaxMarchSteps);
                 const v3 wo = d * -1.0f;
+                Knn<S> kn;
+                bool warm = false;  // the previous sample found k records
                 for (int j = 0; j < nst; ++j) {
                     const float ta = t0 + (float)j * R.step;
                     const float tb = fminf(t0 + (float)(j + 1) * R.step, t1);
@@ -255,12 +485,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
                     const float st = ss + Sc.sigma_a;
                     const float tau_mid = tau + st * (0.5f * dt);
                     if (vol.n > 0) {
-                        Knn<S> kn;
-                        kn.reset(cap, R.k);
-                        knn_search<S>(vol, x, kn, st_node[wib], st_d2[wib], lane);
+                        if (warm) {
+                            rescore<S>(vol, x, kn, ws[wib], cap, lane);
+                        } else {
+                            kn.reset(cap, R.k);
+                        }
+                        knn_search<S>(vol, x, kn, ws[wib], lane, cap, warm);
                         int found;
                         float r2;
                         v3 e = flux_sum<S>(kn, vol, lane, 1, wo, Sc.g, cap, R.r2cap, &found, &r2);
+                        warm = found == R.k;
                         ++nvol;
                         if (found > 0) {
                             const float scale = pm_expf(-tau_mid) * dt * (1.0f / (4.18879020f * r2 * sqrtf(r2)));
@@ -281,7 +515,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
             if (surf.n > 0) {
                 Knn<S> kn;
                 kn.reset(cap, R.k);
-                knn_search<S>(surf, hp, kn, st_node[wib], st_d2[wib], lane);
+                knn_search<S>(surf, hp, kn, ws[wib], lane, cap);
                 int found;
                 float r2;
                 v3 e = flux_sum<S>(kn, surf, lane, 0, nf, 0.0f, cap, R.r2cap, &found, &r2);
