@@ -1,14 +1,22 @@
 // kdtree.cu -- photon-map kd-tree build.
 //
-// 1. 63-bit Morton code of every record (21 bits per axis over the box).
-// 2. Stable LSD radix sort of (code, record index): equal codes keep
-//    emission order, so the layout is deterministic.
-// 3. Records permuted into sorted order (SoA float4 pos / pow).
-// 4. Implicit balanced tree over the sorted sequence: every node splits its
-//    range at the median, leaves hold 32 consecutive records (one warp's
-//    load), node i has children 2i and 2i+1 and leaves sit at depth D. Each
-//    node stores the bounding box of its records (lo, hi), built bottom-up,
-//    so a query can bound the distance to everything below a node.
+// Implicit left-balanced kd-tree: node i has children 2i and 2i+1, leaves
+// hold 32 consecutive records (one warp-wide load) at depth D, and the node
+// at level l covers records [j*32*2^(D-l), (j+1)*32*2^(D-l)) of the final
+// order (j = its index within the level), so no child pointers or ranges
+// are stored.
+//
+// Top-down, one level at a time, all nodes of the level in parallel: every
+// record gets the 64-bit key (node within the level, coordinate along the
+// longest axis of its node's cell), a stable LSD radix sort orders the
+// records by it -- which leaves each node's records sorted along that axis,
+// so the node's first half (the left child) is the lower half: a median
+// split -- and each child's cell is its parent's cell cut at the median
+// coordinate. Equal keys keep their previous order, so the layout is
+// deterministic. The records are then permuted into that order (SoA float4
+// pos / pow) and every node gets the tight bounding box of its records,
+// bottom-up, which is what a query tests. The cells live in the node box
+// arrays until the boxes overwrite them.
 #include "launch_count.cuh"
 #include "kdtree.cuh"
 #include "radix_sort.cuh"
@@ -16,20 +24,75 @@
 namespace pm {
 namespace {
 
-__global__ void morton_kernel(const float4 *__restrict__ pos, uint32_t n, float3 lo, float3 hi,
-                              const float *box_dev, uint64_t *keys, uint32_t *vals) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ uint32_t orderable(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float from_orderable(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u ^ 0x80000000u) : ~u);
+}
+__device__ __forceinline__ int longest_axis(float4 lo, float4 hi) {
+    const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+    return (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
+}
+
+__global__ void root_cell_kernel(float3 lo, float3 hi, const float *box_dev, float4 *cell_lo,
+                                 float4 *cell_hi) {
     if (box_dev) {
         lo = make_float3(box_dev[0], box_dev[1], box_dev[2]);
         hi = make_float3(box_dev[3], box_dev[4], box_dev[5]);
     }
-    float4 p = pos[i];
-    uint64_t c = spread21(quantize21(p.x, lo.x, hi.x)) |
-                 (spread21(quantize21(p.y, lo.y, hi.y)) << 1) |
-                 (spread21(quantize21(p.z, lo.z, hi.z)) << 2);
-    keys[i] = c;
-    vals[i] = i;
+    cell_lo[1] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+    cell_hi[1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+}
+
+// Key of record position i at level l: (node within the level, orderable
+// coordinate along the longest axis of the node's cell).
+__global__ void split_key_kernel(const float4 *__restrict__ pos, const uint32_t *__restrict__ order,
+                                 uint32_t n, int level, uint32_t span,
+                                 const float4 *__restrict__ cell_lo,
+                                 const float4 *__restrict__ cell_hi, uint64_t *keys,
+                                 uint32_t *vals_init) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t node = i / span;
+    const uint32_t g = (1u << level) + node;
+    const int ax = longest_axis(cell_lo[g], cell_hi[g]);
+    uint32_t src = i;
+    if (order) src = order[i];
+    else vals_init[i] = i;
+    const float4 p = pos[src];
+    const float c = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+    keys[i] = ((uint64_t)node << 32) | orderable(c);
+}
+
+// Children cells of every node at `level`: the parent's cell cut at the
+// coordinate of the right child's first record.
+__global__ void split_cell_kernel(const uint64_t *__restrict__ keys, uint32_t n, int level,
+                                  uint32_t span, uint32_t nodes, float4 *cell_lo, float4 *cell_hi) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nodes) return;
+    const uint32_t g = (1u << level) + j;
+    const float4 lo = cell_lo[g], hi = cell_hi[g];
+    const uint32_t start = j * span, half = span >> 1;
+    const uint32_t cnt = min(span, n - start);
+    float4 llo = lo, lhi = hi, rlo = lo, rhi = hi;
+    if (cnt > half) {
+        const int ax = longest_axis(lo, hi);
+        const float m = from_orderable((uint32_t)keys[start + half]);
+        if (ax == 0) { lhi.x = m; rlo.x = m; }
+        else if (ax == 1) { lhi.y = m; rlo.y = m; }
+        else { lhi.z = m; rlo.z = m; }
+    }
+    cell_lo[2 * g] = llo;
+    cell_hi[2 * g] = lhi;
+    cell_lo[2 * g + 1] = rlo;
+    cell_hi[2 * g + 1] = rhi;
+}
+
+__global__ void iota_kernel(uint32_t *v, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = i;
 }
 
 __global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
@@ -109,15 +172,37 @@ size_t tree_nodes(uint32_t n) { return (size_t)2 << tree_depth(n); }
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     const uint32_t n = a.n;
     if (n == 0) return cudaSuccess;
-    morton_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.pos_in, n, a.lo, a.hi, a.box_dev, a.keys,
-                                                   a.vals); note_launch();
-    uint64_t *sk = nullptr;
-    uint32_t *sv = nullptr;
-    cudaError_t e = radix_sort_pairs_u64(a.keys, a.vals, a.keys_tmp, a.vals_tmp, a.n_dev, n, 0, 64,
-                                         a.hist, s, &sk, &sv);
-    if (e != cudaSuccess) return e;
-    permute_kernel<<<(n + 255) / 256, 256, 0, s>>>(sv, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out); note_launch();
     const int D = tree_depth(n);
+    const uint32_t blocks = (n + 255) / 256;
+    // Top-down median splits; the current order ping-pongs between the two
+    // (keys, vals) buffer pairs of the sort.
+    uint64_t *ka = a.keys, *kb = a.keys_tmp;
+    uint32_t *va = a.vals, *vb = a.vals_tmp;
+    cudaError_t e;
+    if (D == 0) {
+        iota_kernel<<<blocks, 256, 0, s>>>(va, n); note_launch();
+    } else {
+        root_cell_kernel<<<1, 1, 0, s>>>(a.lo, a.hi, a.box_dev, a.node_lo, a.node_hi); note_launch();
+    }
+    for (int l = 0; l < D; ++l) {
+        const uint32_t span = 32u << (D - l);
+        const uint32_t nodes = (n + span - 1) / span;
+        split_key_kernel<<<blocks, 256, 0, s>>>(a.pos_in, l == 0 ? nullptr : va, n, l, span,
+                                                a.node_lo, a.node_hi, ka, va); note_launch();
+        int node_bits = 0;
+        while ((1u << node_bits) < nodes) ++node_bits;
+        uint64_t *ko = nullptr;
+        uint32_t *vo = nullptr;
+        e = radix_sort_pairs_u64(ka, va, kb, vb, a.n_dev, n, 0, 32 + node_bits, a.hist, s, &ko, &vo);
+        if (e != cudaSuccess) return e;
+        if (vo != va) {
+            uint64_t *tk = ka; ka = kb; kb = tk;
+            uint32_t *tv = va; va = vb; vb = tv;
+        }
+        split_cell_kernel<<<(nodes + 255) / 256, 256, 0, s>>>(ka, n, l, span, nodes, a.node_lo,
+                                                               a.node_hi); note_launch();
+    }
+    permute_kernel<<<blocks, 256, 0, s>>>(va, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out); note_launch();
     const uint32_t first_leaf = 1u << D;
     leaf_box_kernel<<<(first_leaf * 32 + 255) / 256, 256, 0, s>>>(a.pos_out, n, first_leaf, first_leaf,
                                                                  a.node_lo, a.node_hi); note_launch();
@@ -132,7 +217,7 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         note_launch();
     }
     if (a.order_out) {
-        e = cudaMemcpyAsync(a.order_out, sv, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+        e = cudaMemcpyAsync(a.order_out, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();

@@ -1,4 +1,4 @@
-// kdtree.cuh -- Morton-ordered implicit kd-tree over a photon map.
+// kdtree.cuh -- implicit median-split kd-tree over a photon map.
 #pragma once
 #include "phys_common.cuh"
 
@@ -12,8 +12,8 @@ size_t tree_nodes(uint32_t n);
 struct KdBuildArgs {
     uint32_t n;                 // records
     const uint32_t *n_dev;      // the same count in device memory
-    float3 lo, hi;              // Morton quantisation box
-    const float *box_dev;       // nullable: lo/hi read from device memory (6 floats)
+    float3 lo, hi;              // root cell (the scene box)
+    const float *box_dev;       // nullable: root cell read from device memory (6 floats)
     const float4 *pos_in, *pow_in;   // records in index order (pow_in nullable)
     float4 *pos_out, *pow_out;       // records in tree order (pow_out nullable)
     float4 *node_lo, *node_hi;       // tree_nodes(n) boxes

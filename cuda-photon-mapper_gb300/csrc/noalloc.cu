@@ -72,7 +72,7 @@ cudaError_t scratch_address(unsigned char **out) {
 }
 
 // Copies the points with their index in .w (the tie-break key), writes the
-// count for the sort and the points' bounding box for the Morton codes.
+// count for the sort and the points' bounding box (the tree's root cell).
 __global__ void __launch_bounds__(1024) prepare_kernel(const float4 *__restrict__ pts, uint32_t n,
                                                        float4 *ipos, uint32_t *count, float *box) {
     __shared__ float red[6][32];

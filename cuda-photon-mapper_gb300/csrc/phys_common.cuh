@@ -246,22 +246,4 @@ PM_HD pm_u32x4 philox(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint
     return pm_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 
-// 63-bit Morton code of p in the box, 21 bits per axis, x in the lowest bit.
-PM_HD uint64_t spread21(uint32_t v) {
-    uint64_t x = v & 0x1FFFFFu;
-    x = (x | (x << 32)) & 0x1F00000000FFFFull;
-    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
-    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
-    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
-    x = (x | (x << 2)) & 0x1249249249249249ull;
-    return x;
-}
-
-PM_HD uint32_t quantize21(float v, float lo, float hi) {
-    float f = (v - lo) / (hi - lo) * 2097152.0f;
-    if (!(f > 0.0f)) return 0u;
-    if (f >= 2097151.0f) return 2097151u;
-    return (uint32_t)f;
-}
-
 }  // namespace pm

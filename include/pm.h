@@ -202,7 +202,8 @@ PM_API pm_status pm_update_scene(pm_ctx *ctx, const pm_scene *scene);
 /* Traces photon paths until both maps reach their targets. Synchronises
  * the stream once to learn the map sizes. */
 PM_API pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream);
-/* Builds the kd-tree of each map (Morton sort + median split + node boxes). */
+/* Builds the kd-tree of each map: level-by-level median splits along each
+ * cell's longest axis (stable radix sort per level) and tight node boxes. */
 PM_API pm_status pm_build(pm_ctx *ctx, cudaStream_t stream);
 /* Renders one frame: eye rays, specular chains, the volume march and the
  * surface radiance estimate. radiance (nullable, device): width*height
@@ -226,7 +227,7 @@ PM_API pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out);
 /* Replaces map `map` with n host records in the SoA layout of
  * pm_get_photons_soa (pos.w is overwritten with the record index); used to
  * load a saved map or to query an arbitrary point set. Needs pm_set_scene
- * (its box bounds the Morton codes); follow with pm_build. */
+ * (its box is the tree's root cell); follow with pm_build. */
 PM_API pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *pow,
                                 uint32_t n);
 
