@@ -27,7 +27,7 @@ constexpr int kMaxSpecular = 8;
 constexpr uint32_t kEyeSalt = 0xE7E5A17Bu;
 constexpr int kMaxMarchSteps = 1 << 16;  // per segment
 
-constexpr int kMergeMin = 4;        // leaf candidates at or above which insertion is a merge
+constexpr int kMergeMin = 16;       // leaf candidates at or above which insertion is a merge
 
 // Per-warp shared memory: the traversal stack and the staging areas of the
 // bulk merge (the k-list and the sorted leaf candidates).
@@ -38,6 +38,7 @@ struct WarpScratch {
     uint32_t la[128];
     uint64_t ck[32];
     uint32_t ca[32];
+    uint64_t sk[128];  // warm start: the re-scored previous list, sorted (duplicate filter)
 };
 
 
@@ -89,29 +90,12 @@ struct Knn {
     // among the candidates plus the number of list entries below it. Keys
     // are unique (photon indices), so the new positions are a permutation.
     __device__ __forceinline__ void merge(uint64_t x, uint32_t xa, unsigned mask, int lane,
-                                          WarpScratch &w, bool dedup) {
+                                          WarpScratch &w) {
         constexpr int K = 32 * S;
 #pragma unroll
         for (int s = 0; s < S; ++s) {
             w.lk[lane * S + s] = key[s];
             w.la[lane * S + s] = at[s];
-        }
-        if (dedup) {  // drop candidates already in the list
-            __syncwarp();
-            bool dup = false;
-            if ((mask >> lane) & 1u) {
-                int lo = 0, hi = K;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (w.lk[mid] < x) lo = mid + 1; else hi = mid;
-                }
-                dup = lo < K && w.lk[lo] == x;
-            }
-            mask &= ~__ballot_sync(kFull, dup);
-            if (!mask) {
-                __syncwarp();
-                return;
-            }
         }
         const int n = __popc(mask);
         int rc = 0;
@@ -262,6 +246,19 @@ __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, 
             }
             unsigned mask = __ballot_sync(kFull, key < kn.worst);
             if (!mask) continue;
+            if (warm) {  // drop records the warm-start list already holds
+                bool dup = false;
+                if ((mask >> lane) & 1u) {
+                    int lo = 0, hi = 32 * S;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (ws.sk[mid] < key) lo = mid + 1; else hi = mid;
+                    }
+                    dup = lo < 32 * S && ws.sk[lo] == key;
+                }
+                mask &= ~__ballot_sync(kFull, dup);
+                if (!mask) continue;
+            }
             if (collect) {
                 const int add = __popc(mask);
                 if (count + add <= kCollectMax) {
@@ -279,18 +276,12 @@ __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, 
                 mask = __ballot_sync(kFull, key < kn.worst);
             }
             if (__popc(mask) >= kMergeMin) {
-                kn.merge(key, r, mask, lane, ws, warm);
+                kn.merge(key, r, mask, lane, ws);
             } else {
                 while (mask) {
                     const int src = __ffs(mask) - 1;
                     uint64_t x = __shfl_sync(kFull, key, src);
-                    bool dup = false;
-                    if (warm) {
-#pragma unroll
-                        for (int s = 0; s < S; ++s) dup |= kn.key[s] == x;
-                        dup = __any_sync(kFull, dup);
-                    }
-                    if (!dup) kn.insert(x, base + src, lane);
+                    kn.insert(x, base + src, lane);
                     mask &= mask - 1;
                     mask &= __ballot_sync(kFull, key < kn.worst);
                 }
@@ -362,6 +353,7 @@ __device__ void rescore(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, uin
     for (int s = 0; s < S; ++s) {
         kn.key[s] = ws.lk[lane * S + s];
         kn.at[s] = ws.la[lane * S + s];
+        ws.sk[lane * S + s] = kn.key[s];
     }
     __syncwarp();
     kn.update_worst();
