@@ -27,6 +27,8 @@ struct RenderParams {
 
 cudaError_t knn_query(const MapView &m, const float4 *q, uint32_t nq, int k, float radius,
                       uint32_t *idx, float *d2, cudaStream_t s);
+cudaError_t radius_gather(const MapView &m, const float4 *pts, const float4 *nrm, uint32_t nq,
+                          float sq_radius, float exposure, float4 *out, cudaStream_t s);
 cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vol,
                          const RenderParams &R, float4 *rad, uchar4 *rgba, cudaStream_t s);
 

@@ -316,6 +316,19 @@ pm_status pm_knn(pm_ctx *ctx, int map, const float4 *queries, uint32_t nq, int k
     return PM_OK;
 }
 
+pm_status pm_radius_gather(pm_ctx *ctx, int map, const float4 *points, const float4 *normals,
+                           uint32_t nq, float sq_radius, float exposure, float4 *out,
+                           cudaStream_t stream) {
+    if (!ctx || map < 0 || map > 1 || !(sq_radius > 0.0f) || !(exposure != 0.0f)) return PM_ERR_INVALID;
+    if (nq && (!points || !normals || !out)) return PM_ERR_INVALID;
+    PhysicalState *st = ctx->phys;
+    if (!st || !st->map[map].built) return fail(ctx, PM_ERR_STATE, "pm_radius_gather before pm_build");
+    DeviceGuard g(ctx->device);
+    cudaError_t e;
+    PM_TRY(radius_gather(view_of(st->map[map]), points, normals, nq, sq_radius, exposure, out, stream));
+    return PM_OK;
+}
+
 pm_status pm_get_photons_soa(pm_ctx *ctx, int map, float4 *pos, float4 *pw, uint32_t cap,
                              uint32_t *count) {
     if (!ctx || map < 0 || map > 1) return PM_ERR_INVALID;

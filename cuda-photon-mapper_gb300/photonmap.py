@@ -113,6 +113,7 @@ PROTOTYPES = {
     "pm_build": (_i, [_vp, _vp]),
     "pm_render": (_i, [_vp, _vp, _vp, _vp]),
     "pm_knn": (_i, [_vp, _i, _vp, _c.c_uint32, _i, _f, _vp, _vp, _vp]),
+    "pm_radius_gather": (_i, [_vp, _i, _vp, _vp, _c.c_uint32, _f, _f, _vp, _vp]),
     "pm_get_photons": (_i, [_vp, _i, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
     "pm_get_photons_soa": (_i, [_vp, _i, _vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
     "pm_get_stats": (_i, [_vp, _c.POINTER(FrameStats)]),
@@ -239,6 +240,10 @@ class Context:
     def knn(self, map_id, queries, nq, k, radius, idx, d2, stream=0):
         self._check(self.lib.pm_knn(self.h, map_id, queries, nq, k, radius, idx, d2, stream),
                     "pm_knn")
+
+    def radius_gather(self, map_id, points, normals, nq, sq_radius, exposure, out, stream=0):
+        self._check(self.lib.pm_radius_gather(self.h, map_id, points, normals, nq, sq_radius,
+                                              exposure, out, stream), "pm_radius_gather")
 
     def photons_soa(self, map_id):
         """Map `map_id` in index order: (pos float32[n,4], pow float32[n,4])."""

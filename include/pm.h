@@ -215,6 +215,16 @@ PM_API pm_status pm_render(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStre
  * neighbours are 0xFFFFFFFF / radius^2. Needs pm_build. */
 PM_API pm_status pm_knn(pm_ctx *ctx, int map, const float4 *queries, uint32_t nq, int k,
                         float radius, uint32_t *idx_out, float *d2_out, cudaStream_t stream);
+/* The reference's record-list radius gather (kernelPBO.cu:165-182,
+ * "photonMappingKernel - Copy.cu":191-208) over map `map`: for each of nq
+ * points (device float4 xyz) with normal (device float4 xyz), the sum over
+ * photons with squared distance <= sq_radius of energy * max(0, -N.dir) *
+ * (1 - distance) / exposure, into out (device float4 rgb). Unlike the
+ * reference, photons are not restricted to the queried object. Needs
+ * pm_build. */
+PM_API pm_status pm_radius_gather(pm_ctx *ctx, int map, const float4 *points,
+                                  const float4 *normals, uint32_t nq, float sq_radius,
+                                  float exposure, float4 *out, cudaStream_t stream);
 /* Synchronous copy of a map in index order, in the reference's record
  * layout (cap records at most); *count receives the map size. */
 PM_API pm_status pm_get_photons(pm_ctx *ctx, int map, pm_photon_record *out, uint32_t cap,

@@ -117,6 +117,8 @@ def _phys_protos(lib):
     lib.pmo64_render.restype = None
     lib.pmo_trace_path.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]
     lib.pmo_trace_path.restype = None
+    lib.pmo64_radius_gather.argtypes = [vp, vp, vp, u32, vp, vp, u32, f, f, vp]
+    lib.pmo64_radius_gather.restype = None
     lib.pmo_sample.argtypes = [i, vp, f, f, f, vp]
     lib.pmo_sample.restype = None
     lib.pmo_fresnel.argtypes = [f, f]
@@ -235,4 +237,23 @@ def sample(which, n, g=0.0, direction=(0.0, 0.0, 1.0), seed=0):
     for i in range(n):
         lib.pmo_sample(which, d.ctypes.data, g, float(u[i, 0]), float(u[i, 1]), o.ctypes.data)
         out[i] = o
+    return out
+
+
+def radius_gather(pos, pw, points, normals, sq_radius, exposure):
+    """The reference's radius gather over records in index order (float64)."""
+    lib = phys_lib()
+    pos = np.ascontiguousarray(pos, np.float32)
+    pw = np.ascontiguousarray(pw, np.float32)
+    dirs = np.zeros((len(pw), 3), np.float32)
+    d = np.zeros(3, np.float32)
+    for i in range(len(pw)):
+        lib.pmo_oct_decode(int(pw[i, 3:4].view(np.uint32)[0]), d.ctypes.data)
+        dirs[i] = d
+    pts = np.ascontiguousarray(points, np.float32)
+    nrm = np.ascontiguousarray(normals, np.float32)
+    out = np.zeros((len(pts), 3), np.float64)
+    lib.pmo64_radius_gather(pos.ctypes.data, pw.ctypes.data, dirs.ctypes.data, len(pos),
+                            pts.ctypes.data, nrm.ctypes.data, len(pts), sq_radius, exposure,
+                            out.ctypes.data)
     return out

@@ -102,6 +102,10 @@ void pmo64_render(const pmo_scene *scene, const pmo_config *cfg, const float *he
                   const double *vpow, uint32_t nv, const uint32_t *pixels, uint32_t npix,
                   double *out);
 
+void pmo64_radius_gather(const float (*pos)[4], const float (*pw)[4], const float (*dirs)[3],
+                         uint32_t n, const float (*pts)[4], const float (*nrm)[4], uint32_t nq,
+                         float sq_radius, float exposure, double (*out)[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -488,3 +488,32 @@ void pmo64_render(const pmo_scene *scene, const pmo_config *cfg, const float *he
     grid_free(gs);
     grid_free(gv);
 }
+
+/* The reference's record-list radius gather (kernelPBO.cu:165-182), over
+ * the records in index order with the gated squared distance of
+ * gatedSqDist3 (:245-257) evaluated in float as the reference does, and the
+ * rest in double: energy * max(0, -N.dir) * (1 - distance) / exposure. */
+void pmo64_radius_gather(const float (*pos)[4], const float (*pw)[4], const float (*dirs)[3],
+                         uint32_t n, const float (*pts)[4], const float (*nrm)[4], uint32_t nq,
+                         float sq_radius, float exposure, double (*out)[3]) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long qi = 0; qi < (long)nq; ++qi) {
+        double e[3] = {0, 0, 0};
+        for (uint32_t i = 0; i < n; ++i) {
+            float c = pts[qi][0] - pos[i][0];
+            float d = c * c;
+            if (d > sq_radius) continue;
+            c = pts[qi][1] - pos[i][1];
+            d += c * c;
+            if (d > sq_radius) continue;
+            c = pts[qi][2] - pos[i][2];
+            d += c * c;
+            if (d > sq_radius) continue;
+            double nd = (double)nrm[qi][0] * dirs[i][0] + (double)nrm[qi][1] * dirs[i][1] +
+                        (double)nrm[qi][2] * dirs[i][2];
+            double w = fmax(0.0, -nd) * (1.0 - sqrt((double)d)) / exposure;
+            for (int k = 0; k < 3; ++k) e[k] += pw[i][k] * w;
+        }
+        for (int k = 0; k < 3; ++k) out[qi][k] = e[k];
+    }
+}

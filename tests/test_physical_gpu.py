@@ -204,3 +204,34 @@ def test_state_errors(ctx):
     cf.k = 0
     with pytest.raises(photonmap.PMError):
         ctx.set_scene(sc, cf)
+
+
+def test_radius_gather_matches_reference_weighting(ctx):
+    # kernelPBO.cu:165-182 weighting over the surface map; float32 sums in
+    # tree order against float64 sums in index order: 1e-4 relative.
+    sc, cf = small(1, 20000, 1000)
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    ctx.build()
+    pos, pw = ctx.photons_soa(0)
+    rs = np.random.RandomState(9)
+    nq = 600
+    pts = np.zeros((nq, 4), np.float32)
+    nrm = np.zeros((nq, 4), np.float32)
+    pts[:, 0] = rs.uniform(-0.5, 0.5, nq)
+    pts[:, 2] = rs.uniform(-0.5, 0.5, nq)
+    pts[:300, 1] = 0.0          # on the floor, facing up
+    nrm[:300, 1] = 1.0
+    pts[300:, 1] = rs.uniform(0.0, 1.0, 300)
+    v = rs.standard_normal((300, 3)).astype(np.float32)
+    nrm[300:, :3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    for sq, expo in [(0.01, 50.0), (0.0025, 1.0)]:
+        pd, nd = torch.from_numpy(pts).cuda(), torch.from_numpy(nrm).cuda()
+        out = torch.zeros((nq, 4), dtype=torch.float32, device="cuda")
+        ctx.radius_gather(0, pd.data_ptr(), nd.data_ptr(), nq, sq, expo, out.data_ptr())
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()[:, :3].astype(np.float64)
+        ref = oracle.radius_gather(pos, pw, pts, nrm, sq, expo)
+        scale = np.abs(ref).max()
+        assert scale > 0
+        np.testing.assert_allclose(got, ref, rtol=1e-4, atol=1e-6 * scale)
