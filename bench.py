@@ -136,6 +136,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_ranks(times, counts, device):
+    """Whole-job aggregation over the ranks of the default process group:
+    the slowest rank's times (max) and the sum of every rank's counts."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(times, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor(counts, dtype=torch.float64, device=device)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return t.tolist(), c.tolist()
+
+
 def cpu_frame_sample(scene, cfg, pixels, seed=1234):
     """The CPU restatement on a bounded sample of one frame: full photon
     emission, neighbour grids over both maps, `pixels` random pixels shaded
@@ -293,13 +305,9 @@ def run_ours(args):
     barrier()
 
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_total, t_e2e], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        g = torch.tensor([gathers, e2e_g, paths, launches], dtype=torch.float64, device="cuda")
-        dist.all_reduce(g, op=dist.ReduceOp.SUM)
-        t_total, t_e2e = t.tolist()
-        gathers, e2e_g, paths, launches = [int(x) for x in g.tolist()]
+        (t_total, t_e2e), (gathers, e2e_g, paths, launches) = reduce_ranks(
+            [t_total, t_e2e], [gathers, e2e_g, paths, launches], "cuda")
+        gathers, e2e_g, paths, launches = int(gathers), int(e2e_g), int(paths), int(launches)
     if rank != 0:
         return 0
 
