@@ -7,12 +7,12 @@
 // are stored.
 //
 // Top-down, one level at a time, all nodes of the level in parallel: every
-// record gets the 64-bit key (node within the level, coordinate along the
-// longest axis of its node's cell), a stable LSD radix sort orders the
-// records by it -- which leaves each node's records sorted along that axis,
-// so the node's first half (the left child) is the lower half: a median
-// split -- and each child's cell is its parent's cell cut at the median
-// coordinate. Equal keys keep their previous order, so the layout is
+// record gets the key (node within the level, coordinate along the longest
+// axis of its node's cell, quantised to 16 bits of the cell), a stable LSD
+// radix sort orders the records by it -- which leaves each node's records
+// sorted along that axis, so the node's first half (the left child) is the
+// lower half: a median split -- and each child's cell is its parent's cell
+// cut at the coordinate of the right child's first record. Equal keys keep their previous order, so the layout is
 // deterministic. The records are then permuted into that order (SoA float4
 // pos / pow) and every node gets the tight bounding box of its records,
 // bottom-up, which is what a query tests. The cells live in the node box
@@ -24,13 +24,6 @@
 namespace pm {
 namespace {
 
-__device__ __forceinline__ uint32_t orderable(float f) {
-    const uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float from_orderable(uint32_t u) {
-    return __uint_as_float((u & 0x80000000u) ? (u ^ 0x80000000u) : ~u);
-}
 __device__ __forceinline__ int longest_axis(float4 lo, float4 hi) {
     const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
     return (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
@@ -46,8 +39,9 @@ __global__ void root_cell_kernel(float3 lo, float3 hi, const float *box_dev, flo
     cell_hi[1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
 }
 
-// Key of record position i at level l: (node within the level, orderable
-// coordinate along the longest axis of the node's cell).
+// Key of record position i at level l: (node within the level, coordinate
+// along the longest axis of the node's cell, quantised to 16 bits of the
+// cell's extent). Records that quantise alike keep their previous order.
 __global__ void split_key_kernel(const float4 *__restrict__ pos, const uint32_t *__restrict__ order,
                                  uint32_t n, int level, uint32_t span,
                                  const float4 *__restrict__ cell_lo,
@@ -57,19 +51,25 @@ __global__ void split_key_kernel(const float4 *__restrict__ pos, const uint32_t 
     if (i >= n) return;
     const uint32_t node = i / span;
     const uint32_t g = (1u << level) + node;
-    const int ax = longest_axis(cell_lo[g], cell_hi[g]);
+    const float4 lo = cell_lo[g], hi = cell_hi[g];
+    const int ax = longest_axis(lo, hi);
     uint32_t src = i;
     if (order) src = order[i];
     else vals_init[i] = i;
     const float4 p = pos[src];
     const float c = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
-    keys[i] = ((uint64_t)node << 32) | orderable(c);
+    const float l0 = ax == 0 ? lo.x : (ax == 1 ? lo.y : lo.z);
+    const float l1 = ax == 0 ? hi.x : (ax == 1 ? hi.y : hi.z);
+    const float f = (c - l0) / (l1 - l0) * 65536.0f;
+    const uint32_t qc = !(f > 0.0f) ? 0u : (f >= 65535.0f ? 65535u : (uint32_t)f);
+    keys[i] = ((uint64_t)node << 16) | qc;
 }
 
 // Children cells of every node at `level`: the parent's cell cut at the
 // coordinate of the right child's first record.
-__global__ void split_cell_kernel(const uint64_t *__restrict__ keys, uint32_t n, int level,
-                                  uint32_t span, uint32_t nodes, float4 *cell_lo, float4 *cell_hi) {
+__global__ void split_cell_kernel(const float4 *__restrict__ pos, const uint32_t *__restrict__ order,
+                                  uint32_t n, int level, uint32_t span, uint32_t nodes,
+                                  float4 *cell_lo, float4 *cell_hi) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nodes) return;
     const uint32_t g = (1u << level) + j;
@@ -79,7 +79,8 @@ __global__ void split_cell_kernel(const uint64_t *__restrict__ keys, uint32_t n,
     float4 llo = lo, lhi = hi, rlo = lo, rhi = hi;
     if (cnt > half) {
         const int ax = longest_axis(lo, hi);
-        const float m = from_orderable((uint32_t)keys[start + half]);
+        const float4 p = pos[order[start + half]];
+        const float m = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
         if (ax == 0) { lhi.x = m; rlo.x = m; }
         else if (ax == 1) { lhi.y = m; rlo.y = m; }
         else { lhi.z = m; rlo.z = m; }
@@ -193,14 +194,14 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         while ((1u << node_bits) < nodes) ++node_bits;
         uint64_t *ko = nullptr;
         uint32_t *vo = nullptr;
-        e = radix_sort_pairs_u64(ka, va, kb, vb, a.n_dev, n, 0, 32 + node_bits, a.hist, s, &ko, &vo);
+        e = radix_sort_pairs_u64(ka, va, kb, vb, a.n_dev, n, 0, 16 + node_bits, a.hist, s, &ko, &vo);
         if (e != cudaSuccess) return e;
         if (vo != va) {
             uint64_t *tk = ka; ka = kb; kb = tk;
             uint32_t *tv = va; va = vb; vb = tv;
         }
-        split_cell_kernel<<<(nodes + 255) / 256, 256, 0, s>>>(ka, n, l, span, nodes, a.node_lo,
-                                                               a.node_hi); note_launch();
+        split_cell_kernel<<<(nodes + 255) / 256, 256, 0, s>>>(a.pos_in, va, n, l, span, nodes,
+                                                               a.node_lo, a.node_hi); note_launch();
     }
     permute_kernel<<<blocks, 256, 0, s>>>(va, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out); note_launch();
     const uint32_t first_leaf = 1u << D;

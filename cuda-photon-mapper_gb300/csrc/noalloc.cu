@@ -39,7 +39,9 @@ constexpr size_t kOffKeysTmp = kOffKeys + align256(8 * kMaxPoints);
 constexpr size_t kOffVals = kOffKeysTmp + align256(8 * kMaxPoints);
 constexpr size_t kOffValsTmp = kOffVals + align256(4 * kMaxPoints);
 constexpr size_t kOffHist = kOffValsTmp + align256(4 * kMaxPoints);
-constexpr size_t kOffIpos = kOffHist + align256(4 * 256 * kTiles);
+// digit counts of every tile plus the partial sums of their scan
+constexpr size_t kHistWords = 256 * kTiles + (256 * kTiles + kSortTile - 1) / kSortTile + 1;
+constexpr size_t kOffIpos = kOffHist + align256(4 * kHistWords);
 constexpr size_t kOffTpos = kOffIpos + align256(16 * kMaxPoints);
 constexpr size_t kOffLo = kOffTpos + align256(16 * kMaxPoints);
 constexpr size_t kOffHi = kOffLo + align256(16 * kNodes);

@@ -161,9 +161,20 @@ cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
     uint32_t *vin = vals, *vout = vals_tmp;
     uint32_t ntiles = (max_n + kSortTile - 1) / kSortTile;
     if (ntiles == 0) ntiles = 1;
+    // The digit-count scan runs in three multi-CTA steps once the histogram
+    // outgrows a few tiles; its tile partials live past the histogram.
+    const uint32_t hn = 256u * ntiles;
+    uint32_t *partials = hist + hn;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
         hist_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, n_dev, shift, hist, ntiles); note_launch();
-        scan_kernel<<<1, kScanThreads, 0, stream>>>(hist, hist, 256u * ntiles, nullptr); note_launch();
+        if (hn <= kSortTile) {
+            scan_kernel<<<1, kScanThreads, 0, stream>>>(hist, hist, hn, nullptr); note_launch();
+        } else {
+            const uint32_t tiles = scan_tile_count(hn);
+            tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(hist, hn, partials); note_launch();
+            scan_kernel<<<1, kScanThreads, 0, stream>>>(partials, partials, tiles, nullptr); note_launch();
+            tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(hist, hist, hn, partials); note_launch();
+        }
         scatter_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n_dev, shift,
                                                                hist, ntiles); note_launch();
         K *tk = kin; kin = kout; kout = tk;

@@ -18,11 +18,13 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr uint32_t kSortTile = kSortThreads * kSortItems;
 
-// Number of uint32 words of scratch the sort needs for max_n elements.
+// Number of uint32 words of scratch the sort needs for max_n elements: the
+// digit counts of every tile plus the partial sums of their scan.
 inline size_t radix_sort_hist_words(uint32_t max_n) {
     uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
     if (tiles == 0) tiles = 1;
-    return (size_t)256 * tiles;
+    const size_t hn = (size_t)256 * tiles;
+    return hn + (hn + kSortTile - 1) / kSortTile + 1;
 }
 
 // Sorts keys[0..n) with their values by bits [begin_bit, end_bit), n read

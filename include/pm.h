@@ -263,7 +263,7 @@ PM_API pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const f
  * other host threads on the same device) race and must be serialised by the
  * caller. Needs no pm_ctx. */
 #define PM_KNN_NOALLOC_MAX_POINTS (1u << 17)
-#define PM_KNN_NOALLOC_SCRATCH_BYTES 7635200u
+#define PM_KNN_NOALLOC_SCRATCH_BYTES 7635456u
 PM_API pm_status pm_knn_noalloc(const float4 *points, uint32_t n, const float4 *queries,
                                 uint32_t nq, int k, float radius, uint32_t *idx_out,
                                 float *d2_out, cudaStream_t stream);
