@@ -167,9 +167,10 @@ __global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) {
     }
     Path p;
     bool live = false;
+    bool exhausted = false;  // no path ids left to issue (warp-uniform)
     for (;;) {
         unsigned empty = __ballot_sync(0xffffffffu, !live);
-        if (empty) {
+        if (empty && !exhausted) {
             const int leader = __ffs(empty) - 1;
             uint32_t base = cap;
             if (lane == leader) {
@@ -178,15 +179,22 @@ __global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) {
                 if (!full) base = atomicAdd(P.path_counter, (uint32_t)__popc(empty));
             }
             base = __shfl_sync(0xffffffffu, base, leader);
+            exhausted = base >= cap;
             if (!live) {
                 uint32_t id = base + (uint32_t)__popc(empty & lanemask_lt());
-                if (base < cap && id < cap) {
+                // the writing pass retraces only paths with a record in a map
+                const bool needed = !P.store || (id < ms.paths && P.cnt_s[id] > 0u) ||
+                                    (id < mv.paths && P.cnt_v[id] > 0u);
+                if (base < cap && id < cap && needed) {
                     start_path(P, id, p, S);
                     live = true;
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, live)) break;
+        if (!__any_sync(0xffffffffu, live)) {
+            if (exhausted) break;
+            continue;
+        }
         if (live) {
             if (!step_path(S, P, p, ms, mv)) {
                 if (!P.store) {

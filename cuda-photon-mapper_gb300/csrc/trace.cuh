@@ -17,9 +17,10 @@ struct TraceParams {
     uint32_t *path_counter;       // next path id (zeroed before each pass)
     uint32_t *stored_s, *stored_v;
     uint32_t *cnt_s, *cnt_v;      // records per path (zeroed before the counting pass)
-    // Writing pass (store != 0): paths [0, max(ext_s[1], ext_v[1])) again,
-    // each record written straight to map index off[p] + k when below the
-    // map size ext[0], power scaled by power / ext[1].
+    // Writing pass (store != 0): the paths below max(ext_s[1], ext_v[1])
+    // that hold a record of a map (cnt > 0) are traced again, each record
+    // written straight to map index off[p] + k when below the map size
+    // ext[0], power scaled by power / ext[1].
     int store;
     const uint32_t *off_s, *off_v;
     const uint32_t *ext_s, *ext_v;
