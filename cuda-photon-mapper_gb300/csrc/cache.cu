@@ -1,0 +1,769 @@
+// cache.cu -- the learned radiance cache: query lists, hash-grid encoding,
+// the fused tcgen05 training and inference kernels, Adam, composite.
+//
+// Network: x (64 features) -> 4 x [64 x 64, ReLU] -> [64 x 16] -> rgb in
+// columns 0..2; no biases (feature 52 is a constant 1). Features:
+//   0..31   16 hash-grid levels x 2 fp16 features, trilinear
+//   32..47  real spherical harmonics of wo, degrees 0..3
+//   48..50  facing normal (diffuse queries; zero in the medium)
+//   51      1 for a diffuse query, 0 for a medium query
+//   52      1
+// Loss: relative L2, sum_c (y_c - t_c)^2 / (y_c^2 + eps) with y_c held
+// constant in the denominator, averaged over 3 x batch (targets are
+// divided by their mean first; eps = 0.01 by default).
+//
+// Tensor-core tiles hold 128 samples (one per TMEM lane; thread s of the
+// 128-thread CTA owns sample s). Activations live in shared memory as bf16
+// in the no-swizzle core-matrix layout of tc.cuh. The training kernel keeps
+// every layer's activations (H0 = x .. H4) and activation gradients (dZ1 ..
+// dZ4) of the tile in "pair" buffers of 128 samples x 128 features, so that
+//   forward  Z_{l+1} = H_l W_l       A = H_l  (K-major),  B = W_l (K-major)
+//   backward dH_l = dZ_{l+1} W_l^T   A = dZ   (K-major),  B = W_l (MN-major)
+//   weights  [dW_a | . ; . | dW_b] = [H_a ; H_b]^T [dZ_a+1 , dZ_b+1]
+//                                    A, B = the pair buffers (MN-major)
+// all read the same bytes: no transposed copies. The weight gradients of a
+// CTA accumulate over its tiles in TMEM (M = 128 rows = two layers' inputs,
+// N = 128 columns = their two output blocks; the off-diagonal blocks are
+// unused) and are added to global memory once at the end.
+#include "cache.cuh"
+#include "eye_path.cuh"
+#include "launch_count.cuh"
+#include "tc.cuh"
+
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cmath>
+
+namespace pm {
+namespace {
+
+constexpr int kThreads = kCacheTile;
+
+// Shared-memory layout of the training kernel (bytes).
+constexpr uint32_t kWBytes = 4 * 8192 + 2048;          // bf16 weights, B-operand layout
+constexpr uint32_t kPair = 32768;                      // 128 samples x 128 features bf16
+constexpr uint32_t kOffP0 = kWBytes;                   // H0 | H1
+constexpr uint32_t kOffP1 = kOffP0 + kPair;            // H2 | H3
+constexpr uint32_t kOffP2 = kOffP1 + kPair;            // H4 | unused
+constexpr uint32_t kOffQ0 = kOffP2 + kPair;            // dZ1 | dZ2
+constexpr uint32_t kOffQ1 = kOffQ0 + kPair;            // dZ3 | dZ4
+constexpr uint32_t kOffGY = kOffQ1 + kPair;            // dL/dy, 128 x 16
+constexpr uint32_t kTrainSmem = kOffGY + 4096;
+constexpr uint32_t kPairSbo = 2048;                    // 8-sample groups in a pair buffer
+// Inference: weights + one 128 x 64 activation tile.
+constexpr uint32_t kOffAct = kWBytes;
+constexpr uint32_t kInferSmem = kOffAct + 16384;
+constexpr uint32_t kActSbo = 1024;
+constexpr int kInferCtasPerSm = 4;
+
+// TMEM columns of the training kernel.
+constexpr uint32_t kColDW01 = 128, kColDW23 = 256, kColDW4 = 384, kTrainCols = 512;
+constexpr uint32_t kInferCols = 64;
+
+// Byte offset of feature f (a multiple of 8) of sample s in an activation
+// buffer whose 8-sample groups are sbo bytes apart.
+__device__ __forceinline__ uint32_t row_off(int s, int f, uint32_t sbo) {
+    return (uint32_t)(s >> 3) * sbo + (uint32_t)(f >> 3) * 128u + (uint32_t)(s & 7) * 16u;
+}
+
+__device__ __forceinline__ uint32_t pack_bf2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void st8(unsigned char *base, uint32_t off, const float *v) {
+    *reinterpret_cast<uint4 *>(base + off) = make_uint4(pack_bf2(v[0], v[1]), pack_bf2(v[2], v[3]),
+                                                        pack_bf2(v[4], v[5]), pack_bf2(v[6], v[7]));
+}
+
+__device__ __forceinline__ void ld8(const unsigned char *base, uint32_t off, float *v) {
+    const uint4 u = *reinterpret_cast<const uint4 *>(base + off);
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[2 * j] = __uint_as_float(w[j] << 16);
+        v[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
+    }
+}
+
+// fp32 [in][out] weights -> bf16 B operands: element (out, in) of layer l at
+// l * 8192 + core_offset(out, in, 64); the output layer (16 x 64) at 32768.
+__device__ void load_weights(unsigned char *sw, const float *w) {
+    for (int i = threadIdx.x; i < kCacheWeights; i += blockDim.x) {
+        uint32_t off;
+        if (i < 4 * 4096) {
+            const int l = i >> 12, r = i & 4095;
+            off = (uint32_t)l * 8192u + core_offset(r & 63, r >> 6, 64);
+        } else {
+            const int r = i - 4 * 4096;
+            off = 32768u + core_offset(r & 15, r >> 4, 64);
+        }
+        *reinterpret_cast<__nv_bfloat16 *>(sw + off) = __float2bfloat16(w[i]);
+    }
+}
+
+__device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// Table slots and trilinear weights of the 8 corners around p (in [0,1]^3)
+// on level l: vertices 0..res per axis, dense indexing while (res+1)^3 fits
+// the level, the spatial hash x ^ 2654435761 y ^ 805459861 z beyond.
+__device__ __forceinline__ void level_corners(const CacheGrid &g, int l, float px, float py,
+                                              float pz, uint32_t *idx, float *w) {
+    const int r = g.res[l];
+    const float fx = px * (float)r, fy = py * (float)r, fz = pz * (float)r;
+    const int ix = min((int)fx, r - 1), iy = min((int)fy, r - 1), iz = min((int)fz, r - 1);
+    const float tx = fx - (float)ix, ty = fy - (float)iy, tz = fz - (float)iz;
+    const uint32_t stride = (uint32_t)r + 1u;
+    const bool dense = (uint64_t)stride * stride * stride <= (1ull << g.log2_t);
+    const uint32_t mask = (1u << g.log2_t) - 1u;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t cx = (uint32_t)ix + (c & 1), cy = (uint32_t)iy + ((c >> 1) & 1),
+                       cz = (uint32_t)iz + (c >> 2);
+        idx[c] = dense ? cx + stride * (cy + stride * cz)
+                       : (cx ^ (cy * 2654435761u) ^ (cz * 805459861u)) & mask;
+        const float wx = (c & 1) ? tx : 1.0f - tx;
+        const float wy = (c & 2) ? ty : 1.0f - ty;
+        const float wz = (c & 4) ? tz : 1.0f - tz;
+        w[c] = (wx * wy) * wz;
+    }
+}
+
+// Real spherical harmonics of a unit direction, degrees 0..3.
+__device__ __forceinline__ void sh16(float x, float y, float z, float *o) {
+    const float xx = x * x, yy = y * y, zz = z * z;
+    o[0] = 0.28209479177387814f;
+    o[1] = -0.48860251190291987f * y;
+    o[2] = 0.48860251190291987f * z;
+    o[3] = -0.48860251190291987f * x;
+    o[4] = 1.0925484305920792f * x * y;
+    o[5] = -1.0925484305920792f * y * z;
+    o[6] = 0.94617469575755997f * zz - 0.31539156525251999f;
+    o[7] = -1.0925484305920792f * x * z;
+    o[8] = 0.54627421529603959f * (xx - yy);
+    o[9] = 0.59004358992664352f * y * (-3.0f * xx + yy);
+    o[10] = 2.8906114426405538f * x * y * z;
+    o[11] = 0.45704579946446572f * y * (1.0f - 5.0f * zz);
+    o[12] = 0.3731763325901154f * z * (5.0f * zz - 3.0f);
+    o[13] = 0.45704579946446572f * x * (1.0f - 5.0f * zz);
+    o[14] = 1.4453057213202769f * z * (xx - yy);
+    o[15] = 0.59004358992664352f * x * (-xx + 3.0f * yy);
+}
+
+struct QueryPos {
+    float px, py, pz;
+};
+
+__device__ __forceinline__ QueryPos unit_pos(const CacheGrid &g, float4 a) {
+    QueryPos q;
+    q.px = clamp01((a.x - g.lo[0]) * g.inv_size[0]);
+    q.py = clamp01((a.y - g.lo[1]) * g.inv_size[1]);
+    q.pz = clamp01((a.z - g.lo[2]) * g.inv_size[2]);
+    return q;
+}
+
+// Encodes one query into row `row` of an activation buffer (features
+// 0..63, bf16); dbg (nullable) receives the fp32 features.
+__device__ void encode_row(unsigned char *act, uint32_t sbo, int row, const CacheGrid &g,
+                           const __half2 *tab, const PScene &Sc, float4 a, float4 d, bool valid,
+                           float *dbg) {
+    float v[8];
+    if (!valid) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) st8(act, row_off(row, 8 * c, sbo), v);
+        return;
+    }
+    const QueryPos q = unit_pos(g, a);
+    const size_t T = (size_t)1 << g.log2_t;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int l = 4 * c + j;
+            float f0 = 0.0f, f1 = 0.0f;
+            if (l < g.levels) {
+                uint32_t idx[8];
+                float w[8];
+                level_corners(g, l, q.px, q.py, q.pz, idx, w);
+                const __half2 *lv = tab + (size_t)l * T;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const float2 h = __half22float2(__ldg(lv + idx[k]));
+                    f0 += w[k] * h.x;
+                    f1 += w[k] * h.y;
+                }
+            }
+            v[2 * j] = f0;
+            v[2 * j + 1] = f1;
+        }
+        st8(act, row_off(row, 8 * c, sbo), v);
+        if (dbg)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) dbg[8 * c + j] = v[j];
+    }
+    float sh[16];
+    sh16(d.x, d.y, d.z, sh);
+    st8(act, row_off(row, 32, sbo), sh);
+    st8(act, row_off(row, 40, sbo), sh + 8);
+    const int obj = __float_as_int(a.w);
+    v3 nf = mk3(0.0f, 0.0f, 0.0f);
+    float kind = 0.0f;
+    if (obj != kNone) {
+        nf = facing_normal(Sc, obj, mk3(a.x, a.y, a.z), mk3(d.x, d.y, d.z));
+        kind = 1.0f;
+    }
+    float t[16] = {nf.x, nf.y, nf.z, kind, 1.0f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    st8(act, row_off(row, 48, sbo), t);
+    st8(act, row_off(row, 56, sbo), t + 8);
+    if (dbg) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) dbg[32 + j] = sh[j];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) dbg[48 + j] = t[j];
+    }
+}
+
+// Runs `issue` on thread 0 after the CTA's shared-memory writes are visible
+// to the tensor core, commits, and waits for completion. false when the
+// bounded wait ran out.
+template <class F>
+__device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, F issue) {
+    publish_smem();
+    __syncthreads();
+    after_sync();
+    if (threadIdx.x == 0) {
+        issue();
+        mma_commit(mbar);
+    }
+    const bool ok = mbar_wait(mbar, phase);
+    phase ^= 1u;
+    after_sync();
+    return ok;
+}
+
+// K-major operand descriptor sequence helper: nk MMAs of K = 16.
+__device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t a_step, uint32_t a_lbo,
+                                          uint32_t a_sbo, uint32_t b, uint32_t b_step,
+                                          uint32_t b_lbo, uint32_t b_sbo, int nk, uint32_t idesc,
+                                          bool acc_first) {
+    for (int k = 0; k < nk; ++k)
+        mma_bf16(d, smem_desc(a + k * a_step, a_lbo, a_sbo), smem_desc(b + k * b_step, b_lbo, b_sbo),
+                 idesc, (k > 0 || acc_first) ? 1u : 0u);
+}
+
+// Hidden-layer epilogue: TMEM columns 0..63 of this thread's row -> ReLU ->
+// bf16 at dst (activation buffer with 8-sample stride sbo).
+__device__ __forceinline__ void relu_out(uint32_t taddr, unsigned char *dst, uint32_t sbo, int row) {
+#pragma unroll 1
+    for (int c = 0; c < 64; c += 16) {
+        float v[16];
+        tmem_ld16(taddr, c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.0f);
+        st8(dst, row_off(row, c, sbo), v);
+        st8(dst, row_off(row, c + 8, sbo), v + 8);
+    }
+}
+
+// Backward epilogue: dZ = dH (TMEM 0..63) where H > 0, else 0.
+__device__ __forceinline__ void relu_grad(uint32_t taddr, const unsigned char *h, unsigned char *dz,
+                                          int row) {
+#pragma unroll 1
+    for (int c = 0; c < 64; c += 16) {
+        float v[16], hv[16];
+        tmem_ld16(taddr, c, v);
+        ld8(h, row_off(row, c, kPairSbo), hv);
+        ld8(h, row_off(row, c + 8, kPairSbo), hv + 8);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = hv[j] > 0.0f ? v[j] : 0.0f;
+        st8(dz, row_off(row, c, kPairSbo), v);
+        st8(dz, row_off(row, c + 8, kPairSbo), v + 8);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    train_kernel(CacheGrid g, CacheParams p, PScene Sc, const float4 *qa, const float4 *qd,
+                 const uint32_t *sel, const float4 *val, uint32_t n, float inv_scale,
+                 float loss_norm, float rel_eps, float *x_out, float *y_out) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t taddr_s;
+    __shared__ int abort_s;
+    __shared__ float red[kThreads / 32];
+    const int s = threadIdx.x, warp = s >> 5;
+    const uint32_t ntiles = (n + kThreads - 1) / kThreads;
+
+    load_weights(sm, p.w);
+    for (uint32_t i = s; i < kPair / 16; i += kThreads)  // the unused half of P2 stays finite
+        reinterpret_cast<uint4 *>(sm + kOffP2)[i] = make_uint4(0, 0, 0, 0);
+    if (s == 0) {
+        mbar_init(&mbar);
+        abort_s = 0;
+    }
+    if (warp == 0) tmem_alloc(&taddr_s, kTrainCols);
+    publish_smem();
+    __syncthreads();
+    after_sync();
+    const uint32_t taddr = taddr_s;
+    const uint32_t base = smem_addr(sm);
+    const uint32_t aP[3] = {base + kOffP0, base + kOffP1, base + kOffP2};
+    const uint32_t aQ[2] = {base + kOffQ0, base + kOffQ1};
+    const uint32_t aW = base, aGY = base + kOffGY;
+    uint32_t phase = 0;
+    float lsum = 0.0f;
+    bool first = true, ok = true;
+    const size_t T = (size_t)1 << g.log2_t;
+
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t i = tile * kThreads + s;
+        const bool valid = i < n;
+        const uint32_t qi = valid ? (sel ? sel[i] : i) : 0u;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
+        if (valid) {
+            a = qa[qi];
+            d = qd[qi];
+        }
+        encode_row(sm + kOffP0, kPairSbo, s, g, p.table_h, Sc, a, d, valid,
+                   (valid && x_out) ? x_out + (size_t)i * 64 : nullptr);
+        // forward, hidden layers: H_{l+1} = relu(H_l W_l)
+        for (int l = 0; l < 4; ++l) {
+            const uint32_t src = aP[l >> 1] + (uint32_t)(l & 1) * 1024u;
+            ok &= tc_round(&mbar, phase, [&] {
+                mma_chain(taddr, src, 256, 128, kPairSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
+                          idesc_bf16(128, 64), false);
+            });
+            const int o = l + 1;
+            relu_out(taddr, sm + kOffP0 + (uint32_t)(o >> 1) * kPair + (uint32_t)(o & 1) * 1024u,
+                     kPairSbo, s);
+        }
+        // output layer: y = H4 W4
+        ok &= tc_round(&mbar, phase, [&] {
+            mma_chain(taddr, aP[2], 256, 128, kPairSbo, aW + 32768u, 256, 128, 1024, 4,
+                      idesc_bf16(128, 16), false);
+        });
+        float y[16];
+        tmem_ld16(taddr, 0, y);
+        float gy[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) gy[j] = 0.0f;
+        if (valid) {
+            const float4 t4 = val[i];
+            const float t[3] = {t4.x * inv_scale, t4.y * inv_scale, t4.z * inv_scale};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float diff = y[c] - t[c];
+                const float den = y[c] * y[c] + rel_eps;
+                lsum += diff * diff / den;
+                gy[c] = 2.0f * diff / den * loss_norm;
+            }
+            if (y_out)
+                reinterpret_cast<float4 *>(y_out)[i] = make_float4(y[0], y[1], y[2], 0.0f);
+        }
+        {
+            const uint32_t go = (uint32_t)(s >> 3) * 256u + (uint32_t)(s & 7) * 16u;
+            st8(sm + kOffGY, go, gy);
+            st8(sm + kOffGY, go + 128u, gy + 8);
+        }
+        // dH4 = GY W4^T (B = the output layer read MN-major)
+        ok &= tc_round(&mbar, phase, [&] {
+            mma_chain(taddr, aGY, 0, 128, 256, aW + 32768u, 0, 1024, 128, 1,
+                      idesc_bf16(128, 64, 0, 1), false);
+        });
+        relu_grad(taddr, sm + kOffP2, sm + kOffQ1 + 1024u, s);  // dZ4
+        // dH_l = dZ_{l+1} W_l^T for l = 3, 2, 1
+        for (int l = 3; l >= 1; --l) {
+            const uint32_t dz = aQ[l >> 1] + (uint32_t)(l & 1) * 1024u;  // dZ_{l+1}
+            ok &= tc_round(&mbar, phase, [&] {
+                mma_chain(taddr, dz, 256, 128, kPairSbo, aW + (uint32_t)l * 8192u, 2048, 1024, 128, 4,
+                          idesc_bf16(128, 64, 0, 1), false);
+            });
+            const unsigned char *h = sm + kOffP0 + (uint32_t)(l >> 1) * kPair + (uint32_t)(l & 1) * 1024u;
+            unsigned char *dzl = sm + kOffQ0 + (uint32_t)((l - 1) >> 1) * kPair + (uint32_t)((l - 1) & 1) * 1024u;
+            relu_grad(taddr, h, dzl, s);
+        }
+        // dX = dZ1 W0^T, and the weight gradients of the tile
+        const bool acc = !first;
+        ok &= tc_round(&mbar, phase, [&] {
+            mma_chain(taddr, aQ[0], 256, 128, kPairSbo, aW, 2048, 1024, 128, 4,
+                      idesc_bf16(128, 64, 0, 1), false);
+            mma_chain(taddr + kColDW01, aP[0], 4096, kPairSbo, 128, aQ[0], 4096, kPairSbo, 128, 8,
+                      idesc_bf16(128, 128, 1, 1), acc);
+            mma_chain(taddr + kColDW23, aP[1], 4096, kPairSbo, 128, aQ[1], 4096, kPairSbo, 128, 8,
+                      idesc_bf16(128, 128, 1, 1), acc);
+            mma_chain(taddr + kColDW4, aP[2], 4096, kPairSbo, 128, aGY, 512, 256, 128, 8,
+                      idesc_bf16(128, 16, 1, 1), acc);
+        });
+        first = false;
+        float dx[32];
+        tmem_ld16(taddr, 0, dx);
+        tmem_ld16(taddr, 16, dx + 16);
+        if (valid && ok) {
+            const QueryPos q = unit_pos(g, a);
+            for (int l = 0; l < g.levels; ++l) {
+                uint32_t idx[8];
+                float w[8];
+                level_corners(g, l, q.px, q.py, q.pz, idx, w);
+                float2 *lv = p.table_grad + (size_t)l * T;
+                const float g0 = dx[2 * l], g1 = dx[2 * l + 1];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) atomicAdd(lv + idx[k], make_float2(w[k] * g0, w[k] * g1));
+            }
+        }
+        if (!ok) abort_s = 1;
+        __syncthreads();
+        if (abort_s) {
+            ok = false;
+            break;
+        }
+    }
+    // weight gradients of this CTA -> global
+    if (!first && ok) {
+        const int half = warp >> 1;
+        const int in = s & 63;
+#pragma unroll 1
+        for (int pr = 0; pr < 2; ++pr) {
+            const int l = 2 * pr + half;
+            const uint32_t col = (pr == 0 ? kColDW01 : kColDW23) + (uint32_t)half * 64u;
+#pragma unroll 1
+            for (int c = 0; c < 64; c += 16) {
+                float v[16];
+                tmem_ld16(taddr, (int)col + c, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) atomicAdd(&p.w_grad[l * 4096 + in * 64 + c + j], v[j]);
+            }
+        }
+        if (warp < 2) {
+            float v[16];
+            tmem_ld16(taddr, (int)kColDW4, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) atomicAdd(&p.w_grad[4 * 4096 + s * 16 + j], v[j]);
+        }
+    }
+    if (!ok && s == 0) atomicExch(p.status, 1);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+    if ((s & 31) == 0) red[warp] = lsum;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (s == 0) atomicAdd(p.loss, (red[0] + red[1] + red[2] + red[3]) * loss_norm);
+    if (warp == 0) tmem_free(taddr, kTrainCols);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    infer_kernel(CacheGrid g, CacheParams p, PScene Sc, const float4 *qa, const float4 *qd,
+                 uint32_t n, float out_scale, float4 *val) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t taddr_s;
+    __shared__ int abort_s;
+    const int s = threadIdx.x, warp = s >> 5;
+    const uint32_t ntiles = (n + kThreads - 1) / kThreads;
+    load_weights(sm, p.w);
+    if (s == 0) {
+        mbar_init(&mbar);
+        abort_s = 0;
+    }
+    if (warp == 0) tmem_alloc(&taddr_s, kInferCols);
+    publish_smem();
+    __syncthreads();
+    after_sync();
+    const uint32_t taddr = taddr_s;
+    const uint32_t aW = smem_addr(sm), aA = aW + kOffAct;
+    unsigned char *act = sm + kOffAct;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t i = tile * kThreads + s;
+        const bool valid = i < n;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
+        if (valid) {
+            a = qa[i];
+            d = qd[i];
+        }
+        encode_row(act, kActSbo, s, g, p.table_h, Sc, a, d, valid, nullptr);
+        for (int l = 0; l < 4; ++l) {
+            ok &= tc_round(&mbar, phase, [&] {
+                mma_chain(taddr, aA, 256, 128, kActSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
+                          idesc_bf16(128, 64), false);
+            });
+            relu_out(taddr, act, kActSbo, s);
+        }
+        ok &= tc_round(&mbar, phase, [&] {
+            mma_chain(taddr, aA, 256, 128, kActSbo, aW + 32768u, 256, 128, 1024, 4,
+                      idesc_bf16(128, 16), false);
+        });
+        float y[16];
+        tmem_ld16(taddr, 0, y);
+        if (valid && ok)
+            val[i] = make_float4(fmaxf(y[0], 0.0f) * out_scale, fmaxf(y[1], 0.0f) * out_scale,
+                                 fmaxf(y[2], 0.0f) * out_scale, 0.0f);
+        if (!ok) abort_s = 1;
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        if (abort_s) {
+            ok = false;
+            break;
+        }
+    }
+    if (!ok && s == 0) atomicExch(p.status, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) tmem_free(taddr, kInferCols);
+}
+
+__global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph, uint32_t npairs,
+                            float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
+        float2 pp = reinterpret_cast<float2 *>(p)[i];
+        const float2 gg = reinterpret_cast<float2 *>(gr)[i];
+        float2 mm = reinterpret_cast<float2 *>(m)[i];
+        float2 vv = reinterpret_cast<float2 *>(v)[i];
+        mm.x = b1 * mm.x + (1.0f - b1) * gg.x;
+        mm.y = b1 * mm.y + (1.0f - b1) * gg.y;
+        vv.x = b2 * vv.x + (1.0f - b2) * gg.x * gg.x;
+        vv.y = b2 * vv.y + (1.0f - b2) * gg.y * gg.y;
+        pp.x -= lr * (mm.x * c1) / (sqrtf(vv.x * c2) + eps);
+        pp.y -= lr * (mm.y * c1) / (sqrtf(vv.y * c2) + eps);
+        reinterpret_cast<float2 *>(p)[i] = pp;
+        reinterpret_cast<float2 *>(m)[i] = mm;
+        reinterpret_cast<float2 *>(v)[i] = vv;
+        reinterpret_cast<float2 *>(gr)[i] = make_float2(0.0f, 0.0f);
+        if (ph) ph[i] = __floats2half2_rn(pp.x, pp.y);
+    }
+}
+
+__global__ void init_kernel(float *p, float *gr, float *m, float *v, __half2 *ph, uint32_t npairs,
+                            uint64_t seed, uint32_t salt, int hidden_pairs, float a_hidden,
+                            float a_out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
+        const pm_u32x4 r = philox(seed, i, salt, 0x1A17u, 0u);
+        const float a = (hidden_pairs < 0 || (int)i < hidden_pairs) ? a_hidden : a_out;
+        const float x0 = (2.0f * pm_u01(r.v[0]) - 1.0f) * a;
+        const float x1 = (2.0f * pm_u01(r.v[1]) - 1.0f) * a;
+        reinterpret_cast<float2 *>(p)[i] = make_float2(x0, x1);
+        reinterpret_cast<float2 *>(gr)[i] = make_float2(0.0f, 0.0f);
+        reinterpret_cast<float2 *>(m)[i] = make_float2(0.0f, 0.0f);
+        reinterpret_cast<float2 *>(v)[i] = make_float2(0.0f, 0.0f);
+        if (ph) ph[i] = __floats2half2_rn(x0, x1);
+    }
+}
+
+__global__ void half_copy_kernel(const float *p, __half2 *ph, uint32_t npairs) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
+        const float2 v = reinterpret_cast<const float2 *>(p)[i];
+        ph[i] = __floats2half2_rn(v.x, v.y);
+    }
+}
+
+struct CountSink {
+    uint32_t n = 0, ns = 0;
+    __device__ void volume(v3, v3, float) { ++n; }
+    __device__ void surface(v3, int, v3, float) { ++n; ++ns; }
+};
+
+struct WriteSink {
+    float4 *qa, *qd;
+    uint32_t *slist;
+    uint32_t at, sat;
+    __device__ void volume(v3 x, v3 wo, float w) {
+        qa[at] = make_float4(x.x, x.y, x.z, __int_as_float(kNone));
+        qd[at] = make_float4(wo.x, wo.y, wo.z, w);
+        ++at;
+    }
+    __device__ void surface(v3 x, int obj, v3 wo, float w) {
+        slist[sat++] = at;
+        qa[at] = make_float4(x.x, x.y, x.z, __int_as_float(obj));
+        qd[at] = make_float4(wo.x, wo.y, wo.z, w);
+        ++at;
+    }
+};
+
+__global__ void count_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on, uint32_t *cnt,
+                             uint32_t *scnt) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= (uint32_t)R.width * (uint32_t)R.height) return;
+    CountSink c;
+    walk_eye(Sc, R, pix, vol_on, surf_on, c);
+    cnt[pix] = c.n;
+    scnt[pix] = c.ns;
+}
+
+__global__ void write_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on,
+                             const uint32_t *off, const uint32_t *soff, float4 *qa, float4 *qd,
+                             uint32_t *slist) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= (uint32_t)R.width * (uint32_t)R.height) return;
+    WriteSink w{qa, qd, slist, off[pix], soff[pix]};
+    walk_eye(Sc, R, pix, vol_on, surf_on, w);
+}
+
+__global__ void composite_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
+                                 const float4 *val, uint32_t npix, float exposure, float4 *rad,
+                                 uchar4 *rgba) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    v3 L = mk3(0.f, 0.f, 0.f);
+    const uint32_t e = off[pix + 1];
+    for (uint32_t i = off[pix]; i < e; ++i) {
+        const int obj = __float_as_int(qa[i].w);
+        const float w = qd[i].w;
+        const float4 v = val[i];
+        if (obj != kNone) {
+            const v3 al = material_albedo(Sc, obj);
+            L = L + mk3(al.x * (v.x * w), al.y * (v.y * w), al.z * (v.z * w));
+        } else {
+            L = L + mk3(v.x * w, v.y * w, v.z * w);
+        }
+    }
+    if (rad) rad[pix] = make_float4(L.x, L.y, L.z, 1.0f);
+    if (rgba)
+        rgba[pix] = make_uchar4(to_u8_sat((double)(L.x * exposure) * 255.0),
+                                to_u8_sat((double)(L.y * exposure) * 255.0),
+                                to_u8_sat((double)(L.z * exposure) * 255.0), 255);
+}
+
+__global__ void select_kernel(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
+                              uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const pm_u32x4 r = philox(seed, i, frame, 0x5E1Eu, 0u);
+    if (ns_total > 0 && pm_u01(r.v[1]) < surf_frac)
+        sel[i] = slist[(uint32_t)(((uint64_t)r.v[0] * ns_total) >> 32)];
+    else
+        sel[i] = (uint32_t)(((uint64_t)r.v[0] * total) >> 32);
+}
+
+__global__ void value_sum_kernel(const float4 *val, uint32_t n, float *sum) {
+    float acc = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 v = val[i];
+        acc += (v.x + v.y + v.z) * (1.0f / 3.0f);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+}
+
+}  // namespace
+
+cudaError_t cache_count_queries(const PScene &S, const RenderParams &R, bool vol_on, bool surf_on,
+                                uint32_t *cnt, uint32_t *scnt, cudaStream_t s) {
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
+    if (npix == 0) return cudaSuccess;
+    count_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, R, vol_on, surf_on, cnt, scnt);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_write_queries(const PScene &S, const RenderParams &R, bool vol_on, bool surf_on,
+                                const uint32_t *off, const uint32_t *soff, float4 *qa, float4 *qd,
+                                uint32_t *slist, cudaStream_t s) {
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
+    if (npix == 0) return cudaSuccess;
+    write_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, R, vol_on, surf_on, off, soff, qa, qd, slist);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *qa,
+                            const float4 *qd, const float4 *val, uint32_t npix, float exposure,
+                            float4 *rad, uchar4 *rgba, cudaStream_t s) {
+    if (npix == 0) return cudaSuccess;
+    composite_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, off, qa, qd, val, npix, exposure, rad, rgba);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
+                         uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel,
+                         cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    select_kernel<<<(n + 255) / 256, 256, 0, s>>>(seed, frame, total, slist, ns_total, n, surf_frac, sel);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 1024);
+    value_sum_kernel<<<blocks, 256, 0, s>>>(val, n, sum);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_init(const CacheGrid &g, const CacheParams &p, uint64_t seed, cudaStream_t s) {
+    const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));  // 2 floats per entry
+    init_kernel<<<1024, 256, 0, s>>>(p.table, reinterpret_cast<float *>(p.table_grad), p.table_m,
+                                     p.table_v, p.table_h, tpairs, seed, 0x7AB1Eu, -1, 1e-4f, 1e-4f);
+    note_launch();
+    const float a = sqrtf(6.0f / 64.0f);
+    init_kernel<<<(kCacheWeights / 2 + 255) / 256, 256, 0, s>>>(p.w, p.w_grad, p.w_m, p.w_v, nullptr,
+                                                                kCacheWeights / 2, seed, 0x3E16u,
+                                                                4 * 4096 / 2, a, a);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_sync_half(const CacheGrid &g, const CacheParams &p, cudaStream_t s) {
+    const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));
+    half_copy_kernel<<<1024, 256, 0, s>>>(p.table, p.table_h, tpairs);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScene &S,
+                           const float4 *qa, const float4 *qd, const uint32_t *sel,
+                           const float4 *val, uint32_t n, float inv_scale, float loss_norm,
+                           float rel_eps, float *x_out, float *y_out, int sm_count, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kTrainSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint32_t ntiles = (n + kThreads - 1) / kThreads;
+    const uint32_t grid = std::min<uint32_t>(ntiles, (uint32_t)sm_count);
+    train_kernel<<<grid, kThreads, kTrainSmem, s>>>(g, p, S, qa, qd, sel, val, n, inv_scale, loss_norm,
+                                                    rel_eps, x_out, y_out);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float beta1,
+                       float beta2, float eps, int step, cudaStream_t s) {
+    const float c1 = 1.0f / (1.0f - powf(beta1, (float)step));
+    const float c2 = 1.0f / (1.0f - powf(beta2, (float)step));
+    const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));
+    adam_kernel<<<2048, 256, 0, s>>>(p.table, reinterpret_cast<float *>(p.table_grad), p.table_m,
+                                     p.table_v, p.table_h, tpairs, lr, beta1, beta2, eps, c1, c2);
+    note_launch();
+    adam_kernel<<<(kCacheWeights / 2 + 255) / 256, 256, 0, s>>>(p.w, p.w_grad, p.w_m, p.w_v, nullptr,
+                                                                kCacheWeights / 2, lr, beta1, beta2,
+                                                                eps, c1, c2);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &S,
+                        const float4 *qa, const float4 *qd, uint32_t n, float out_scale,
+                        float4 *val, int sm_count, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kInferSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint32_t ntiles = (n + kThreads - 1) / kThreads;
+    const uint32_t grid = std::min<uint32_t>(ntiles, (uint32_t)sm_count * kInferCtasPerSm);
+    infer_kernel<<<grid, kThreads, kInferSmem, s>>>(g, p, S, qa, qd, n, out_scale, val);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace pm

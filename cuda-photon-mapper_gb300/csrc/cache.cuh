@@ -1,0 +1,96 @@
+// cache.cuh -- learned radiance cache: a multiresolution hash-grid encoding
+// and a 4 x 64 ReLU MLP (bf16 operands on the tcgen05 tensor cores, fp32
+// accumulation in TMEM), trained online on the photon map's own k-NN
+// radiance estimates and queried in their place when rendering.
+//
+// A frame is rendered as a query list (eye_path.cuh): every volume march
+// sample and every diffuse hit of every pixel becomes one query record
+//   qa = (x, y, z, object id bits; kNone for a volume query)
+//   qd = (wo.x, wo.y, wo.z, w)     wo toward the viewer, w = transmittance (* dt)
+// whose value -- the k-NN estimate or the network's prediction of it -- is
+// summed per pixel in query order: L = sum w * albedo(obj) * value.
+#pragma once
+#include <cuda_fp16.h>
+#include <cstdint>
+
+#include "gather.cuh"
+#include "phys_common.cuh"
+
+namespace pm {
+
+constexpr int kCacheIn = 64;        // 32 hash-grid + 16 SH(wo) + normal 3 + kind + bias + zero padding
+constexpr int kCacheHidden = 64;
+constexpr int kCacheLayers = 4;     // hidden layers
+constexpr int kCacheOut = 16;       // output columns, rgb in the first three
+constexpr int kCacheMaxLevels = 16;
+constexpr int kCacheTile = 128;     // samples per tensor-core tile (one per TMEM lane)
+// fp32 MLP parameters, each layer [in][out] row-major: four 64 x 64 hidden
+// layers, then 64 x 16.
+constexpr int kCacheWeights = kCacheLayers * kCacheIn * kCacheHidden + kCacheHidden * kCacheOut;
+
+struct CacheGrid {
+    int levels;              // <= kCacheMaxLevels
+    uint32_t log2_t;         // entries per level = 2^log2_t
+    int res[kCacheMaxLevels];
+    float lo[3], inv_size[3];  // world box -> [0,1]^3
+};
+
+struct CacheParams {
+    float *w;              // fp32 master weights (kCacheWeights)
+    float *w_grad, *w_m, *w_v;
+    float *table;          // fp32 master table, levels * 2^log2_t * 2
+    float2 *table_grad;
+    float *table_m, *table_v;
+    __half2 *table_h;      // fp16 copy read by the forward passes
+    float *loss;           // device scalar, summed over a step
+    int *status;           // set when a bounded tensor-core wait runs out
+};
+
+// Per-pixel query counts and diffuse-query counts (0 or 1) (count pass);
+// records plus the list of diffuse-query indices (write pass, after
+// exclusive scans of the counts into off and soff).
+cudaError_t cache_count_queries(const PScene &S, const RenderParams &R, bool vol_on, bool surf_on,
+                                uint32_t *cnt, uint32_t *scnt, cudaStream_t s);
+cudaError_t cache_write_queries(const PScene &S, const RenderParams &R, bool vol_on, bool surf_on,
+                                const uint32_t *off, const uint32_t *soff, float4 *qa, float4 *qd,
+                                uint32_t *slist, cudaStream_t s);
+// rad / rgba of every pixel from the ordered sum of its queries' values.
+cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *qa,
+                            const float4 *qd, const float4 *val, uint32_t npix, float exposure,
+                            float4 *rad, uchar4 *rgba, cudaStream_t s);
+// k-NN estimate of query sel[i] (or i when sel is null) into val[i]:
+// diffuse queries e / (pi r^2) / pi from the surface map, volume queries
+// e / (4/3 pi r^3) with the phase function toward wo from the volume map.
+cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView &vol,
+                             const float4 *qa, const float4 *qd, const uint32_t *sel, uint32_t n,
+                             int k, float radius, float4 *val, cudaStream_t s);
+// Training picks from Philox(seed, frame, i): with probability surf_frac
+// uniform over the diffuse queries slist[0..ns_total), else uniform over
+// all `total` queries.
+cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
+                         uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel,
+                         cudaStream_t s);
+// *sum += mean over rgb of val[0..n).
+cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s);
+
+cudaError_t cache_init(const CacheGrid &g, const CacheParams &p, uint64_t seed, cudaStream_t s);
+// Refreshes the fp16 table from the fp32 master copy.
+cudaError_t cache_sync_half(const CacheGrid &g, const CacheParams &p, cudaStream_t s);
+// Forward + backward of the relative L2 loss (denominator y^2 + rel_eps)
+// over n samples (query sel[i], target val[i] * inv_scale); gradients and loss are added to p.w_grad,
+// p.table_grad, p.loss with the factor loss_norm (1 / (3 * batch)). x_out
+// (n x 64 encoded features) and y_out (n x 4 outputs) are debug copies,
+// nullable.
+cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScene &S,
+                           const float4 *qa, const float4 *qd, const uint32_t *sel,
+                           const float4 *val, uint32_t n, float inv_scale, float loss_norm,
+                           float rel_eps, float *x_out, float *y_out, int sm_count, cudaStream_t s);
+// One Adam step over all parameters; gradients are zeroed after use.
+cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float beta1,
+                       float beta2, float eps, int step, cudaStream_t s);
+// val[i] = max(network(query i), 0) * out_scale for the first n queries.
+cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &S,
+                        const float4 *qa, const float4 *qd, uint32_t n, float out_scale,
+                        float4 *val, int sm_count, cudaStream_t s);
+
+}  // namespace pm

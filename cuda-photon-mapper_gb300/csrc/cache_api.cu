@@ -1,0 +1,571 @@
+// cache_api.cu -- the learned radiance cache behind the pm_cache_* C ABI:
+// configuration, the per-camera query list, online training frames, cached
+// and k-NN renders through the query list, parameter access and files.
+#include "cache.cuh"
+#include "phys_state.cuh"
+#include "pm_ctx.cuh"
+#include "radix_sort.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+struct CacheState {
+    pm_cache_config cfg;
+    pm::CacheGrid grid;
+    pm::CacheParams p;
+    size_t table_floats = 0;
+    int sm_count = 148;
+    // query list of the current camera
+    uint32_t npix_cap = 0;
+    uint32_t *cnt = nullptr, *off = nullptr, *scan_tmp = nullptr;
+    uint32_t *scnt = nullptr, *soff = nullptr, *slist = nullptr;  // diffuse queries
+    float4 *qa = nullptr, *qd = nullptr, *val = nullptr;
+    uint32_t qcap = 0, nq = 0, nsurf = 0;
+    uint64_t qgen = 0;
+    int qflags = -1;  // bit 0: volume queries, bit 1: diffuse queries
+    // training
+    uint32_t *sel = nullptr;
+    float4 *tgt = nullptr;
+    float *scale_sum = nullptr;
+    float target_scale = 0.0f;  // 0: set from the first training frame
+    unsigned long long steps = 0, frames = 0;
+    cudaEvent_t ev[7] = {};  // queries start/end, values start, values end/composite start, composite end, train mid/end
+    cudaEvent_t tev0 = nullptr;
+    bool rendered = false, trained = false;
+    pm_cache_stats stats;
+};
+
+namespace pm {
+namespace {
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+void free_cache(CacheState *c) {
+    if (!c) return;
+    cudaFree(c->p.w); cudaFree(c->p.w_grad); cudaFree(c->p.w_m); cudaFree(c->p.w_v);
+    cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
+    cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status);
+    cudaFree(c->cnt); cudaFree(c->off); cudaFree(c->scan_tmp);
+    cudaFree(c->scnt); cudaFree(c->soff); cudaFree(c->slist);
+    cudaFree(c->qa); cudaFree(c->qd); cudaFree(c->val);
+    cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->tev0) cudaEventDestroy(c->tev0);
+    delete c;
+}
+
+// World box of the scene (walls included) -> [0,1]^3, with a 1 % margin.
+void set_grid_box(CacheGrid &g, const pm_scene &sc) {
+    for (int a = 0; a < 3; ++a) {
+        const float ext = sc.box_max[a] - sc.box_min[a];
+        const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
+        g.lo[a] = sc.box_min[a] - m;
+        const float size = ext + 2.0f * m;
+        g.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
+    }
+}
+
+// Builds the query list of the installed camera unless it is current.
+pm_status ensure_queries(pm_ctx *ctx, PhysicalState *st, CacheState *c, cudaStream_t stream) {
+    const MapView surf = view_of(st->map[0]), vol = view_of(st->map[1]);
+    const int flags = (vol.n > 0 ? 1 : 0) | (surf.n > 0 ? 2 : 0);
+    if (c->qgen == st->gen && c->qflags == flags) return PM_OK;
+    cudaError_t e;
+#define PM_TRY(x) do { e = (x); if (e != cudaSuccess) return check_cuda(ctx, e, #x); } while (0)
+    const uint32_t npix = (uint32_t)st->cfg.width * (uint32_t)st->cfg.height;
+    if (npix > c->npix_cap) {
+        cudaFree(c->cnt); cudaFree(c->off); cudaFree(c->scan_tmp);
+        cudaFree(c->scnt); cudaFree(c->soff); cudaFree(c->slist);
+        c->cnt = c->off = c->scan_tmp = c->scnt = c->soff = c->slist = nullptr;
+        c->npix_cap = 0;
+        PM_TRY(dalloc(&c->cnt, npix));
+        PM_TRY(dalloc(&c->off, (size_t)npix + 1));
+        PM_TRY(dalloc(&c->scnt, npix));
+        PM_TRY(dalloc(&c->soff, (size_t)npix + 1));
+        PM_TRY(dalloc(&c->slist, npix));
+        PM_TRY(dalloc(&c->scan_tmp, scan_tile_count(npix) + 1));
+        c->npix_cap = npix;
+    }
+    const RenderParams R = render_params(st);
+    PM_TRY(cudaEventRecord(c->ev[0], stream));
+    PM_TRY(cache_count_queries(st->dscene, R, flags & 1, flags & 2, c->cnt, c->scnt, stream));
+    PM_TRY(exclusive_scan_u32_large(c->cnt, c->off, npix, c->off + npix, c->scan_tmp, stream));
+    PM_TRY(exclusive_scan_u32_large(c->scnt, c->soff, npix, c->soff + npix, c->scan_tmp, stream));
+    uint32_t totals[2] = {0, 0};
+    PM_TRY(cudaMemcpyAsync(&totals[0], c->off + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    PM_TRY(cudaMemcpyAsync(&totals[1], c->soff + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    PM_TRY(cudaStreamSynchronize(stream));
+    const uint32_t total = totals[0];
+    if (total > c->qcap) {
+        cudaFree(c->qa); cudaFree(c->qd); cudaFree(c->val);
+        c->qa = c->qd = c->val = nullptr;
+        c->qcap = 0;
+        const uint32_t cap = total + total / 8;
+        PM_TRY(dalloc(&c->qa, cap));
+        PM_TRY(dalloc(&c->qd, cap));
+        PM_TRY(dalloc(&c->val, cap));
+        c->qcap = cap;
+    }
+    PM_TRY(cache_write_queries(st->dscene, R, flags & 1, flags & 2, c->off, c->soff, c->qa, c->qd,
+                               c->slist, stream));
+    PM_TRY(cudaEventRecord(c->ev[1], stream));
+    PM_TRY(cudaEventSynchronize(c->ev[1]));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    c->stats.ms_queries = ms;
+    c->nq = total;
+    c->nsurf = totals[1];
+    c->qgen = st->gen;
+    c->qflags = flags;
+    set_grid_box(c->grid, st->scene);
+    return PM_OK;
+}
+
+pm_status need_cache(pm_ctx *ctx, bool need_maps) {
+    if (!ctx->cache) return fail(ctx, PM_ERR_STATE, "radiance cache not enabled");
+    if (need_maps) {
+        PhysicalState *st = ctx->phys;
+        if (!st || !st->map[0].built || !st->map[1].built)
+            return fail(ctx, PM_ERR_STATE, "photon maps not built");
+    }
+    return PM_OK;
+}
+
+}  // namespace
+
+void cache_free(pm_ctx *ctx) {
+    free_cache(ctx->cache);
+    ctx->cache = nullptr;
+}
+
+}  // namespace pm
+
+using namespace pm;
+
+extern "C" {
+
+void pm_cache_default_config(pm_cache_config *cfg) {
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->levels = 16;
+    cfg->log2_table = 19;
+    cfg->base_res = 16;
+    cfg->max_res = 2048;
+    cfg->train_samples = 1u << 20;
+    cfg->batch = 1u << 14;
+    cfg->lr = 1e-2f;
+    cfg->beta1 = 0.9f;
+    cfg->beta2 = 0.99f;
+    cfg->eps = 1e-15f;
+    cfg->lr_min = 1e-3f;
+    cfg->lr_half_life = 1000.0f;
+    cfg->loss_eps = 1.0f;
+    cfg->surface_fraction = 0.5f;
+    cfg->seed = 0x5EED0004ull;
+}
+
+pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_cache_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else pm_cache_default_config(&cfg);
+    if (cfg.levels < 1 || cfg.levels > kCacheMaxLevels || cfg.log2_table < 8 || cfg.log2_table > 22 ||
+        cfg.base_res < 2 || cfg.max_res < cfg.base_res || cfg.max_res > 65536 ||
+        cfg.train_samples < 1 || cfg.train_samples > (1u << 24) || cfg.batch < 128 ||
+        cfg.batch % 128 != 0 || !(cfg.lr > 0.0f) || !(cfg.beta1 >= 0.0f && cfg.beta1 < 1.0f) ||
+        !(cfg.beta2 >= 0.0f && cfg.beta2 < 1.0f) || !(cfg.eps >= 0.0f) ||
+        !(cfg.lr_min >= 0.0f) || !(cfg.lr_half_life >= 0.0f) || !(cfg.loss_eps > 0.0f) ||
+        !(cfg.surface_fraction >= 0.0f && cfg.surface_fraction <= 1.0f))
+        return fail(ctx, PM_ERR_INVALID, "invalid radiance-cache configuration");
+    DeviceGuard g(ctx->device);
+    cache_free(ctx);
+    CacheState *c = new CacheState();
+    ctx->cache = c;
+    c->cfg = cfg;
+    memset(&c->stats, 0, sizeof(c->stats));
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+    CacheGrid &gr = c->grid;
+    memset(&gr, 0, sizeof(gr));
+    gr.levels = cfg.levels;
+    gr.log2_t = (uint32_t)cfg.log2_table;
+    const double b = cfg.levels > 1 ? std::exp(std::log((double)cfg.max_res / cfg.base_res) / (cfg.levels - 1)) : 1.0;
+    for (int l = 0; l < cfg.levels; ++l) gr.res[l] = (int)std::floor(cfg.base_res * std::pow(b, l) + 1e-6);
+    for (int a = 0; a < 3; ++a) { gr.lo[a] = 0.0f; gr.inv_size[a] = 1.0f; }
+    if (ctx->phys) set_grid_box(gr, ctx->phys->scene);
+    c->table_floats = (size_t)cfg.levels << (cfg.log2_table + 1);
+    cudaError_t e;
+#define PM_TRY_FREE(x) do { e = (x); if (e != cudaSuccess) { cache_free(ctx); return check_cuda(ctx, e, #x); } } while (0)
+    CacheParams &p = c->p;
+    PM_TRY_FREE(dalloc(&p.w, kCacheWeights));
+    PM_TRY_FREE(dalloc(&p.w_grad, kCacheWeights));
+    PM_TRY_FREE(dalloc(&p.w_m, kCacheWeights));
+    PM_TRY_FREE(dalloc(&p.w_v, kCacheWeights));
+    PM_TRY_FREE(dalloc(&p.table, c->table_floats));
+    PM_TRY_FREE(dalloc(&p.table_grad, c->table_floats / 2));
+    PM_TRY_FREE(dalloc(&p.table_m, c->table_floats));
+    PM_TRY_FREE(dalloc(&p.table_v, c->table_floats));
+    PM_TRY_FREE(dalloc(&p.table_h, c->table_floats / 2));
+    PM_TRY_FREE(dalloc(&p.loss, 1));
+    PM_TRY_FREE(dalloc(&p.status, 1));
+    PM_TRY_FREE(cudaMemset(p.status, 0, sizeof(int)));
+    PM_TRY_FREE(dalloc(&c->sel, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->tgt, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->scale_sum, 1));
+    for (auto &ev : c->ev) PM_TRY_FREE(cudaEventCreate(&ev));
+    PM_TRY_FREE(cudaEventCreate(&c->tev0));
+    PM_TRY_FREE(cache_init(gr, p, cfg.seed, 0));
+    PM_TRY_FREE(cudaDeviceSynchronize());
+#undef PM_TRY_FREE
+    return PM_OK;
+}
+
+pm_status pm_cache_disable(pm_ctx *ctx) {
+    if (!ctx) return PM_ERR_INVALID;
+    DeviceGuard g(ctx->device);
+    cudaDeviceSynchronize();
+    cache_free(ctx);
+    return PM_OK;
+}
+
+pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
+    if (!ctx || frames < 0) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, true);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    PhysicalState *st = ctx->phys;
+    CacheState *c = ctx->cache;
+    s = ensure_queries(ctx, st, c, stream);
+    if (s != PM_OK) return s;
+    if (c->nq == 0 || frames == 0) return PM_OK;
+    cudaError_t e;
+    const uint32_t ns = c->cfg.train_samples, batch = c->cfg.batch;
+    const uint32_t nb = (ns + batch - 1) / batch;
+    const MapView surf = view_of(st->map[0]), vol = view_of(st->map[1]);
+    for (int f = 0; f < frames; ++f) {
+        PM_TRY(cudaEventRecord(c->tev0, stream));
+        PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, c->nq, c->slist, c->nsurf, ns,
+                            c->cfg.surface_fraction, c->sel, stream));
+        PM_TRY(cache_knn_values(st->dscene, surf, vol, c->qa, c->qd, c->sel, ns, st->cfg.k,
+                                st->cfg.radius, c->tgt, stream));
+        PM_TRY(cudaEventRecord(c->ev[5], stream));
+        if (!(c->target_scale > 0.0f)) {
+            float sum = 0.0f;
+            PM_TRY(cudaMemsetAsync(c->scale_sum, 0, sizeof(float), stream));
+            PM_TRY(cache_value_sum(c->tgt, ns, c->scale_sum, stream));
+            PM_TRY(cudaMemcpyAsync(&sum, c->scale_sum, sizeof(float), cudaMemcpyDeviceToHost, stream));
+            PM_TRY(cudaStreamSynchronize(stream));
+            const float mean = sum / (float)ns;
+            c->target_scale = mean > 0.0f && std::isfinite(mean) ? mean : 1.0f;
+        }
+        PM_TRY(cudaMemsetAsync(c->p.loss, 0, sizeof(float), stream));
+        for (uint32_t b = 0; b < nb; ++b) {
+            const uint32_t o = b * batch, n = std::min(batch, ns - o);
+            PM_TRY(cache_backward(c->grid, c->p, st->dscene, c->qa, c->qd, c->sel + o, c->tgt + o, n,
+                                  1.0f / c->target_scale, 1.0f / (3.0f * (float)n), c->cfg.loss_eps,
+                                  nullptr, nullptr, c->sm_count, stream));
+            float lr = c->cfg.lr;
+            if (c->cfg.lr_half_life > 0.0f)
+                lr = c->cfg.lr_min + (c->cfg.lr - c->cfg.lr_min) *
+                                         (float)std::exp2(-(double)c->steps / c->cfg.lr_half_life);
+            ++c->steps;
+            PM_TRY(cache_adam(c->grid, c->p, lr, c->cfg.beta1, c->cfg.beta2, c->cfg.eps,
+                              (int)std::min<unsigned long long>(c->steps, 1u << 30), stream));
+        }
+        PM_TRY(cudaEventRecord(c->ev[6], stream));
+        ++c->frames;
+    }
+    float loss = 0.0f;
+    PM_TRY(cudaMemcpyAsync(&loss, c->p.loss, sizeof(float), cudaMemcpyDeviceToHost, stream));
+    PM_TRY(cudaStreamSynchronize(stream));
+    c->stats.loss = loss / (float)nb;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->tev0, c->ev[5]);
+    c->stats.ms_targets = ms;
+    cudaEventElapsedTime(&ms, c->ev[5], c->ev[6]);
+    c->stats.ms_train = ms;
+    c->trained = true;
+    return PM_OK;
+}
+
+pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int source,
+                           cudaStream_t stream) {
+    if (!ctx || source < 0 || source > 1) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, true);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    PhysicalState *st = ctx->phys;
+    CacheState *c = ctx->cache;
+    s = ensure_queries(ctx, st, c, stream);
+    if (s != PM_OK) return s;
+    cudaError_t e;
+    const uint32_t npix = (uint32_t)st->cfg.width * (uint32_t)st->cfg.height;
+    PM_TRY(cudaEventRecord(c->ev[2], stream));
+    if (source == 0) {
+        const float scale = c->target_scale > 0.0f ? c->target_scale : 1.0f;
+        PM_TRY(cache_infer(c->grid, c->p, st->dscene, c->qa, c->qd, c->nq, scale, c->val, c->sm_count,
+                           stream));
+    } else {
+        PM_TRY(cache_knn_values(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->qa, c->qd,
+                                nullptr, c->nq, st->cfg.k, st->cfg.radius, c->val, stream));
+    }
+    PM_TRY(cudaEventRecord(c->ev[3], stream));
+    PM_TRY(cache_composite(st->dscene, c->off, c->qa, c->qd, c->val, npix, st->cfg.exposure,
+                           radiance, rgba, stream));
+    PM_TRY(cudaEventRecord(c->ev[4], stream));
+    c->stats.queries = c->nq;
+    c->rendered = true;
+    return PM_OK;
+}
+
+pm_status pm_cache_get_stats(pm_ctx *ctx, pm_cache_stats *out) {
+    if (!ctx || !out) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    cudaError_t e;
+    if (c->rendered) {
+        PM_TRY(cudaEventSynchronize(c->ev[4]));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        c->stats.ms_values = ms;
+        cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
+        c->stats.ms_composite = ms;
+    }
+    int status = 0;
+    PM_TRY(cudaMemcpy(&status, c->p.status, sizeof(int), cudaMemcpyDeviceToHost));
+    c->stats.tc_status = status;
+    c->stats.train_steps = c->steps;
+    c->stats.train_frames = c->frames;
+    c->stats.target_scale = c->target_scale;
+    *out = c->stats;
+    return PM_OK;
+}
+
+pm_status pm_cache_get_params(pm_ctx *ctx, float *weights, float *table, int *res) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    if (weights) PM_TRY(cudaMemcpy(weights, c->p.w, sizeof(float) * kCacheWeights, cudaMemcpyDeviceToHost));
+    if (table) PM_TRY(cudaMemcpy(table, c->p.table, sizeof(float) * c->table_floats, cudaMemcpyDeviceToHost));
+    if (res)
+        for (int l = 0; l < c->grid.levels; ++l) res[l] = c->grid.res[l];
+    return PM_OK;
+}
+
+pm_status pm_cache_set_params(pm_ctx *ctx, const float *weights, const float *table) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    if (weights) {
+        PM_TRY(cudaMemcpy(c->p.w, weights, sizeof(float) * kCacheWeights, cudaMemcpyHostToDevice));
+        PM_TRY(cudaMemset(c->p.w_m, 0, sizeof(float) * kCacheWeights));
+        PM_TRY(cudaMemset(c->p.w_v, 0, sizeof(float) * kCacheWeights));
+    }
+    if (table) {
+        PM_TRY(cudaMemcpy(c->p.table, table, sizeof(float) * c->table_floats, cudaMemcpyHostToDevice));
+        PM_TRY(cudaMemset(c->p.table_m, 0, sizeof(float) * c->table_floats));
+        PM_TRY(cudaMemset(c->p.table_v, 0, sizeof(float) * c->table_floats));
+        PM_TRY(cache_sync_half(c->grid, c->p, 0));
+    }
+    PM_TRY(cudaDeviceSynchronize());
+    return PM_OK;
+}
+
+pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, const float4 *target,
+                              uint32_t n, float target_scale, float *x, float *y, float *loss,
+                              float *w_grad, float *table_grad) {
+    if (!ctx || (n && (!qa || !qd || !target)) || !(target_scale > 0.0f)) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    if (!ctx->phys) return fail(ctx, PM_ERR_STATE, "pm_cache_debug_step before pm_set_scene");
+    if (n > (1u << 20)) return fail(ctx, PM_ERR_LIMIT, "debug step above 2^20 samples");
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    PhysicalState *st = ctx->phys;
+    set_grid_box(c->grid, st->scene);
+    cudaError_t e;
+    float4 *dqa = nullptr, *dqd = nullptr, *dt = nullptr;
+    float *dx = nullptr, *dy = nullptr;
+    std::string where;
+#define PM_DBG(x) do { e = (x); if (e != cudaSuccess) { where = #x; goto done; } } while (0)
+    PM_DBG(cudaDeviceSynchronize());
+    PM_DBG(dalloc(&dqa, n));
+    PM_DBG(dalloc(&dqd, n));
+    PM_DBG(dalloc(&dt, n));
+    PM_DBG(dalloc(&dx, (size_t)n * 64));
+    PM_DBG(dalloc(&dy, (size_t)n * 4));
+    if (n) {
+        PM_DBG(cudaMemcpy(dqa, qa, sizeof(float4) * n, cudaMemcpyHostToDevice));
+        PM_DBG(cudaMemcpy(dqd, qd, sizeof(float4) * n, cudaMemcpyHostToDevice));
+        PM_DBG(cudaMemcpy(dt, target, sizeof(float4) * n, cudaMemcpyHostToDevice));
+    }
+    PM_DBG(cudaMemset(c->p.w_grad, 0, sizeof(float) * kCacheWeights));
+    PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(float) * c->table_floats));
+    PM_DBG(cudaMemset(c->p.loss, 0, sizeof(float)));
+    PM_DBG(cache_backward(c->grid, c->p, st->dscene, dqa, dqd, nullptr, dt, n, 1.0f / target_scale,
+                          n ? 1.0f / (3.0f * (float)n) : 0.0f, c->cfg.loss_eps, dx, dy, c->sm_count,
+                          0));
+    PM_DBG(cudaDeviceSynchronize());
+    if (x && n) PM_DBG(cudaMemcpy(x, dx, sizeof(float) * 64 * n, cudaMemcpyDeviceToHost));
+    if (y && n) PM_DBG(cudaMemcpy(y, dy, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost));
+    if (loss) PM_DBG(cudaMemcpy(loss, c->p.loss, sizeof(float), cudaMemcpyDeviceToHost));
+    if (w_grad) PM_DBG(cudaMemcpy(w_grad, c->p.w_grad, sizeof(float) * kCacheWeights, cudaMemcpyDeviceToHost));
+    if (table_grad)
+        PM_DBG(cudaMemcpy(table_grad, c->p.table_grad, sizeof(float) * c->table_floats, cudaMemcpyDeviceToHost));
+    PM_DBG(cudaMemset(c->p.w_grad, 0, sizeof(float) * kCacheWeights));
+    PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(float) * c->table_floats));
+done:
+#undef PM_DBG
+    cudaFree(dqa); cudaFree(dqd); cudaFree(dt); cudaFree(dx); cudaFree(dy);
+    if (e != cudaSuccess) return check_cuda(ctx, e, where.c_str());
+    return PM_OK;
+}
+
+pm_status pm_cache_get_queries(pm_ctx *ctx, float4 *qa, float4 *qd, uint32_t cap, uint32_t *count) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, true);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    s = ensure_queries(ctx, ctx->phys, c, 0);
+    if (s != PM_OK) return s;
+    if (count) *count = c->nq;
+    const uint32_t n = std::min(cap, c->nq);
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    if (n && qa) PM_TRY(cudaMemcpy(qa, c->qa, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    if (n && qd) PM_TRY(cudaMemcpy(qd, c->qd, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    return PM_OK;
+}
+
+pm_status pm_cache_get_values(pm_ctx *ctx, float4 *val, uint32_t cap, uint32_t *count) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    CacheState *c = ctx->cache;
+    if (!c->rendered) return fail(ctx, PM_ERR_STATE, "pm_cache_get_values before pm_render_cached");
+    DeviceGuard g(ctx->device);
+    if (count) *count = c->nq;
+    const uint32_t n = std::min(cap, c->nq);
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    if (n && val) PM_TRY(cudaMemcpy(val, c->val, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    return PM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+const char kCacheMagic[] = "{\"format\": \"pm-radiance-cache\", \"version\": 1";
+
+}  // namespace
+
+extern "C" {
+
+// File = one JSON header line, then fp32 arrays: weights, their two Adam
+// moments, the table, its two Adam moments.
+pm_status pm_cache_save(pm_ctx *ctx, const char *path) {
+    if (!ctx || !path) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    const size_t nw = kCacheWeights, nt = c->table_floats;
+    std::vector<float> buf(3 * nw + 3 * nt);
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    const float *src[6] = {c->p.w, c->p.w_m, c->p.w_v, c->p.table, c->p.table_m, c->p.table_v};
+    size_t at = 0;
+    for (int i = 0; i < 6; ++i) {
+        const size_t len = i < 3 ? nw : nt;
+        PM_TRY(cudaMemcpy(buf.data() + at, src[i], sizeof(float) * len, cudaMemcpyDeviceToHost));
+        at += len;
+    }
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(ctx, PM_ERR_INVALID, std::string("cannot open ") + path);
+    fprintf(f,
+            "%s, \"levels\": %d, \"log2_table\": %d, \"base_res\": %d, \"max_res\": %d, "
+            "\"target_scale\": %.9g, \"steps\": %llu, \"frames\": %llu, \"weights\": %zu, "
+            "\"table_floats\": %zu, \"layout\": \"fp32 weights, m, v; table, m, v\"}\n",
+            kCacheMagic, c->cfg.levels, c->cfg.log2_table, c->cfg.base_res, c->cfg.max_res,
+            c->target_scale, c->steps, c->frames, nw, nt);
+    bool ok = fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    ok = (fclose(f) == 0) && ok;
+    return ok ? PM_OK : fail(ctx, PM_ERR_INVALID, "short write");
+}
+
+pm_status pm_cache_load(pm_ctx *ctx, const char *path) {
+    if (!ctx || !path) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    CacheState *c = ctx->cache;
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(ctx, PM_ERR_INVALID, std::string("cannot open ") + path);
+    char line[1024];
+    if (!fgets(line, sizeof(line), f) || strncmp(line, kCacheMagic, strlen(kCacheMagic)) != 0) {
+        fclose(f);
+        return fail(ctx, PM_ERR_INVALID, "not a radiance-cache file");
+    }
+    int levels = -1, log2t = -1, base = -1, maxr = -1;
+    float scale = 0.0f;
+    unsigned long long steps = 0, frames = 0;
+    const char *q;
+    if ((q = strstr(line, "\"levels\": "))) sscanf(q + 10, "%d", &levels);
+    if ((q = strstr(line, "\"log2_table\": "))) sscanf(q + 14, "%d", &log2t);
+    if ((q = strstr(line, "\"base_res\": "))) sscanf(q + 12, "%d", &base);
+    if ((q = strstr(line, "\"max_res\": "))) sscanf(q + 11, "%d", &maxr);
+    if ((q = strstr(line, "\"target_scale\": "))) sscanf(q + 16, "%f", &scale);
+    if ((q = strstr(line, "\"steps\": "))) sscanf(q + 9, "%llu", &steps);
+    if ((q = strstr(line, "\"frames\": "))) sscanf(q + 10, "%llu", &frames);
+    if (levels != c->cfg.levels || log2t != c->cfg.log2_table || base != c->cfg.base_res ||
+        maxr != c->cfg.max_res) {
+        fclose(f);
+        return fail(ctx, PM_ERR_INVALID, "radiance-cache file has another grid configuration");
+    }
+    const size_t nw = kCacheWeights, nt = c->table_floats;
+    std::vector<float> buf(3 * nw + 3 * nt);
+    const bool ok = fread(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    fclose(f);
+    if (!ok) return fail(ctx, PM_ERR_INVALID, "truncated radiance-cache file");
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    float *dst[6] = {c->p.w, c->p.w_m, c->p.w_v, c->p.table, c->p.table_m, c->p.table_v};
+    size_t at = 0;
+    for (int i = 0; i < 6; ++i) {
+        const size_t len = i < 3 ? nw : nt;
+        PM_TRY(cudaMemcpy(dst[i], buf.data() + at, sizeof(float) * len, cudaMemcpyHostToDevice));
+        at += len;
+    }
+    PM_TRY(cudaMemset(c->p.w_grad, 0, sizeof(float) * nw));
+    PM_TRY(cudaMemset(c->p.table_grad, 0, sizeof(float) * nt));
+    PM_TRY(cache_sync_half(c->grid, c->p, 0));
+    PM_TRY(cudaDeviceSynchronize());
+    c->target_scale = scale;
+    c->steps = steps;
+    c->frames = frames;
+    return PM_OK;
+}
+
+#undef PM_TRY
+}  // extern "C"

@@ -3,43 +3,16 @@
 #include "gather.cuh"
 #include "kdtree.cuh"
 #include "launch_count.cuh"
+#include "phys_state.cuh"
 #include "pm_ctx.cuh"
 #include "radix_sort.cuh"
 #include "scene.cuh"
 #include "trace.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
-
-struct PhysicalState {
-    pm_scene scene;
-    pm_config cfg;
-    pm::PScene dscene;
-    float *het = nullptr;
-    uint32_t path_cap = 0;
-    int mb = 0;
-    uint32_t *cnt[2] = {nullptr, nullptr};  // records per path, per map
-    uint32_t *off[2] = {nullptr, nullptr};  // exclusive scans of cnt
-    uint32_t *scan_tmp = nullptr;
-    uint32_t *words = nullptr;  // [0] path counter [1] stored_s [2] stored_v [3] total [4..7] extents
-    struct Map {
-        float4 *pos = nullptr, *pow = nullptr, *tpos = nullptr, *tpow = nullptr;
-        float4 *lo = nullptr, *hi = nullptr;
-        uint32_t cap = 0, n = 0, paths = 0;
-        int depth = 0;
-        bool built = false;
-    } map[2];
-    uint64_t *keys = nullptr, *keys_tmp = nullptr;
-    uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
-    uint32_t sort_cap = 0;
-    unsigned long long *gctr = nullptr;
-    cudaEvent_t ev[6] = {};  // emit, build, render: start/stop
-    pm_frame_stats stats;
-    bool emitted = false;
-    bool rendered = false;
-    int sm_count = 148;
-};
 
 namespace pm {
 
@@ -71,18 +44,13 @@ void free_state(PhysicalState *st) {
     delete st;
 }
 
-MapView view_of(const PhysicalState::Map &m) {
-    MapView v;
-    v.pos = m.tpos;
-    v.pow = m.tpow;
-    v.lo = m.lo;
-    v.hi = m.hi;
-    v.n = m.built ? m.n : 0;
-    v.depth = m.depth;
-    return v;
-}
 
 }  // namespace
+
+uint64_t next_scene_gen() {
+    static std::atomic<uint64_t> gen{0};
+    return ++gen;
+}
 
 void physical_free(pm_ctx *ctx) {
     free_state(ctx->phys);
@@ -150,6 +118,7 @@ pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg)
     PM_TRY(cudaDeviceSynchronize());
 #undef PM_TRY
     st->dscene = to_device_scene(*scene, st->het);
+    st->gen = next_scene_gen();
     return PM_OK;
 }
 
@@ -172,6 +141,7 @@ pm_status pm_update_scene(pm_ctx *ctx, const pm_scene *scene) {
         if (e != cudaSuccess) return check_cuda(ctx, e, "make_noise_grid");
     }
     st->dscene = to_device_scene(*scene, st->het);
+    st->gen = next_scene_gen();
     return PM_OK;
 }
 
@@ -285,16 +255,7 @@ pm_status pm_render(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStream_t st
         return fail(ctx, PM_ERR_STATE, "pm_render before pm_build");
     DeviceGuard g(ctx->device);
     cudaError_t e;
-    RenderParams R;
-    R.width = st->cfg.width;
-    R.height = st->cfg.height;
-    R.aspect = st->cfg.height > 0 ? (float)st->cfg.width / (float)st->cfg.height : 1.0f;
-    R.k = st->cfg.k;
-    R.r2cap = st->cfg.radius * st->cfg.radius;
-    R.step = st->cfg.march_step;
-    R.exposure = st->cfg.exposure;
-    R.seed = st->cfg.seed;
-    R.scene_id = st->cfg.scene_id;
+    RenderParams R = render_params(st);
     R.counters = st->gctr;
     PM_TRY(cudaMemsetAsync(st->gctr, 0, 2 * sizeof(unsigned long long), stream));
     PM_TRY(cudaEventRecord(st->ev[4], stream));
@@ -436,6 +397,8 @@ size_t pm_abi_struct_size(int which) {
         case 1: return sizeof(pm_config);
         case 2: return sizeof(pm_photon_record);
         case 3: return sizeof(pm_frame_stats);
+        case 4: return sizeof(pm_cache_config);
+        case 5: return sizeof(pm_cache_stats);
     }
     return 0;
 }

@@ -78,6 +78,7 @@ void pm_destroy(pm_ctx *ctx) {
         DeviceGuard g(ctx->device);
         if (ctx->legacy_ready) legacy_free(ctx->legacy);
         physical_free(ctx);
+        cache_free(ctx);
     }
     delete ctx;
 }

@@ -12,6 +12,7 @@ struct pm_ctx {
     pm::LegacyState legacy;
     bool legacy_ready = false;
     struct PhysicalState *phys = nullptr;
+    struct CacheState *cache = nullptr;
 };
 
 namespace pm {
@@ -29,5 +30,6 @@ class DeviceGuard {
 pm_status fail(pm_ctx *ctx, pm_status s, const std::string &msg);
 pm_status check_cuda(pm_ctx *ctx, cudaError_t e, const char *where);
 void physical_free(pm_ctx *ctx);
+void cache_free(pm_ctx *ctx);
 
 }  // namespace pm

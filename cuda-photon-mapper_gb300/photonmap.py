@@ -76,6 +76,23 @@ class ViewerState(_c.Structure):
                 ("anim_inc", _c.c_float), ("frames", _c.c_ulonglong)]
 
 
+class CacheConfig(_c.Structure):
+    _fields_ = [("levels", _c.c_int), ("log2_table", _c.c_int), ("base_res", _c.c_int),
+                ("max_res", _c.c_int), ("train_samples", _c.c_uint32), ("batch", _c.c_uint32),
+                ("lr", _c.c_float), ("beta1", _c.c_float), ("beta2", _c.c_float),
+                ("eps", _c.c_float), ("lr_min", _c.c_float), ("lr_half_life", _c.c_float),
+                ("loss_eps", _c.c_float), ("surface_fraction", _c.c_float), ("seed", _c.c_uint64)]
+
+
+class CacheStats(_c.Structure):
+    _fields_ = [("queries", _c.c_ulonglong), ("train_steps", _c.c_ulonglong),
+                ("train_frames", _c.c_ulonglong), ("loss", _c.c_float),
+                ("target_scale", _c.c_float), ("ms_queries", _c.c_float),
+                ("ms_values", _c.c_float), ("ms_composite", _c.c_float),
+                ("ms_targets", _c.c_float), ("ms_train", _c.c_float), ("tc_status", _c.c_int)]
+
+
+CACHE_WEIGHTS = 4 * 64 * 64 + 64 * 16
 MAP_SURFACE = 0
 MAP_VOLUME = 1
 MAT_DIFFUSE, MAT_MIRROR, MAT_DIELECTRIC = 0, 1, 2
@@ -129,6 +146,19 @@ PROTOTYPES = {
     "pm_viewer_key": (None, [_vp, _c.c_ubyte]),
     "pm_viewer_state_get": (_i, [_vp, _c.POINTER(ViewerState)]),
     "pm_viewer_display": (_i, [_vp, _vp]),
+    "pm_cache_default_config": (None, [_c.POINTER(CacheConfig)]),
+    "pm_cache_enable": (_i, [_vp, _c.POINTER(CacheConfig)]),
+    "pm_cache_disable": (_i, [_vp]),
+    "pm_cache_train": (_i, [_vp, _i, _vp]),
+    "pm_render_cached": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "pm_cache_get_stats": (_i, [_vp, _c.POINTER(CacheStats)]),
+    "pm_cache_get_params": (_i, [_vp, _vp, _vp, _vp]),
+    "pm_cache_set_params": (_i, [_vp, _vp, _vp]),
+    "pm_cache_debug_step": (_i, [_vp, _vp, _vp, _vp, _c.c_uint32, _f, _vp, _vp, _vp, _vp, _vp]),
+    "pm_cache_get_queries": (_i, [_vp, _vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
+    "pm_cache_get_values": (_i, [_vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
+    "pm_cache_save": (_i, [_vp, _c.c_char_p]),
+    "pm_cache_load": (_i, [_vp, _c.c_char_p]),
 }
 
 _lib = None
@@ -284,6 +314,90 @@ class Context:
         self._check(self.lib.pm_get_stats(self.h, _c.byref(st)), "pm_get_stats")
         return st
 
+    # ---- learned radiance cache (pm_cache_*) ----
+    def cache_enable(self, cfg=None, **overrides):
+        if cfg is None:
+            cfg = cache_default_config()
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        self._check(self.lib.pm_cache_enable(self.h, _c.byref(cfg)), "pm_cache_enable")
+        self.cache_cfg = cfg
+        return cfg
+
+    def cache_disable(self):
+        self._check(self.lib.pm_cache_disable(self.h), "pm_cache_disable")
+
+    def cache_train(self, frames=1, stream=0):
+        self._check(self.lib.pm_cache_train(self.h, frames, stream), "pm_cache_train")
+
+    def render_cached(self, radiance=None, rgba=None, source=0, stream=0):
+        self._check(self.lib.pm_render_cached(self.h, radiance, rgba, source, stream),
+                    "pm_render_cached")
+
+    def cache_stats(self):
+        st = CacheStats()
+        self._check(self.lib.pm_cache_get_stats(self.h, _c.byref(st)), "pm_cache_get_stats")
+        return st
+
+    def cache_params(self):
+        """(weights [PM_CACHE_WEIGHTS], table [levels, 2^log2, 2], res [levels])."""
+        cfg = self.cache_cfg
+        w = np.zeros(CACHE_WEIGHTS, np.float32)
+        t = np.zeros((cfg.levels, 1 << cfg.log2_table, 2), np.float32)
+        r = np.zeros(cfg.levels, np.int32)
+        self._check(self.lib.pm_cache_get_params(self.h, w.ctypes.data, t.ctypes.data, r.ctypes.data),
+                    "pm_cache_get_params")
+        return w, t, r
+
+    def cache_set_params(self, weights=None, table=None):
+        w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        t = None if table is None else np.ascontiguousarray(table, np.float32)
+        self._check(self.lib.pm_cache_set_params(self.h, None if w is None else w.ctypes.data,
+                                                 None if t is None else t.ctypes.data),
+                    "pm_cache_set_params")
+
+    def cache_debug_step(self, qa, qd, target, target_scale=1.0):
+        """Forward + backward on host queries: dict of x, y, loss, w_grad, table_grad."""
+        cfg = self.cache_cfg
+        qa = np.ascontiguousarray(qa, np.float32)
+        qd = np.ascontiguousarray(qd, np.float32)
+        tg = np.ascontiguousarray(target, np.float32)
+        n = len(qa)
+        x = np.zeros((n, 64), np.float32)
+        y = np.zeros((n, 4), np.float32)
+        loss = np.zeros(1, np.float32)
+        wg = np.zeros(CACHE_WEIGHTS, np.float32)
+        tgr = np.zeros((cfg.levels, 1 << cfg.log2_table, 2), np.float32)
+        self._check(self.lib.pm_cache_debug_step(self.h, qa.ctypes.data, qd.ctypes.data, tg.ctypes.data,
+                                                 n, target_scale, x.ctypes.data, y.ctypes.data,
+                                                 loss.ctypes.data, wg.ctypes.data, tgr.ctypes.data),
+                    "pm_cache_debug_step")
+        return {"x": x, "y": y, "loss": float(loss[0]), "w_grad": wg, "table_grad": tgr}
+
+    def cache_queries(self):
+        n = _c.c_uint32(0)
+        self._check(self.lib.pm_cache_get_queries(self.h, None, None, 0, _c.byref(n)),
+                    "pm_cache_get_queries")
+        qa = np.zeros((n.value, 4), np.float32)
+        qd = np.zeros((n.value, 4), np.float32)
+        self._check(self.lib.pm_cache_get_queries(self.h, qa.ctypes.data, qd.ctypes.data, n.value,
+                                                  _c.byref(n)), "pm_cache_get_queries")
+        return qa, qd
+
+    def cache_values(self):
+        n = _c.c_uint32(0)
+        self._check(self.lib.pm_cache_get_values(self.h, None, 0, _c.byref(n)), "pm_cache_get_values")
+        v = np.zeros((n.value, 4), np.float32)
+        self._check(self.lib.pm_cache_get_values(self.h, v.ctypes.data, n.value, _c.byref(n)),
+                    "pm_cache_get_values")
+        return v
+
+    def cache_save(self, path):
+        self._check(self.lib.pm_cache_save(self.h, path.encode()), "pm_cache_save")
+
+    def cache_load(self, path):
+        self._check(self.lib.pm_cache_load(self.h, path.encode()), "pm_cache_load")
+
 
 class Viewer:
     """Headless frame driver (pm_viewer_*): the reference's display()/keyboard()."""
@@ -318,6 +432,12 @@ class Viewer:
             self.close()
         except Exception:
             pass
+
+
+def cache_default_config():
+    cfg = CacheConfig()
+    load().pm_cache_default_config(_c.byref(cfg))
+    return cfg
 
 
 def write_ppm(path, rgba):

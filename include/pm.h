@@ -301,12 +301,92 @@ PM_API void pm_viewer_key(pm_viewer *v, unsigned char key);
 PM_API pm_status pm_viewer_state_get(const pm_viewer *v, pm_viewer_state *out);
 PM_API pm_status pm_viewer_display(pm_viewer *v, uchar4 *pos);
 
+/* ---- 6. learned radiance cache ------------------------------------------------
+ * No counterpart in the reference, whose render always gathers photons. A
+ * frame is split into radiance queries -- every volume march sample and the
+ * diffuse hit of each pixel's eye path, as pm_render visits them -- whose
+ * k-NN estimates a small network learns: a multiresolution hash-grid
+ * encoding of the position (fp16 table), spherical harmonics of the view
+ * direction, the facing normal, and a 4 x 64 ReLU MLP run in bf16 on the
+ * tensor cores with fp32 accumulation. pm_cache_train fits it online to
+ * k-NN estimates at random queries of the current frame; pm_render_cached
+ * sums the network's predictions per pixel (source 0) or, as its fallback
+ * and judge, the k-NN estimates of every query (source 1, equal to
+ * pm_render up to summation rounding). The cache lives in the context and
+ * survives pm_set_scene. */
+typedef struct pm_cache_config {
+    int levels;              /* hash-grid levels, 1..16 */
+    int log2_table;          /* entries per level = 2^log2_table, 8..22 */
+    int base_res, max_res;   /* coarsest and finest grid resolution */
+    uint32_t train_samples;  /* k-NN samples per training frame, <= 2^24 */
+    uint32_t batch;          /* samples per Adam step, a multiple of 128 */
+    float lr, beta1, beta2, eps;  /* Adam */
+    float lr_min;            /* learning rate decays toward lr_min ... */
+    float lr_half_life;      /* ... halving the gap every lr_half_life steps (0: constant) */
+    float loss_eps;          /* relative L2 denominator y^2 + loss_eps (targets have mean 1) */
+    float surface_fraction;  /* share of each frame's samples drawn from the diffuse queries */
+    uint64_t seed;
+} pm_cache_config;
+
+typedef struct pm_cache_stats {
+    unsigned long long queries;      /* queries of the last cached frame */
+    unsigned long long train_steps;  /* Adam steps so far */
+    unsigned long long train_frames;
+    float loss;                      /* mean loss of the last training frame */
+    float target_scale;              /* targets are divided by this before the loss */
+    float ms_queries;                /* last query-list build */
+    float ms_values;                 /* last per-query values (network or k-NN) */
+    float ms_composite;
+    float ms_targets, ms_train;      /* last training frame: k-NN targets, steps */
+    int tc_status;                   /* nonzero: a tensor-core wait ran out */
+} pm_cache_stats;
+
+#define PM_CACHE_WEIGHTS (4 * 64 * 64 + 64 * 16)
+PM_API void pm_cache_default_config(pm_cache_config *cfg);
+/* Allocates and initialises the cache (cfg NULL: defaults). Re-enabling
+ * resets the network. */
+PM_API pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg);
+PM_API pm_status pm_cache_disable(pm_ctx *ctx);
+/* `frames` training frames on the built photon maps and the current camera:
+ * each draws train_samples queries, estimates them with the k-NN gather and
+ * takes train_samples / batch Adam steps. */
+PM_API pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream);
+/* Renders through the query list: source 0 = network, 1 = k-NN estimates.
+ * radiance / rgba as pm_render (either nullable). */
+PM_API pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int source,
+                                  cudaStream_t stream);
+PM_API pm_status pm_cache_get_stats(pm_ctx *ctx, pm_cache_stats *out);
+/* Host copies of the fp32 weights (PM_CACHE_WEIGHTS: four [64 in][64 out]
+ * layers, then [64][16]), the fp32 table (levels * 2^log2_table * 2,
+ * nullable) and the grid resolutions (levels ints, nullable). */
+PM_API pm_status pm_cache_get_params(pm_ctx *ctx, float *weights, float *table, int *res);
+PM_API pm_status pm_cache_set_params(pm_ctx *ctx, const float *weights, const float *table);
+/* Forward and backward of the loss over n host queries (qa, qd as the query
+ * list stores them; target = k-NN values), without an update. Outputs, all
+ * host and nullable: x (n x 64 encoded features), y (n x 4), *loss, weight
+ * gradients (PM_CACHE_WEIGHTS), table gradients (table size). */
+PM_API pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd,
+                                     const float4 *target, uint32_t n, float target_scale,
+                                     float *x, float *y, float *loss, float *w_grad,
+                                     float *table_grad);
+/* Query list of the current camera (host copies, nullable; *count always). */
+PM_API pm_status pm_cache_get_queries(pm_ctx *ctx, float4 *qa, float4 *qd, uint32_t cap,
+                                      uint32_t *count);
+/* Per-query values of the last pm_render_cached (network or k-NN, before
+ * the transmittance and albedo factors), host copy. */
+PM_API pm_status pm_cache_get_values(pm_ctx *ctx, float4 *val, uint32_t cap, uint32_t *count);
+/* Network + table + Adam state to a file (JSON header line, then raw fp32
+ * arrays) and back; load requires the same levels and log2_table. */
+PM_API pm_status pm_cache_save(pm_ctx *ctx, const char *path);
+PM_API pm_status pm_cache_load(pm_ctx *ctx, const char *path);
+
 /* Kernels this library has launched since it was loaded (all contexts). */
 PM_API unsigned long long pm_kernel_launches(void);
 
 /* sizeof of the ABI structs as this library was compiled (0 = pm_scene,
- * 1 = pm_config, 2 = pm_photon_record, 3 = pm_frame_stats), for bindings
- * in other languages to check their struct layouts against. */
+ * 1 = pm_config, 2 = pm_photon_record, 3 = pm_frame_stats,
+ * 4 = pm_cache_config, 5 = pm_cache_stats), for bindings in other
+ * languages to check their struct layouts against. */
 PM_API size_t pm_abi_struct_size(int which);
 
 #ifdef __cplusplus

@@ -70,3 +70,17 @@ def test_reference_exports_record_error_when_asked():
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
     assert int(r.stdout.strip().splitlines()[-1]) != 0
+
+
+def test_struct_layouts_match_the_library():
+    lib = photonmap.load()
+    structs = [photonmap.Scene, photonmap.Config, photonmap.PhotonRecord, photonmap.FrameStats,
+               photonmap.CacheConfig, photonmap.CacheStats]
+    for which, st in enumerate(structs):
+        assert lib.pm_abi_struct_size(which) == ctypes.sizeof(st), st.__name__
+
+
+def test_cache_default_config():
+    cfg = photonmap.cache_default_config()
+    assert (cfg.levels, cfg.log2_table, cfg.base_res, cfg.max_res) == (16, 19, 16, 2048)
+    assert cfg.train_samples == 1 << 20 and cfg.batch % 128 == 0

@@ -1,0 +1,166 @@
+"""Learned radiance cache on the GPU, through the C ABI: the query-list
+render against pm_render, the encoding and the tensor-core forward/backward
+against the FP64 oracle (oracle/cache_oracle.py), training, files."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+import photonmap  # noqa: E402
+import cache_oracle as co  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def small(preset, surface=20000, volume=20000, size=(48, 40), seed=0x5EED0001):
+    sc, cf = photonmap.preset(preset, seed)
+    cf.surface_photons, cf.volume_photons = surface, volume
+    cf.width, cf.height = size
+    return sc, cf
+
+
+@pytest.fixture
+def ctx():
+    c = photonmap.Context(0)
+    yield c
+    c.close()
+
+
+def frame(ctx, sc, cf):
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    ctx.build()
+
+
+def render(ctx, cf, cached=None):
+    rad = torch.zeros((cf.height * cf.width, 4), dtype=torch.float32, device="cuda")
+    if cached is None:
+        ctx.render(rad.data_ptr(), None)
+    else:
+        ctx.render_cached(rad.data_ptr(), None, cached)
+    torch.cuda.synchronize()
+    return rad.cpu().numpy()
+
+
+def rel_rmse(a, b):
+    return float(np.sqrt(np.mean((a[:, :3] - b[:, :3]) ** 2)) / np.sqrt(np.mean(b[:, :3] ** 2)))
+
+
+def scene_geometry(sc):
+    spheres = np.array([list(sc.spheres[i]) for i in range(sc.num_spheres)], np.float64)
+    axes = [int(sc.planes[i][0]) for i in range(sc.num_planes)]
+    return spheres, axes
+
+
+@pytest.mark.parametrize("preset,size", [(1, (48, 40)), (2, (40, 40)), (3, (64, 36))])
+def test_query_list_render_equals_render(ctx, preset, size):
+    sc, cf = small(preset, size=size)
+    frame(ctx, sc, cf)
+    ref = render(ctx, cf)
+    ctx.cache_enable(log2_table=12)
+    via = render(ctx, cf, cached=1)
+    # same queries in the same order; only the factor order of each term differs
+    np.testing.assert_allclose(via[:, :3], ref[:, :3], rtol=2e-5, atol=1e-6 * ref[:, :3].max())
+    st = ctx.stats()
+    assert ctx.cache_stats().queries == st.surface_gathers + st.volume_gathers
+
+
+def enable_small(ctx, sc, log2_table=12, table_seed=7, table_scale=0.5):
+    cfg = ctx.cache_enable(log2_table=log2_table)
+    w, t, res = ctx.cache_params()
+    rng = np.random.default_rng(table_seed)
+    t = rng.uniform(-table_scale, table_scale, t.shape).astype(np.float32)
+    ctx.cache_set_params(table=t)
+    return cfg, w, t, res
+
+
+def sample_queries(ctx, n, seed=3):
+    qa, qd = ctx.cache_queries()
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(qa), n, replace=len(qa) < n)
+    return qa[pick], qd[pick]
+
+
+def test_encoding_matches_oracle(ctx):
+    sc, cf = small(2, size=(40, 40))
+    frame(ctx, sc, cf)
+    cfg, w, t, res = enable_small(ctx, sc)
+    qa, qd = sample_queries(ctx, 700)
+    kinds = qa[:, 3].view(np.int32) != co.KNONE
+    assert kinds.any() and (~kinds).any()
+    out = ctx.cache_debug_step(qa, qd, np.ones((len(qa), 4), np.float32))
+    lo, inv = co.grid_box(sc.box_min, sc.box_max)
+    spheres, axes = scene_geometry(sc)
+    x = co.features(qa, qd, lo, inv, t, res, cfg.log2_table, spheres, axes)
+    np.testing.assert_allclose(out["x"][:, :32], x[:, :32], rtol=0, atol=2e-5)
+    np.testing.assert_allclose(out["x"][:, 32:], x[:, 32:], rtol=0, atol=2e-6)
+
+
+@pytest.mark.parametrize("n", [128, 1000, 5000])
+def test_forward_backward_matches_oracle(ctx, n):
+    sc, cf = small(2, size=(40, 40))
+    frame(ctx, sc, cf)
+    cfg, w, t, res = enable_small(ctx, sc, table_scale=0.3)
+    qa, qd = sample_queries(ctx, n, seed=n)
+    rng = np.random.default_rng(11)
+    target = np.zeros((n, 4), np.float32)
+    target[:, :3] = rng.uniform(0.0, 2.0, (n, 3))
+    scale = 1.7
+    out = ctx.cache_debug_step(qa, qd, target, target_scale=scale)
+    assert ctx.cache_stats().tc_status == 0
+    ref = co.mlp_step(out["x"].astype(np.float64), w, target[:, :3] / np.float32(scale),
+                      eps=cfg.loss_eps)
+    y = out["y"][:, :3]
+    assert np.linalg.norm(y - ref["y"]) / np.linalg.norm(ref["y"]) < 1e-2
+    assert abs(out["loss"] - ref["loss"]) / ref["loss"] < 1e-2
+    gw = out["w_grad"]
+    for l, (a, b) in enumerate(zip(co.split_weights(gw), co.split_weights(ref["w_grad"]))):
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err < 2e-2, (l, err)
+    lo, inv = co.grid_box(sc.box_min, sc.box_max)
+    tg = co.table_grad(co.unit_pos(qa[:, :3], lo, inv), ref["dx"], res, cfg.log2_table)
+    err = np.linalg.norm(out["table_grad"] - tg) / np.linalg.norm(tg)
+    assert err < 2e-2, err
+
+
+def test_training_learns_the_knn_estimate(ctx):
+    """What the trained network gains: the untrained cache renders with
+    ~100 % error against the k-NN render; after training it is within a few
+    per cent."""
+    sc, cf = small(1, 30000, 30000, size=(64, 48))
+    frame(ctx, sc, cf)
+    ctx.cache_enable(train_samples=1 << 16, batch=1 << 12)
+    knn = render(ctx, cf, cached=1)
+    untrained = rel_rmse(render(ctx, cf, cached=0), knn)
+    ctx.cache_train(2)
+    first = ctx.cache_stats().loss
+    ctx.cache_train(78)
+    st = ctx.cache_stats()
+    assert st.tc_status == 0
+    assert st.train_steps == 80 * 16
+    trained = rel_rmse(render(ctx, cf, cached=0), knn)
+    print("untrained %.4f trained %.4f loss %.4g -> %.4g" % (untrained, trained, first, st.loss))
+    assert st.loss < 0.5 * first, (first, st.loss)
+    assert trained < 0.25 * untrained, (untrained, trained)
+    assert trained < 0.1, trained
+
+
+def test_cache_file_round_trip(ctx, tmp_path):
+    sc, cf = small(1, size=(32, 32))
+    frame(ctx, sc, cf)
+    ctx.cache_enable(log2_table=12, train_samples=1 << 12, batch=1 << 11)
+    ctx.cache_train(3)
+    a = render(ctx, cf, cached=0)
+    path = str(tmp_path / "cache.bin")
+    ctx.cache_save(path)
+    w0, t0, _ = ctx.cache_params()
+    ctx.cache_enable(log2_table=12, train_samples=1 << 12, batch=1 << 11, seed=99)
+    ctx.cache_load(path)
+    w1, t1, _ = ctx.cache_params()
+    np.testing.assert_array_equal(w0, w1)
+    np.testing.assert_array_equal(t0, t1)
+    b = render(ctx, cf, cached=0)
+    np.testing.assert_array_equal(a, b)
+    assert ctx.cache_stats().train_steps == 6
+    ctx.cache_enable(log2_table=13)
+    with pytest.raises(photonmap.PMError):
+        ctx.cache_load(path)
