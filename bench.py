@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--seed", type=lambda s: int(s, 0), default=0x5EED0002)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache A/B")
+    ap.add_argument("--cache-warm-frames", type=int, default=128)
     return ap.parse_args()
 
 
@@ -175,6 +177,102 @@ def cpu_frame_sample(scene, cfg, pixels, seed=1234):
         "sample_pixels": int(len(pix)),
         "paths": int(max(maps.paths)),
         "cores": os.cpu_count(),
+    }
+
+
+def peaks_bf16():
+    """(dense bf16 TFLOP/s, source) of the GB300s."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        for key in ("bf16_tflops", "bf16_tflops_burst"):
+            if key in d:
+                return float(d[key]), "measured " + key
+    except (OSError, ValueError):
+        pass
+    return 1900.0, "fallback"
+
+
+# Tensor-core FLOPs per query of the cache network as the kernels issue
+# them: 4 hidden 64x64 layers and the 64x16 output layer (inference); the
+# training kernel adds the activation-gradient GEMMs (same shapes) and the
+# weight-gradient GEMMs, issued as two 128x128x128 and one 128x16x128 per
+# 128-sample tile (half of the 128x128 products are unused blocks).
+CACHE_INFER_FLOPS = 2 * (4 * 64 * 64 + 64 * 16)
+CACHE_TRAIN_FLOPS = 2 * CACHE_INFER_FLOPS + 2 * (2 * 128 * 128 + 128 * 16)
+
+
+def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak):
+    """The learned radiance cache on the same scene and photon maps: after
+    `cache_warm_frames` online training frames, each timed step is one online
+    frame (2^20 k-NN training samples + their Adam steps, then the cached
+    render of every query). Error is the relative RMSE of the cached image
+    against the k-NN render of the same frame (the cache's judge)."""
+    import numpy as np
+    import torch
+    sh = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        ctx.render(rad.data_ptr(), None, sh)
+        stream.synchronize()
+        knn_img = rad[:, :3].double().cpu().numpy()
+        cc = ctx.cache_enable()
+        t0 = time.perf_counter()
+        ctx.cache_train(args.cache_warm_frames, sh)
+        stream.synchronize()
+        warm_s = time.perf_counter() - t0
+        for _ in range(2):
+            ctx.render_cached(rad.data_ptr(), None, 0, sh)
+        frame_ms, train_ms, render_ms, targets_ms, values_ms = [], [], [], [], []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e2 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.cache_train(1, sh)
+            e1.record(stream)
+            ctx.render_cached(rad.data_ptr(), None, 0, sh)
+            e2.record(stream)
+            e2.synchronize()
+            cs = ctx.cache_stats()
+            frame_ms.append(e0.elapsed_time(e2))
+            train_ms.append(e0.elapsed_time(e1))
+            render_ms.append(e1.elapsed_time(e2))
+            targets_ms.append(cs.ms_targets)
+            values_ms.append(cs.ms_values)
+        cached = rad[:, :3].double().cpu().numpy()
+    err = float(np.sqrt(np.mean((cached - knn_img) ** 2)) / np.sqrt(np.mean(knn_img ** 2)))
+    nq = cs.queries
+    values_s = statistics.mean(values_ms) / 1e3
+    infer_tflops = nq * CACHE_INFER_FLOPS / values_s / 1e12
+    steps_per_frame = -(-cc.train_samples // cc.batch)
+    train_s = statistics.mean(train_ms) / 1e3 - statistics.mean(targets_ms) / 1e3
+    train_tflops = cc.train_samples * CACHE_TRAIN_FLOPS / train_s / 1e12
+    return {
+        "workload": "preset-2 scene and maps; 16-level hash grid (2^19 x 2 fp16 per level), "
+                    "4x64 ReLU MLP in bf16 on tcgen05 with fp32 TMEM accumulation; %d k-NN "
+                    "training samples per frame, batch %d; inference on every render query"
+                    % (cc.train_samples, cc.batch),
+        "warm_frames": args.cache_warm_frames, "warm_s": warm_s,
+        "train_steps": int(cs.train_steps), "steps_per_frame": steps_per_frame,
+        "frame_ms": statistics.mean(frame_ms),
+        "train_ms": statistics.mean(train_ms), "targets_ms": statistics.mean(targets_ms),
+        "render_ms": statistics.mean(render_ms), "infer_ms": statistics.mean(values_ms),
+        "knn_render_ms": knn_render_ms,
+        "speedup_online_frame": knn_render_ms / statistics.mean(frame_ms),
+        "speedup_render": knn_render_ms / statistics.mean(render_ms),
+        "rel_rmse_vs_knn": err,
+        "queries_per_frame": int(nq), "queries_per_s": nq / values_s,
+        "loss": float(cs.loss),
+        "tensor": {"infer_tflops": infer_tflops, "train_tflops": train_tflops,
+                   "peak_tflops": bf16_peak[0], "peak_source": bf16_peak[1],
+                   "infer_frac": infer_tflops / bf16_peak[0],
+                   "train_frac": train_tflops / bf16_peak[0],
+                   "flops_per_query_infer": CACHE_INFER_FLOPS,
+                   "flops_per_sample_train": CACHE_TRAIN_FLOPS},
+        "tc_status": int(cs.tc_status),
+        "l2": "flushed before each timed frame",
     }
 
 
@@ -363,6 +461,9 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    if not args.no_cache:
+        line["cache"] = cache_ab(ctx, lib, stream, rad, flush, args, cfg,
+                                 statistics.mean(render_ms), peaks_bf16())
     if world == 1 and not args.no_cpu_baseline:
         r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
         line["cpu_baseline"] = {

@@ -164,3 +164,29 @@ def test_cache_file_round_trip(ctx, tmp_path):
     ctx.cache_enable(log2_table=13)
     with pytest.raises(photonmap.PMError):
         ctx.cache_load(path)
+
+
+def test_cached_render_against_float64_at_bench_scale(ctx):
+    """The A/B of the benchmark scene (preset 2: 1M + 1M photons, 1024^2,
+    k = 100): the cached render after 128 online training frames and the
+    k-NN render, both against the FP64 oracle render on 8192 random pixels.
+    The cache must stay within 1e-2 relative RMSE of the k-NN render and
+    within 1e-2 of the k-NN render's own error against FP64."""
+    import oracle
+    sc, cf = photonmap.preset(2, 0x5EED0002)
+    frame(ctx, sc, cf)
+    knn = render(ctx, cf)
+    ctx.cache_enable()
+    ctx.cache_train(128)
+    cached = render(ctx, cf, cached=0)
+    assert ctx.cache_stats().tc_status == 0
+    rng = np.random.default_rng(2024)
+    pix = np.sort(rng.choice(cf.width * cf.height, 8192, replace=False)).astype(np.uint32)
+    m64 = oracle.emit(sc, cf, None, double=True)
+    r64 = oracle.render(sc, cf, None, m64, pixels=pix, double=True)
+    e_knn = rel_rmse(knn[pix], r64)
+    e_cache = rel_rmse(cached[pix], r64)
+    e_ab = rel_rmse(cached, knn)
+    print("rel RMSE vs FP64: k-NN %.4f cached %.4f; cached vs k-NN %.4f" % (e_knn, e_cache, e_ab))
+    assert e_ab < 1e-2, e_ab
+    assert e_cache < e_knn + 1e-2, (e_knn, e_cache)
