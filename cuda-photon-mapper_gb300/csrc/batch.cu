@@ -1,0 +1,642 @@
+// batch.cu -- many independent scenes per frame behind the pm_batch_* C ABI:
+// persistent multi-scene trace and render launches, per-scene kd builds on
+// side streams, CUDA-graph capture of the whole frame, and the autotuner of
+// the search knobs.
+//
+// Frame (all on the caller's stream, no host round trip):
+//   1. zero the per-scene words, path counts and gather counters
+//   2. counting pass: one persistent launch over every scene's paths
+//   3. per scene and map: scan of the path counts over the whole path cap
+//      (zero beyond the issued paths) -> record extent (records, paths)
+//   4. writing pass: one persistent launch
+//   5. per scene and map, on kBuildStreams side streams: records past the
+//      map's size are set to infinity, then the kd-tree is built over the
+//      map's capacity (so every launch size is a host constant)
+//   6. one persistent render launch over every scene's pixels
+// A scene's image equals the single-scene render of the same scene bit for
+// bit: the paths, extents and records are the same, and the k-NN lists do
+// not depend on the tree (records at infinity are never within a radius).
+#include "gather.cuh"
+#include "kdtree.cuh"
+#include "launch_count.cuh"
+#include "pm_ctx.cuh"
+#include "radix_sort.cuh"
+#include "scene.cuh"
+#include "trace.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace pm {
+namespace {
+
+constexpr int kBuildStreams = 8;
+constexpr int kWords = 16;  // device words per scene, all reset every frame
+enum {
+    W_COUNTER = 0,  // path counter (count pass, then write pass)
+    W_STORED_S = 1, W_STORED_V = 2,
+    W_TOTAL_S = 3, W_TOTAL_V = 4,   // scan totals
+    W_EXT_S = 5,                    // records, paths of the surface map
+    W_EXT_V = 7,                    // records, paths of the volume map
+    W_ISSUED = 9,                   // paths issued by the counting pass
+};
+constexpr int kPathCapFactor = 8;
+
+__global__ void reset_counters_kernel(uint32_t *words, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    words[s * kWords + W_ISSUED] = words[s * kWords + W_COUNTER];
+    words[s * kWords + W_COUNTER] = 0u;
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+int shift_of(int leaf_size) { return leaf_size >= 128 ? 2 : (leaf_size >= 64 ? 1 : 0); }
+
+}  // namespace
+}  // namespace pm
+
+using namespace pm;
+
+struct pm_batch {
+    pm_ctx *ctx = nullptr;
+    int n = 0;
+    int sm_count = 148;
+    std::vector<pm_scene> scenes;
+    std::vector<pm_config> cfgs;
+    std::vector<PScene> dsc;
+    std::vector<float *> het;
+    struct Map {
+        float4 *pos = nullptr, *pow = nullptr, *tpos = nullptr, *tpow = nullptr;
+        float4 *lo = nullptr, *hi = nullptr;
+        uint32_t cap = 0;
+    };
+    std::vector<Map> maps;             // 2 per scene
+    std::vector<uint32_t> path_cap;    // per scene
+    std::vector<size_t> cnt_off;       // offset of scene s's counts in the pools
+    std::vector<size_t> pix_off;       // offset of scene s's pixels in the image pools
+    std::vector<pm_batch_tune> tune;
+    uint32_t *cnt = nullptr, *off = nullptr;  // pools: per scene [cnt_s | cnt_v] over the path cap
+    size_t cnt_words = 0;
+    uint32_t *scan_tmp = nullptr;
+    uint32_t *words = nullptr;         // kWords per scene
+    uint32_t *capn = nullptr;          // 2 per scene: map capacities (device n of the builds)
+    unsigned long long *gathers = nullptr;  // 2 per scene
+    uint32_t *work = nullptr;
+    float4 *rad = nullptr;
+    uchar4 *rgba = nullptr;
+    PScene *scenes_dev = nullptr;
+    TraceParams *count_dev = nullptr, *write_dev = nullptr;
+    BatchRenderScene *render_dev = nullptr;
+    uint32_t *prefix_dev = nullptr;
+    struct Sort {
+        uint64_t *keys = nullptr, *keys_tmp = nullptr;
+        uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
+    } sort[kBuildStreams];
+    cudaStream_t side[kBuildStreams] = {};
+    cudaEvent_t fork = nullptr, join[kBuildStreams] = {};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long graph_kernels = 0;
+    bool ran = false;
+};
+
+namespace {
+
+void free_batch(pm_batch *b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto &m : b->maps) {
+        cudaFree(m.pos); cudaFree(m.pow); cudaFree(m.tpos); cudaFree(m.tpow);
+        cudaFree(m.lo); cudaFree(m.hi);
+    }
+    for (float *h : b->het) cudaFree(h);
+    cudaFree(b->cnt); cudaFree(b->off); cudaFree(b->scan_tmp); cudaFree(b->words);
+    cudaFree(b->capn); cudaFree(b->gathers); cudaFree(b->work); cudaFree(b->rad); cudaFree(b->rgba);
+    cudaFree(b->scenes_dev); cudaFree(b->count_dev); cudaFree(b->write_dev);
+    cudaFree(b->render_dev); cudaFree(b->prefix_dev);
+    for (auto &s : b->sort) {
+        cudaFree(s.keys); cudaFree(s.keys_tmp); cudaFree(s.vals); cudaFree(s.vals_tmp); cudaFree(s.hist);
+    }
+    for (auto &s : b->side)
+        if (s) cudaStreamDestroy(s);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (auto &e : b->join)
+        if (e) cudaEventDestroy(e);
+    delete b;
+}
+
+int depth_of(const pm_batch *b, int s, int m) {
+    return tree_depth(b->maps[2 * s + m].cap, shift_of(b->tune[s].leaf_size));
+}
+
+BatchRenderScene render_desc(const pm_batch *b, int s) {
+    BatchRenderScene d;
+    memset(&d, 0, sizeof(d));
+    d.sc = b->dsc[s];
+    const pm_config &c = b->cfgs[s];
+    for (int m = 0; m < 2; ++m) {
+        const auto &mp = b->maps[2 * s + m];
+        MapView v;
+        v.pos = mp.tpos;
+        v.pow = mp.tpow;
+        v.lo = mp.lo;
+        v.hi = mp.hi;
+        v.n = mp.cap;
+        v.depth = mp.cap ? depth_of(b, s, m) : 0;
+        v.leaf_shift = shift_of(b->tune[s].leaf_size);
+        (m == 0 ? d.surf : d.vol) = v;
+    }
+    RenderParams R;
+    R.width = c.width;
+    R.height = c.height;
+    R.aspect = c.height > 0 ? (float)c.width / (float)c.height : 1.0f;
+    R.k = c.k;
+    R.r2cap = c.radius * c.radius;
+    R.step = c.march_step;
+    R.exposure = c.exposure;
+    R.seed = c.seed;
+    R.scene_id = c.scene_id;
+    R.counters = b->gathers + 2 * s;
+    R.tune.collect_max = b->tune[s].collect_max;
+    R.tune.merge_min = b->tune[s].merge_min;
+    d.R = R;
+    d.rad = b->rad + b->pix_off[s];
+    d.rgba = b->rgba + b->pix_off[s];
+    d.slots = slots_for_k(c.k);
+    d.tile = b->tune[s].tile;
+    return d;
+}
+
+// Uploads the render descriptors and chunk prefix of scenes `ids` (all
+// scenes when empty) to dst / prefix.
+cudaError_t upload_render(const pm_batch *b, const std::vector<int> &ids, BatchRenderScene *dst,
+                          uint32_t *prefix) {
+    std::vector<BatchRenderScene> d;
+    std::vector<uint32_t> pre(1, 0u);
+    for (int s : ids) {
+        d.push_back(render_desc(b, s));
+        const uint64_t npix = (uint64_t)b->cfgs[s].width * (uint64_t)b->cfgs[s].height;
+        const uint64_t per = (uint64_t)4 * (uint64_t)b->tune[s].tile;
+        pre.push_back(pre.back() + (uint32_t)((npix + per - 1) / per));
+    }
+    cudaError_t e = cudaMemcpy(dst, d.data(), sizeof(BatchRenderScene) * d.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(prefix, pre.data(), sizeof(uint32_t) * pre.size(), cudaMemcpyHostToDevice);
+}
+
+std::vector<int> all_ids(const pm_batch *b) {
+    std::vector<int> v(b->n);
+    for (int i = 0; i < b->n; ++i) v[i] = i;
+    return v;
+}
+
+// Pads and builds the two trees of scene s on `st` with sort scratch `so`.
+cudaError_t build_scene(pm_batch *b, int s, cudaStream_t st, const pm_batch::Sort &so) {
+    for (int m = 0; m < 2; ++m) {
+        auto &mp = b->maps[2 * s + m];
+        if (mp.cap == 0) continue;
+        cudaError_t e = pad_map(mp.pos, mp.pow, b->words + s * kWords + (m == 0 ? W_EXT_S : W_EXT_V),
+                                mp.cap, st);
+        if (e != cudaSuccess) return e;
+        KdBuildArgs a;
+        a.n = mp.cap;
+        a.n_dev = b->capn + 2 * s + m;
+        const pm_scene &sc = b->scenes[s];
+        a.lo = make_float3(sc.box_min[0], sc.box_min[1], sc.box_min[2]);
+        a.hi = make_float3(sc.box_max[0], sc.box_max[1], sc.box_max[2]);
+        a.box_dev = nullptr;
+        a.pos_in = mp.pos;
+        a.pow_in = mp.pow;
+        a.pos_out = mp.tpos;
+        a.pow_out = mp.tpow;
+        a.node_lo = mp.lo;
+        a.node_hi = mp.hi;
+        a.keys = so.keys; a.keys_tmp = so.keys_tmp;
+        a.vals = so.vals; a.vals_tmp = so.vals_tmp;
+        a.hist = so.hist;
+        a.order_out = nullptr;
+        a.leaf_shift = shift_of(b->tune[s].leaf_size);
+        e = build_tree(a, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
+    cudaError_t e;
+#define B_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    B_TRY(cudaMemsetAsync(b->words, 0, sizeof(uint32_t) * kWords * b->n, st));
+    B_TRY(cudaMemsetAsync(b->cnt, 0, sizeof(uint32_t) * b->cnt_words, st));
+    B_TRY(cudaMemsetAsync(b->gathers, 0, sizeof(unsigned long long) * 2 * b->n, st));
+    B_TRY(trace_photons_batch(b->scenes_dev, b->count_dev, b->n, b->sm_count, st));
+    for (int s = 0; s < b->n; ++s) {
+        uint32_t *w = b->words + s * kWords;
+        const uint32_t cap = b->path_cap[s];
+        const size_t o = b->cnt_off[s];
+        B_TRY(map_extent_dev(cap, w + W_COUNTER, b->cnt + o, b->off + o, w + W_TOTAL_S, b->scan_tmp,
+                             b->cfgs[s].surface_photons, w + W_EXT_S, st));
+        B_TRY(map_extent_dev(cap, w + W_COUNTER, b->cnt + o + cap, b->off + o + cap, w + W_TOTAL_V,
+                             b->scan_tmp, b->cfgs[s].volume_photons, w + W_EXT_V, st));
+    }
+    reset_counters_kernel<<<(b->n + 127) / 128, 128, 0, st>>>(b->words, b->n);
+    note_launch();
+    B_TRY(cudaGetLastError());
+    B_TRY(trace_photons_batch(b->scenes_dev, b->write_dev, b->n, b->sm_count, st));
+    B_TRY(cudaEventRecord(b->fork, st));
+    for (int k = 0; k < kBuildStreams; ++k) B_TRY(cudaStreamWaitEvent(b->side[k], b->fork, 0));
+    for (int s = 0; s < b->n; ++s) {
+        const int k = s % kBuildStreams;
+        B_TRY(build_scene(b, s, b->side[k], b->sort[k]));
+    }
+    for (int k = 0; k < kBuildStreams; ++k) {
+        B_TRY(cudaEventRecord(b->join[k], b->side[k]));
+        B_TRY(cudaStreamWaitEvent(st, b->join[k], 0));
+    }
+    B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n, b->work, b->sm_count, st));
+#undef B_TRY
+    return cudaSuccess;
+}
+
+void drop_graph(pm_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_config *cfgs,
+                          pm_batch **out) {
+    if (!ctx || !out || n < 1 || n > 4096 || !scenes || !cfgs) return PM_ERR_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        std::string why;
+        pm_status s = validate(scenes[i], cfgs[i], &why);
+        if (s != PM_OK) return fail(ctx, s, "scene " + std::to_string(i) + ": " + why);
+        if (std::max(cfgs[i].surface_photons, cfgs[i].volume_photons) > (1u << 26))
+            return fail(ctx, PM_ERR_LIMIT, "batched map above 2^26 records");
+    }
+    DeviceGuard g(ctx->device);
+    pm_batch *b = new pm_batch();
+    b->ctx = ctx;
+    b->n = n;
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+    b->scenes.assign(scenes, scenes + n);
+    b->cfgs.assign(cfgs, cfgs + n);
+    b->maps.resize(2 * (size_t)n);
+    b->het.assign(n, nullptr);
+    b->tune.resize(n);
+    cudaError_t e = cudaSuccess;
+#define C_TRY(x) do { e = (x); if (e != cudaSuccess) { free_batch(b); return check_cuda(ctx, e, #x); } } while (0)
+    size_t cnt_words = 0, pix = 0;
+    uint32_t max_cap = 0, max_map = 1;
+    for (int s = 0; s < n; ++s) {
+        const pm_config &c = cfgs[s];
+        b->tune[s] = pm_batch_tune{c.leaf_size, 1, 128, 16};
+        const uint32_t tmax = std::max(c.surface_photons, c.volume_photons);
+        uint64_t cap = c.max_paths ? c.max_paths : (uint64_t)tmax * kPathCapFactor;
+        cap = std::max<uint64_t>(cap, 1024);
+        if (cap > (1ull << 30)) { free_batch(b); return fail(ctx, PM_ERR_LIMIT, "path cap above 2^30"); }
+        b->path_cap.push_back((uint32_t)cap);
+        b->cnt_off.push_back(cnt_words);
+        cnt_words += 2 * cap;
+        max_cap = std::max(max_cap, (uint32_t)cap);
+        b->pix_off.push_back(pix);
+        pix += (size_t)c.width * (size_t)c.height;
+        const uint32_t targets[2] = {c.surface_photons, c.volume_photons};
+        for (int m = 0; m < 2; ++m) {
+            auto &mp = b->maps[2 * s + m];
+            mp.cap = targets[m];
+            max_map = std::max(max_map, mp.cap);
+            C_TRY(dalloc(&mp.pos, mp.cap));
+            C_TRY(dalloc(&mp.pow, mp.cap));
+            C_TRY(dalloc(&mp.tpos, mp.cap));
+            C_TRY(dalloc(&mp.tpow, mp.cap));
+            C_TRY(dalloc(&mp.lo, tree_nodes(mp.cap)));
+            C_TRY(dalloc(&mp.hi, tree_nodes(mp.cap)));
+        }
+        if (scenes[s].het_res > 0) {
+            const size_t nv = (size_t)scenes[s].het_res * scenes[s].het_res * scenes[s].het_res;
+            C_TRY(dalloc(&b->het[s], nv));
+            C_TRY(make_noise_grid(b->het[s], scenes[s].het_res, c.seed ^ 0x6E6F697365ull,
+                                  scenes[s].het_min, scenes[s].het_max, 0));
+        }
+        b->dsc.push_back(to_device_scene(scenes[s], b->het[s]));
+    }
+    b->cnt_words = cnt_words;
+    C_TRY(dalloc(&b->cnt, cnt_words));
+    C_TRY(dalloc(&b->off, cnt_words));
+    C_TRY(dalloc(&b->scan_tmp, scan_tile_count(max_cap) + 1));
+    C_TRY(dalloc(&b->words, (size_t)kWords * n));
+    C_TRY(dalloc(&b->capn, 2 * (size_t)n));
+    C_TRY(dalloc(&b->gathers, 2 * (size_t)n));
+    C_TRY(dalloc(&b->work, 1));
+    C_TRY(dalloc(&b->rad, pix));
+    C_TRY(dalloc(&b->rgba, pix));
+    C_TRY(dalloc(&b->scenes_dev, n));
+    C_TRY(dalloc(&b->count_dev, n));
+    C_TRY(dalloc(&b->write_dev, n));
+    C_TRY(dalloc(&b->render_dev, n));
+    C_TRY(dalloc(&b->prefix_dev, (size_t)n + 1));
+    for (auto &so : b->sort) {
+        C_TRY(dalloc(&so.keys, max_map));
+        C_TRY(dalloc(&so.keys_tmp, max_map));
+        C_TRY(dalloc(&so.vals, max_map));
+        C_TRY(dalloc(&so.vals_tmp, max_map));
+        C_TRY(dalloc(&so.hist, radix_sort_hist_words(max_map)));
+    }
+    for (auto &st : b->side) C_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    C_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    for (auto &ev : b->join) C_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    // static per-scene parameters
+    std::vector<uint32_t> capn(2 * (size_t)n);
+    std::vector<TraceParams> cp(n), wp(n);
+    for (int s = 0; s < n; ++s) {
+        const pm_config &c = cfgs[s];
+        capn[2 * s] = b->maps[2 * s].cap;
+        capn[2 * s + 1] = b->maps[2 * s + 1].cap;
+        uint32_t *w = b->words + s * kWords;
+        const size_t o = b->cnt_off[s];
+        const uint32_t cap = b->path_cap[s];
+        TraceParams P;
+        memset(&P, 0, sizeof(P));
+        P.seed = c.seed;
+        P.scene_id = c.scene_id;
+        P.max_bounces = c.max_bounces;
+        P.rr = c.rr_survival;
+        P.target_s = c.surface_photons;
+        P.target_v = c.volume_photons;
+        P.path_cap = cap;
+        P.path_counter = w + W_COUNTER;
+        P.stored_s = w + W_STORED_S;
+        P.stored_v = w + W_STORED_V;
+        P.cnt_s = b->cnt + o;
+        P.cnt_v = b->cnt + o + cap;
+        cp[s] = P;
+        P.store = 1;
+        P.off_s = b->off + o;
+        P.off_v = b->off + o + cap;
+        P.ext_s = w + W_EXT_S;
+        P.ext_v = w + W_EXT_V;
+        P.power = scenes[s].light_power;
+        P.spos = b->maps[2 * s].pos; P.spow = b->maps[2 * s].pow;
+        P.vpos = b->maps[2 * s + 1].pos; P.vpow = b->maps[2 * s + 1].pow;
+        wp[s] = P;
+    }
+    C_TRY(cudaMemcpy(b->capn, capn.data(), sizeof(uint32_t) * capn.size(), cudaMemcpyHostToDevice));
+    C_TRY(cudaMemcpy(b->scenes_dev, b->dsc.data(), sizeof(PScene) * n, cudaMemcpyHostToDevice));
+    C_TRY(cudaMemcpy(b->count_dev, cp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
+    C_TRY(cudaMemcpy(b->write_dev, wp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
+    C_TRY(upload_render(b, all_ids(b), b->render_dev, b->prefix_dev));
+    C_TRY(cudaDeviceSynchronize());
+#undef C_TRY
+    *out = b;
+    return PM_OK;
+}
+
+void pm_batch_destroy(pm_batch *b) {
+    if (!b) return;
+    DeviceGuard g(b->ctx->device);
+    cudaDeviceSynchronize();
+    free_batch(b);
+}
+
+pm_status pm_batch_frame(pm_batch *b, cudaStream_t stream) {
+    if (!b) return PM_ERR_INVALID;
+    DeviceGuard g(b->ctx->device);
+    cudaError_t e = enqueue_frame(b, stream);
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "pm_batch_frame");
+    b->ran = true;
+    return PM_OK;
+}
+
+pm_status pm_batch_capture(pm_batch *b, cudaStream_t stream) {
+    if (!b) return PM_ERR_INVALID;
+    DeviceGuard g(b->ctx->device);
+    drop_graph(b);
+    cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "cudaStreamBeginCapture");
+    const unsigned long long l0 = launch_counter().load();
+    cudaError_t fe = enqueue_frame(b, stream);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(stream, &graph);
+    if (fe != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return check_cuda(b->ctx, fe, "pm_batch_capture (frame)");
+    }
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "cudaStreamEndCapture");
+    b->graph = graph;
+    b->graph_kernels = launch_counter().load() - l0;
+    // the captured launches ran nowhere: take them off the launch count
+    launch_counter().fetch_sub(b->graph_kernels);
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (e != cudaSuccess) {
+        drop_graph(b);
+        return check_cuda(b->ctx, e, "cudaGraphInstantiate");
+    }
+    return PM_OK;
+}
+
+pm_status pm_batch_launch(pm_batch *b, cudaStream_t stream) {
+    if (!b) return PM_ERR_INVALID;
+    if (!b->exec) return fail(b->ctx, PM_ERR_STATE, "pm_batch_launch before pm_batch_capture");
+    DeviceGuard g(b->ctx->device);
+    cudaError_t e = cudaGraphLaunch(b->exec, stream);
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "cudaGraphLaunch");
+    note_launches(b->graph_kernels);
+    b->ran = true;
+    return PM_OK;
+}
+
+pm_status pm_batch_image(pm_batch *b, int scene, float4 **radiance, uchar4 **rgba) {
+    if (!b || scene < 0 || scene >= b->n) return PM_ERR_INVALID;
+    if (radiance) *radiance = b->rad + b->pix_off[scene];
+    if (rgba) *rgba = b->rgba + b->pix_off[scene];
+    return PM_OK;
+}
+
+pm_status pm_batch_read(pm_batch *b, int scene, float4 *radiance, uchar4 *rgba) {
+    if (!b || scene < 0 || scene >= b->n) return PM_ERR_INVALID;
+    DeviceGuard g(b->ctx->device);
+    const size_t npix = (size_t)b->cfgs[scene].width * (size_t)b->cfgs[scene].height;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && radiance && npix)
+        e = cudaMemcpy(radiance, b->rad + b->pix_off[scene], sizeof(float4) * npix, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && rgba && npix)
+        e = cudaMemcpy(rgba, b->rgba + b->pix_off[scene], sizeof(uchar4) * npix, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "pm_batch_read");
+    return PM_OK;
+}
+
+pm_status pm_batch_stats(pm_batch *b, int scene, pm_frame_stats *out) {
+    if (!b || !out || scene < 0 || scene >= b->n) return PM_ERR_INVALID;
+    DeviceGuard g(b->ctx->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    uint32_t w[kWords];
+    unsigned long long gc[2];
+    if (e == cudaSuccess)
+        e = cudaMemcpy(w, b->words + scene * kWords, sizeof(w), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(gc, b->gathers + 2 * scene, sizeof(gc), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "pm_batch_stats");
+    memset(out, 0, sizeof(*out));
+    out->paths_traced = std::min(w[W_ISSUED], b->path_cap[scene]);
+    out->map_size[0] = w[W_EXT_S];
+    out->map_paths[0] = w[W_EXT_S + 1];
+    out->map_size[1] = w[W_EXT_V];
+    out->map_paths[1] = w[W_EXT_V + 1];
+    out->surface_gathers = gc[0];
+    out->volume_gathers = gc[1];
+    return PM_OK;
+}
+
+pm_status pm_batch_set_tune(pm_batch *b, int scene, const pm_batch_tune *t) {
+    if (!b || !t || scene < 0 || scene >= b->n) return PM_ERR_INVALID;
+    if ((t->leaf_size != 32 && t->leaf_size != 64 && t->leaf_size != 128) || t->tile < 1 ||
+        t->tile > 64 || (t->collect_max != 32 && t->collect_max != 64 && t->collect_max != 128) ||
+        t->merge_min < 1 || t->merge_min > 33)
+        return fail(b->ctx, PM_ERR_INVALID, "invalid batch tune");
+    DeviceGuard g(b->ctx->device);
+    cudaDeviceSynchronize();
+    b->tune[scene] = *t;
+    drop_graph(b);
+    cudaError_t e = upload_render(b, all_ids(b), b->render_dev, b->prefix_dev);
+    if (e != cudaSuccess) return check_cuda(b->ctx, e, "pm_batch_set_tune");
+    return PM_OK;
+}
+
+pm_status pm_batch_get_tune(pm_batch *b, int scene, pm_batch_tune *t) {
+    if (!b || !t || scene < 0 || scene >= b->n) return PM_ERR_INVALID;
+    *t = b->tune[scene];
+    return PM_OK;
+}
+
+pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t stream) {
+    if (!b) return PM_ERR_INVALID;
+    DeviceGuard g(b->ctx->device);
+    pm_ctx *ctx = b->ctx;
+    cudaError_t e;
+#define A_TRY(x) do { e = (x); if (e != cudaSuccess) return check_cuda(ctx, e, #x); } while (0)
+    if (!b->ran) {
+        A_TRY(enqueue_frame(b, stream));
+        b->ran = true;
+    }
+    A_TRY(cudaStreamSynchronize(stream));
+    drop_graph(b);
+    BatchRenderScene *one = nullptr;
+    uint32_t *one_prefix = nullptr;
+    A_TRY(dalloc(&one, 1));
+    A_TRY(dalloc(&one_prefix, 2));
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    std::string js = "{\"format\": \"pm-batch-autotune\", \"version\": 1, \"classes\": [";
+    bool first_class = true;
+    const int leaves[3] = {32, 64, 128}, tiles[4] = {1, 2, 4, 8}, collects[3] = {32, 64, 128},
+              merges[3] = {8, 16, 32};
+    auto time_scene = [&](int s, float *ms_out) -> cudaError_t {
+        cudaError_t ee = upload_render(b, {s}, one, one_prefix);
+        if (ee != cudaSuccess) return ee;
+        float best = 3.0e38f;
+        for (int rep = 0; rep < 3; ++rep) {
+            ee = cudaEventRecord(t0, stream);
+            if (ee == cudaSuccess) ee = render_batch(one, one_prefix, 1, b->work, b->sm_count, stream);
+            if (ee == cudaSuccess) ee = cudaEventRecord(t1, stream);
+            if (ee == cudaSuccess) ee = cudaEventSynchronize(t1);
+            if (ee != cudaSuccess) return ee;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (rep > 0) best = std::min(best, ms);  // first repetition warms the caches
+        }
+        *ms_out = best;
+        return cudaSuccess;
+    };
+    for (int kc = 32; kc <= 128; kc <<= 1) {
+        int rep = -1;
+        uint64_t most = 0;
+        for (int s = 0; s < b->n; ++s) {
+            const uint64_t px = (uint64_t)b->cfgs[s].width * b->cfgs[s].height;
+            if (b->cfgs[s].k == kc && px > most) { most = px; rep = s; }
+        }
+        if (rep < 0) continue;
+        std::string trials;
+        pm_batch_tune best = b->tune[rep];
+        float best_ms = 3.0e38f;
+        for (int li = 0; li < 3; ++li) {
+            b->tune[rep].leaf_size = leaves[li];
+            A_TRY(build_scene(b, rep, stream, b->sort[0]));
+            for (int ti = 0; ti < 4; ++ti) {
+                b->tune[rep].tile = tiles[ti];
+                b->tune[rep].collect_max = 128;
+                b->tune[rep].merge_min = 16;
+                float ms;
+                A_TRY(time_scene(rep, &ms));
+                char buf[160];
+                snprintf(buf, sizeof(buf), "%s{\"leaf_size\": %d, \"tile\": %d, \"collect_max\": 128, "
+                         "\"merge_min\": 16, \"ms\": %.4f}", trials.empty() ? "" : ", ", leaves[li],
+                         tiles[ti], ms);
+                trials += buf;
+                if (ms < best_ms) { best_ms = ms; best = b->tune[rep]; }
+            }
+        }
+        b->tune[rep] = best;
+        A_TRY(build_scene(b, rep, stream, b->sort[0]));
+        for (int ci = 0; ci < 3; ++ci)
+            for (int mi = 0; mi < 3; ++mi) {
+                b->tune[rep].collect_max = collects[ci];
+                b->tune[rep].merge_min = merges[mi];
+                float ms;
+                A_TRY(time_scene(rep, &ms));
+                char buf[160];
+                snprintf(buf, sizeof(buf), ", {\"leaf_size\": %d, \"tile\": %d, \"collect_max\": %d, "
+                         "\"merge_min\": %d, \"ms\": %.4f}", best.leaf_size, best.tile, collects[ci],
+                         merges[mi], ms);
+                trials += buf;
+                if (ms < best_ms) { best_ms = ms; best = b->tune[rep]; }
+            }
+        int members = 0;
+        for (int s = 0; s < b->n; ++s)
+            if (b->cfgs[s].k == kc) { b->tune[s] = best; ++members; }
+        A_TRY(build_scene(b, rep, stream, b->sort[0]));
+        char head[400];
+        snprintf(head, sizeof(head), "%s{\"k\": %d, \"scenes\": %d, \"probe_scene\": %d, \"pixels\": %llu, "
+                 "\"choice\": {\"leaf_size\": %d, \"tile\": %d, \"collect_max\": %d, \"merge_min\": %d, "
+                 "\"ms\": %.4f}, \"trials\": [", first_class ? "" : ", ", kc, members, rep,
+                 (unsigned long long)most, best.leaf_size, best.tile, best.collect_max, best.merge_min,
+                 best_ms);
+        js += head + trials + "]}";
+        first_class = false;
+    }
+    js += "]}\n";
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaFree(one);
+    cudaFree(one_prefix);
+    A_TRY(upload_render(b, all_ids(b), b->render_dev, b->prefix_dev));
+    // every scene's trees follow the new leaf sizes from the next frame on
+    A_TRY(enqueue_frame(b, stream));
+    A_TRY(cudaStreamSynchronize(stream));
+#undef A_TRY
+    if (json_path) {
+        FILE *f = fopen(json_path, "w");
+        if (!f) return fail(ctx, PM_ERR_INVALID, std::string("cannot open ") + json_path);
+        const bool ok = fputs(js.c_str(), f) >= 0;
+        if (fclose(f) != 0 || !ok) return fail(ctx, PM_ERR_INVALID, "short write");
+    }
+    return PM_OK;
+}
+
+}  // extern "C"

@@ -25,7 +25,6 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kStackCap = 192;     // 32 entries per wide level, 6 levels: depth <= 29
 constexpr int kWarpsPerBlock = 4;
 
-constexpr int kMergeMin = 16;       // leaf candidates at or above which insertion is a merge
 
 // Per-warp shared memory: the traversal stack and the staging areas of the
 // bulk merge (the k-list and the sorted leaf candidates).
@@ -214,12 +213,13 @@ __device__ __forceinline__ void load_sorted(Knn<S> &kn, WarpScratch &w, int coun
 // buffer once at the end. Both modes produce the same exact list.
 template <int S>
 __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, int lane,
-                           uint64_t cap, bool warm = false) {
+                           uint64_t cap, bool warm = false, KnnTune tune = KnnTune()) {
     if (m.n == 0) return;
-    constexpr int kCollectMax = 128;
+    const int collect_max = tune.collect_max;
     uint32_t *st_node = ws.st_node;
     float *st_d2 = ws.st_d2;
     const uint32_t first_leaf = 1u << m.depth;
+    const int chunks = 1 << m.leaf_shift;
     bool collect = !warm;
     int count = 0;
     int top = 1;
@@ -234,54 +234,57 @@ __device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, 
         if (nd2 > wd2) continue;
         const int dn = 31 - __clz(node);
         if (dn == m.depth) {
-            const uint32_t base = (node - first_leaf) * 32u;
-            const uint32_t r = base + lane;
-            uint64_t key = ~0ull;
-            if (r < m.n) {
-                float4 p = __ldg(&m.pos[r]);
-                float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                key = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
-            }
-            unsigned mask = __ballot_sync(kFull, key < kn.worst);
-            if (!mask) continue;
-            if (warm) {  // drop records the warm-start list already holds
-                bool dup = false;
-                if ((mask >> lane) & 1u) {
-                    int lo = 0, hi = 32 * S;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (ws.sk[mid] < key) lo = mid + 1; else hi = mid;
-                    }
-                    dup = lo < 32 * S && ws.sk[lo] == key;
+            // a leaf: 32 << leaf_shift records, 32 at a time
+            for (int c = 0; c < chunks; ++c) {
+                const uint32_t base = ((node - first_leaf) << (5 + m.leaf_shift)) + ((uint32_t)c << 5);
+                const uint32_t r = base + lane;
+                uint64_t key = ~0ull;
+                if (r < m.n) {
+                    float4 p = __ldg(&m.pos[r]);
+                    float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                    key = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
                 }
-                mask &= ~__ballot_sync(kFull, dup);
+                unsigned mask = __ballot_sync(kFull, key < kn.worst);
                 if (!mask) continue;
-            }
-            if (collect) {
-                const int add = __popc(mask);
-                if (count + add <= kCollectMax) {
+                if (warm) {  // drop records the warm-start list already holds
+                    bool dup = false;
                     if ((mask >> lane) & 1u) {
-                        const int at = count + __popc(mask & ((1u << lane) - 1u));
-                        ws.lk[at] = key;
-                        ws.la[at] = r;
+                        int lo = 0, hi = 32 * S;
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            if (ws.sk[mid] < key) lo = mid + 1; else hi = mid;
+                        }
+                        dup = lo < 32 * S && ws.sk[lo] == key;
                     }
-                    count += add;
-                    __syncwarp();
-                    continue;
+                    mask &= ~__ballot_sync(kFull, dup);
+                    if (!mask) continue;
                 }
-                load_sorted<S>(kn, ws, count, cap, lane);
-                collect = false;
-                mask = __ballot_sync(kFull, key < kn.worst);
-            }
-            if (__popc(mask) >= kMergeMin) {
-                kn.merge(key, r, mask, lane, ws);
-            } else {
-                while (mask) {
-                    const int src = __ffs(mask) - 1;
-                    uint64_t x = __shfl_sync(kFull, key, src);
-                    kn.insert(x, base + src, lane);
-                    mask &= mask - 1;
-                    mask &= __ballot_sync(kFull, key < kn.worst);
+                if (collect) {
+                    const int add = __popc(mask);
+                    if (count + add <= collect_max) {
+                        if ((mask >> lane) & 1u) {
+                            const int at = count + __popc(mask & ((1u << lane) - 1u));
+                            ws.lk[at] = key;
+                            ws.la[at] = r;
+                        }
+                        count += add;
+                        __syncwarp();
+                        continue;
+                    }
+                    load_sorted<S>(kn, ws, count, cap, lane);
+                    collect = false;
+                    mask = __ballot_sync(kFull, key < kn.worst);
+                }
+                if (__popc(mask) >= tune.merge_min) {
+                    kn.merge(key, r, mask, lane, ws);
+                } else {
+                    while (mask) {
+                        const int src = __ffs(mask) - 1;
+                        uint64_t x = __shfl_sync(kFull, key, src);
+                        kn.insert(x, base + src, lane);
+                        mask &= mask - 1;
+                        mask &= __ballot_sync(kFull, key < kn.worst);
+                    }
                 }
             }
         } else {
@@ -434,15 +437,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) knn_kernel(MapView m, con
     }
 }
 
+// One pixel (one warp): eye ray, specular chain, volume march with a k-NN
+// in-scattering estimate per step, k-NN estimate at the diffuse hit.
 template <int S>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, MapView surf,
-                                                                     MapView vol, RenderParams R,
-                                                                     float4 *rad, uchar4 *rgba) {
-    __shared__ WarpScratch ws[kWarpsPerBlock];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t pix = blockIdx.x * kWarpsPerBlock + wib;
-    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
-    if (pix >= npix) return;
+__device__ __forceinline__ void render_pixel(const PScene &Sc, const MapView &surf,
+                                             const MapView &vol, const RenderParams &R,
+                                             uint32_t pix, WarpScratch &wsc, int lane, float4 *rad,
+                                             uchar4 *rgba) {
     const uint32_t px = pix % (uint32_t)R.width, py = pix / (uint32_t)R.width;
     const float u = ((float)px / (float)R.width - 0.5f) * R.aspect;
     const float v = -((float)py / (float)R.height - 0.5f);
@@ -476,11 +477,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
                     const float tau_mid = tau + st * (0.5f * dt);
                     if (vol.n > 0) {
                         if (warm) {
-                            rescore<S>(vol, x, kn, ws[wib], cap, lane);
+                            rescore<S>(vol, x, kn, wsc, cap, lane);
                         } else {
                             kn.reset(cap, R.k);
                         }
-                        knn_search<S>(vol, x, kn, ws[wib], lane, cap, warm);
+                        knn_search<S>(vol, x, kn, wsc, lane, cap, warm, R.tune);
                         int found;
                         float r2;
                         v3 e = flux_sum<S>(kn, vol, lane, 1, wo, Sc.g, cap, R.r2cap, &found, &r2);
@@ -505,7 +506,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
             if (surf.n > 0) {
                 Knn<S> kn;
                 kn.reset(cap, R.k);
-                knn_search<S>(surf, hp, kn, ws[wib], lane, cap);
+                knn_search<S>(surf, hp, kn, wsc, lane, cap, false, R.tune);
                 int found;
                 float r2;
                 v3 e = flux_sum<S>(kn, surf, lane, 0, nf, 0.0f, cap, R.r2cap, &found, &r2);
@@ -551,6 +552,69 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, 
             if (nsurf) atomicAdd(&R.counters[0], (unsigned long long)nsurf);
             if (nvol) atomicAdd(&R.counters[1], (unsigned long long)nvol);
         }
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) render_kernel(PScene Sc, MapView surf,
+                                                                     MapView vol, RenderParams R,
+                                                                     float4 *rad, uchar4 *rgba) {
+    __shared__ WarpScratch ws[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t pix = blockIdx.x * kWarpsPerBlock + wib;
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
+    if (pix >= npix) return;
+    render_pixel<S>(Sc, surf, vol, R, pix, ws[wib], lane, rad, rgba);
+}
+
+// Many scenes in one persistent launch. The work is a list of chunks --
+// scene s contributes ceil(pixels_s / (4 * tile_s)) chunks of 4 warps x
+// tile_s pixels -- handed out one per block by an atomic counter, so scenes
+// of very different sizes and costs share the GPU dynamically. A block
+// keeps the current scene in shared memory and dispatches each pixel to the
+// k-list width of that scene's k, so every pixel is rendered exactly as
+// the single-scene render_kernel renders it.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
+    render_batch_kernel(const BatchRenderScene *scenes, const uint32_t *chunk_prefix, int nscenes,
+                        uint32_t *work) {
+    __shared__ WarpScratch ws[kWarpsPerBlock];
+    __shared__ BatchRenderScene cur;
+    __shared__ uint32_t s_chunk;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t total = chunk_prefix[nscenes];
+    int cur_scene = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_chunk = atomicAdd(work, 1u);
+        __syncthreads();
+        const uint32_t chunk = s_chunk;
+        if (chunk >= total) break;
+        int lo = 0, hi = nscenes;  // last scene whose first chunk <= chunk
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (chunk_prefix[mid] <= chunk) lo = mid; else hi = mid;
+        }
+        if (lo != cur_scene) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&scenes[lo]);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&cur);
+            for (int i = threadIdx.x; i < (int)(sizeof(BatchRenderScene) / 4); i += blockDim.x)
+                dst[i] = src[i];
+            __syncthreads();
+            cur_scene = lo;
+        }
+        const uint32_t npix = (uint32_t)cur.R.width * (uint32_t)cur.R.height;
+        const uint32_t tile = (uint32_t)cur.tile;
+        const uint32_t first = (chunk - chunk_prefix[lo]) * kWarpsPerBlock * tile + (uint32_t)wib * tile;
+        for (uint32_t t = 0; t < tile; ++t) {
+            const uint32_t pix = first + t;
+            if (pix >= npix) break;
+            switch (cur.slots) {
+                case 1: render_pixel<1>(cur.sc, cur.surf, cur.vol, cur.R, pix, ws[wib], lane, cur.rad, cur.rgba); break;
+                case 2: render_pixel<2>(cur.sc, cur.surf, cur.vol, cur.R, pix, ws[wib], lane, cur.rad, cur.rgba); break;
+                case 3: render_pixel<3>(cur.sc, cur.surf, cur.vol, cur.R, pix, ws[wib], lane, cur.rad, cur.rgba); break;
+                default: render_pixel<4>(cur.sc, cur.surf, cur.vol, cur.R, pix, ws[wib], lane, cur.rad, cur.rgba); break;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -609,6 +673,27 @@ cudaError_t knn_query(const MapView &m, const float4 *q, uint32_t nq, int k, flo
     }
     return cudaGetLastError();
 }
+
+cudaError_t render_batch(const BatchRenderScene *scenes, const uint32_t *chunk_prefix, int nscenes,
+                         uint32_t *work, int sm_count, cudaStream_t s) {
+    if (nscenes <= 0) return cudaSuccess;
+    static int per_sm = 0;  // resident blocks per SM (queried once, outside any capture)
+    cudaError_t e;
+    if (per_sm == 0) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel,
+                                                          kWarpsPerBlock * 32, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    e = cudaMemsetAsync(work, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    render_batch_kernel<<<sm_count * per_sm, kWarpsPerBlock * 32, 0, s>>>(scenes, chunk_prefix,
+                                                                          nscenes, work);
+    note_launch();
+    return cudaGetLastError();
+}
+
+int slots_for_k(int k) { return (k + 31) / 32; }
 
 cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vol,
                          const RenderParams &R, float4 *rad, uchar4 *rgba, cudaStream_t s) {

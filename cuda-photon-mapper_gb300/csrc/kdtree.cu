@@ -1,10 +1,10 @@
 // kdtree.cu -- photon-map kd-tree build.
 //
 // Implicit left-balanced kd-tree: node i has children 2i and 2i+1, leaves
-// hold 32 consecutive records (one warp-wide load) at depth D, and the node
-// at level l covers records [j*32*2^(D-l), (j+1)*32*2^(D-l)) of the final
-// order (j = its index within the level), so no child pointers or ranges
-// are stored.
+// hold L = 32 << leaf_shift consecutive records (one or more warp-wide
+// loads) at depth D, and the node at level l covers records
+// [j*L*2^(D-l), (j+1)*L*2^(D-l)) of the final order (j = its index within
+// the level), so no child pointers or ranges are stored.
 //
 // Top-down, one level at a time, all nodes of the level in parallel: every
 // record gets the key (node within the level, coordinate along the longest
@@ -106,18 +106,22 @@ __global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
     if (pow_in) pow_out[i] = pow_in[s];
 }
 
-// One warp per leaf slot: box of its (up to) 32 records.
+// One warp per leaf slot: box of its (up to) 32 << leaf_shift records.
 __global__ void leaf_box_kernel(const float4 *__restrict__ pos, uint32_t n, uint32_t first_leaf,
-                                uint32_t leaf_slots, float4 *node_lo, float4 *node_hi) {
+                                uint32_t leaf_slots, int leaf_shift, float4 *node_lo,
+                                float4 *node_hi) {
     uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= leaf_slots) return;
-    uint32_t r = warp * 32u + lane;
     const float inf = __int_as_float(0x7f800000);
     float lx = inf, ly = inf, lz = inf, hx = -inf, hy = -inf, hz = -inf;
-    if (r < n) {
-        float4 p = pos[r];
-        lx = hx = p.x; ly = hy = p.y; lz = hz = p.z;
+    for (int c = 0; c < (1 << leaf_shift); ++c) {
+        const uint32_t r = (warp << (5 + leaf_shift)) + ((uint32_t)c << 5) + lane;
+        if (r < n) {
+            float4 p = pos[r];
+            lx = fminf(lx, p.x); ly = fminf(ly, p.y); lz = fminf(lz, p.z);
+            hx = fmaxf(hx, p.x); hy = fmaxf(hy, p.y); hz = fmaxf(hz, p.z);
+        }
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
@@ -161,19 +165,20 @@ __global__ void top_box_kernel(uint32_t levels, float4 *node_lo, float4 *node_hi
 
 }  // namespace
 
-int tree_depth(uint32_t n) {
-    uint32_t leaves = (n + 31) / 32;
+int tree_depth(uint32_t n, int leaf_shift) {
+    const uint32_t leaf = 32u << leaf_shift;
+    uint32_t leaves = (uint32_t)(((uint64_t)n + leaf - 1) / leaf);
     int d = 0;
     while ((1u << d) < leaves) ++d;
     return d;
 }
 
-size_t tree_nodes(uint32_t n) { return (size_t)2 << tree_depth(n); }
+size_t tree_nodes(uint32_t n, int leaf_shift) { return (size_t)2 << tree_depth(n, leaf_shift); }
 
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     const uint32_t n = a.n;
     if (n == 0) return cudaSuccess;
-    const int D = tree_depth(n);
+    const int D = tree_depth(n, a.leaf_shift);
     const uint32_t blocks = (n + 255) / 256;
     // Top-down median splits; the current order ping-pongs between the two
     // (keys, vals) buffer pairs of the sort.
@@ -186,7 +191,7 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         root_cell_kernel<<<1, 1, 0, s>>>(a.lo, a.hi, a.box_dev, a.node_lo, a.node_hi); note_launch();
     }
     for (int l = 0; l < D; ++l) {
-        const uint32_t span = 32u << (D - l);
+        const uint32_t span = (32u << a.leaf_shift) << (D - l);
         const uint32_t nodes = (n + span - 1) / span;
         split_key_kernel<<<blocks, 256, 0, s>>>(a.pos_in, l == 0 ? nullptr : va, n, l, span,
                                                 a.node_lo, a.node_hi, ka, va); note_launch();
@@ -206,7 +211,8 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     permute_kernel<<<blocks, 256, 0, s>>>(va, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out); note_launch();
     const uint32_t first_leaf = 1u << D;
     leaf_box_kernel<<<(first_leaf * 32 + 255) / 256, 256, 0, s>>>(a.pos_out, n, first_leaf, first_leaf,
-                                                                 a.node_lo, a.node_hi); note_launch();
+                                                                 a.leaf_shift, a.node_lo, a.node_hi);
+    note_launch();
     // Wide levels one launch each; the top 10 levels in a single CTA.
     int l = D - 1;
     for (; l >= 10; --l) {

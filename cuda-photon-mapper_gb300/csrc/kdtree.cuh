@@ -4,10 +4,11 @@
 
 namespace pm {
 
-// Depth D of the tree over n records (leaves of 32 at depth D, 2^D leaf slots).
-int tree_depth(uint32_t n);
+// Depth D of the tree over n records (leaves of 32 << leaf_shift records at
+// depth D, 2^D leaf slots).
+int tree_depth(uint32_t n, int leaf_shift = 0);
 // Node array length (index 0 unused, root at 1): 2^(D+1).
-size_t tree_nodes(uint32_t n);
+size_t tree_nodes(uint32_t n, int leaf_shift = 0);
 
 struct KdBuildArgs {
     uint32_t n;                 // records
@@ -21,6 +22,7 @@ struct KdBuildArgs {
     uint32_t *vals, *vals_tmp;       // n each
     uint32_t *hist;                  // radix_sort_hist_words(n)
     uint32_t *order_out;             // nullable: tree position -> record index
+    int leaf_shift = 0;              // leaves of 32 << leaf_shift records
 };
 
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s);

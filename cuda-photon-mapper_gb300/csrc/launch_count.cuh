@@ -12,5 +12,9 @@ inline std::atomic<unsigned long long> &launch_counter() {
 }
 
 inline void note_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
+// Kernels of a replayed CUDA graph (counted when the graph was captured).
+inline void note_launches(unsigned long long n) {
+    launch_counter().fetch_add(n, std::memory_order_relaxed);
+}
 
 }  // namespace pm

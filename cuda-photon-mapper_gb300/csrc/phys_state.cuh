@@ -20,6 +20,7 @@ struct PhysicalState {
         float4 *lo = nullptr, *hi = nullptr;
         uint32_t cap = 0, n = 0, paths = 0;
         int depth = 0;
+        int leaf_shift = 0;
         bool built = false;
     } map[2];
     uint64_t *keys = nullptr, *keys_tmp = nullptr;
@@ -44,6 +45,7 @@ inline MapView view_of(const PhysicalState::Map &m) {
     v.hi = m.hi;
     v.n = m.built ? m.n : 0;
     v.depth = m.depth;
+    v.leaf_shift = m.leaf_shift;
     return v;
 }
 

@@ -91,8 +91,10 @@ pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg)
     PM_TRY(dalloc(&st->words, 16));
     PM_TRY(cudaMemset(st->words, 0, 16 * sizeof(uint32_t)));
     const uint32_t targets[2] = {cfg->surface_photons, cfg->volume_photons};
+    const int leaf_shift = cfg->leaf_size == 128 ? 2 : (cfg->leaf_size == 64 ? 1 : 0);
     for (int m = 0; m < 2; ++m) {
         auto &mp = st->map[m];
+        mp.leaf_shift = leaf_shift;
         mp.cap = targets[m];
         PM_TRY(dalloc(&mp.pos, mp.cap));
         PM_TRY(dalloc(&mp.pow, mp.cap));
@@ -198,7 +200,7 @@ pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream) {
         st->map[m].n = ext[2 * m];
         st->map[m].paths = ext[2 * m + 1];
         st->map[m].built = false;
-        st->map[m].depth = tree_depth(ext[2 * m]);
+        st->map[m].depth = tree_depth(ext[2 * m], st->map[m].leaf_shift);
         st->stats.map_size[m] = ext[2 * m];
         st->stats.map_paths[m] = ext[2 * m + 1];
     }
@@ -237,6 +239,7 @@ pm_status pm_build(pm_ctx *ctx, cudaStream_t stream) {
         a.vals = st->vals; a.vals_tmp = st->vals_tmp;
         a.hist = st->hist;
         a.order_out = nullptr;
+        a.leaf_shift = mp.leaf_shift;
         PM_TRY(build_tree(a, stream));
         mp.built = true;
     }
@@ -358,7 +361,9 @@ pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *
     if (n > mp.cap) {
         cudaFree(mp.pos); cudaFree(mp.pow); cudaFree(mp.tpos); cudaFree(mp.tpow);
         cudaFree(mp.lo); cudaFree(mp.hi);
+        const int ls = mp.leaf_shift;
         mp = PhysicalState::Map();
+        mp.leaf_shift = ls;
         PM_TRY(dalloc(&mp.pos, n)); PM_TRY(dalloc(&mp.pow, n));
         PM_TRY(dalloc(&mp.tpos, n)); PM_TRY(dalloc(&mp.tpow, n));
         PM_TRY(dalloc(&mp.lo, tree_nodes(n))); PM_TRY(dalloc(&mp.hi, tree_nodes(n)));
@@ -382,7 +387,7 @@ pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *
     mp.n = n;
     mp.paths = 0;
     mp.built = false;
-    mp.depth = tree_depth(n);
+    mp.depth = tree_depth(n, mp.leaf_shift);
     st->stats.map_size[map] = n;
     st->stats.map_paths[map] = 0;
     st->emitted = true;

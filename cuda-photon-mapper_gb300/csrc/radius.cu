@@ -65,8 +65,10 @@ __global__ void __launch_bounds__(kWarps * 32) radius_kernel(MapView m, const fl
             __syncwarp();
             const int dn = 31 - __clz(node);
             if (dn == m.depth) {
-                const uint32_t r = (node - first_leaf) * 32u + lane;
-                if (r < m.n) {
+                for (int ch = 0; ch < (1 << m.leaf_shift); ++ch) {
+                    const uint32_t r = ((node - first_leaf) << (5 + m.leaf_shift)) +
+                                       ((uint32_t)ch << 5) + lane;
+                    if (r >= m.n) continue;
                     const float4 p = __ldg(&m.pos[r]);
                     // gatedSqDist3: x, then y, then z, each partial sum gated
                     float c = q.x - p.x;

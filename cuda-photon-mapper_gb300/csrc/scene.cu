@@ -148,6 +148,44 @@ pm_status preset(int which, uint64_t seed, pm_scene *scene, pm_config *cfg) {
     return PM_OK;
 }
 
+// Scene `index` of the batched benchmark: the preset box with 2..32 seeded
+// spheres, sigma_s uniform in [0, 0.2], a photon count log-uniform in
+// [1e5, 4e6] split evenly between the two maps (no volume map without a
+// medium), an image of 256^2, 512^2 or 1024^2 and k of 32, 64 or 128.
+pm_status batch_scene(int index, uint64_t seed, pm_scene *scene, pm_config *cfg) {
+    if (!scene || !cfg || index < 0) return PM_ERR_INVALID;
+    pm_scene s;
+    memset(&s, 0, sizeof(s));
+    pm_config c;
+    memset(&c, 0, sizeof(c));
+    base_box(s);
+    SplitMix rng{seed ^ (0xBA7C4ull * (uint64_t)(index + 1))};
+    const int spheres = 2 + (int)(rng.next() % 31u);
+    seeded_spheres(s, spheres, 0.05f, 0.3f, rng);
+    s.sigma_s = rng.range(0.0f, 0.2f);
+    s.sigma_a = 0.02f;
+    s.hg_g = 0.3f;
+    const double photons = 1e5 * std::exp(std::log(40.0) * (double)rng.uniform());
+    const uint32_t half = (uint32_t)(photons * 0.5);
+    c.seed = seed;
+    c.scene_id = (uint32_t)index;
+    c.surface_photons = half;
+    c.volume_photons = s.sigma_s > 0.0f ? half : 0u;
+    c.max_bounces = 5;
+    c.rr_survival = 0.8f;
+    const int res = 256 << (int)(rng.next() % 3u);
+    c.width = res;
+    c.height = res;
+    c.k = 32 << (int)(rng.next() % 3u);
+    c.radius = 0.05f;
+    c.march_step = 0.01f;
+    c.leaf_size = 32;
+    c.exposure = 8.0f;
+    *scene = s;
+    *cfg = c;
+    return PM_OK;
+}
+
 pm_status validate(const pm_scene &s, const pm_config &c, std::string *why) {
     auto bad = [&](const char *m) { *why = m; return PM_ERR_INVALID; };
     if (s.num_spheres < 0 || s.num_spheres > PM_MAX_SPHERES) return bad("num_spheres out of range");
@@ -170,7 +208,8 @@ pm_status validate(const pm_scene &s, const pm_config &c, std::string *why) {
     if (!(c.radius > 0.0f)) return bad("radius must be positive");
     if (c.width < 0 || c.height < 0 || (long long)c.width * c.height > (1ll << 28))
         return bad("image size out of range");
-    if (c.leaf_size != 32) return bad("leaf_size must be 32");
+    if (c.leaf_size != 32 && c.leaf_size != 64 && c.leaf_size != 128)
+        return bad("leaf_size must be 32, 64 or 128");
     if (!(c.march_step >= 0.0f)) return bad("march_step must be >= 0");
     if (c.march_step > 0.0f && c.march_step < 1e-4f) return bad("march_step below 1e-4");
     return PM_OK;
@@ -258,4 +297,8 @@ cudaError_t make_noise_grid(float *grid, int res, uint64_t seed, float lo, float
 
 extern "C" pm_status pm_preset(int which, uint64_t seed, pm_scene *scene, pm_config *cfg) {
     return pm::preset(which, seed, scene, cfg);
+}
+
+extern "C" pm_status pm_batch_scene(int index, uint64_t seed, pm_scene *scene, pm_config *cfg) {
+    return pm::batch_scene(index, seed, scene, cfg);
 }

@@ -7,6 +7,7 @@
 namespace pm {
 
 pm_status preset(int which, uint64_t seed, pm_scene *scene, pm_config *cfg);
+pm_status batch_scene(int index, uint64_t seed, pm_scene *scene, pm_config *cfg);
 pm_status validate(const pm_scene &s, const pm_config &c, std::string *why);
 PScene to_device_scene(const pm_scene &s, const float *het_dev);
 // Fills grid[res^3] (x fastest) with seeded value noise scaled to [lo, hi].

@@ -20,6 +20,8 @@
 #include "trace.cuh"
 #include "radix_sort.cuh"
 
+#include <algorithm>
+
 namespace pm {
 namespace {
 
@@ -154,7 +156,9 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const 
     return p.ev < P.max_bounces;
 }
 
-__global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) {
+// The persistent per-warp loop of one scene: keep 32 live paths, refill
+// empty lanes from the scene's path counter until no ids are left.
+__device__ __forceinline__ void trace_loop(const PScene &S, const TraceParams &P) {
     const int lane = threadIdx.x & 31;
     MapOut ms = {0u, 0u, 0.0f}, mv = {0u, 0u, 0.0f};
     uint32_t cap = P.path_cap;
@@ -211,9 +215,35 @@ __global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) {
     }
 }
 
+__global__ void __launch_bounds__(128) trace_kernel(PScene S, TraceParams P) { trace_loop(S, P); }
+
+// Many scenes in one persistent launch: every block walks the scene list
+// (starting at a different scene per block, so scenes are worked on side
+// by side), stages the scene in shared memory and traces its paths with
+// the single-scene loop until the scene's path ids run out.
+__global__ void __launch_bounds__(128) trace_batch_kernel(const PScene *scenes,
+                                                          const TraceParams *params, int n) {
+    __shared__ PScene sS;
+    __shared__ TraceParams sP;
+    for (int j = 0; j < n; ++j) {
+        const int sc = (int)((blockIdx.x + (unsigned)j) % (unsigned)n);
+        __syncthreads();
+        const uint32_t *a = reinterpret_cast<const uint32_t *>(&scenes[sc]);
+        uint32_t *b = reinterpret_cast<uint32_t *>(&sS);
+        for (int i = threadIdx.x; i < (int)(sizeof(PScene) / 4); i += blockDim.x) b[i] = a[i];
+        const uint32_t *c = reinterpret_cast<const uint32_t *>(&params[sc]);
+        uint32_t *d = reinterpret_cast<uint32_t *>(&sP);
+        for (int i = threadIdx.x; i < (int)(sizeof(TraceParams) / 4); i += blockDim.x) d[i] = c[i];
+        __syncthreads();
+        trace_loop(sS, sP);
+    }
+}
+
 // Smallest path count whose records reach the target (or all issued paths).
 __global__ void map_extent_kernel(const uint32_t *off, const uint32_t *cnt, uint32_t issued,
-                                  const uint32_t *total_p, uint32_t target, uint32_t *extent) {
+                                  const uint32_t *issued_dev, const uint32_t *total_p,
+                                  uint32_t target, uint32_t *extent) {
+    if (issued_dev) issued = min(*issued_dev, issued);
     uint32_t total = *total_p;
     if (target == 0) {
         extent[0] = 0;
@@ -247,7 +277,44 @@ cudaError_t map_extent(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint
     if (issued == 0) return cudaMemsetAsync(extent, 0, 2 * sizeof(uint32_t), s);
     cudaError_t e = exclusive_scan_u32_large(cnt, off, issued, total, scan_tmp, s);
     if (e != cudaSuccess) return e;
-    map_extent_kernel<<<1, 1, 0, s>>>(off, cnt, issued, total, target, extent); note_launch();
+    map_extent_kernel<<<1, 1, 0, s>>>(off, cnt, issued, nullptr, total, target, extent); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t map_extent_dev(uint32_t cap, const uint32_t *issued_dev, const uint32_t *cnt,
+                           uint32_t *off, uint32_t *total, uint32_t *scan_tmp, uint32_t target,
+                           uint32_t *extent, cudaStream_t s) {
+    if (cap == 0) return cudaMemsetAsync(extent, 0, 2 * sizeof(uint32_t), s);
+    cudaError_t e = exclusive_scan_u32_large(cnt, off, cap, total, scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    map_extent_kernel<<<1, 1, 0, s>>>(off, cnt, cap, issued_dev, total, target, extent); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t trace_photons_batch(const PScene *scenes, const TraceParams *params, int n,
+                                int sm_count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    trace_batch_kernel<<<sm_count * 8, 128, 0, s>>>(scenes, params, n); note_launch();
+    return cudaGetLastError();
+}
+
+namespace {
+
+__global__ void pad_map_kernel(float4 *pos, float4 *pw, const uint32_t *n_dev, uint32_t cap) {
+    const uint32_t n = *n_dev;
+    const float inf = __int_as_float(0x7f800000);
+    for (uint32_t i = n + blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
+        pos[i] = make_float4(inf, inf, inf, __uint_as_float(i));
+        pw[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+}  // namespace
+
+cudaError_t pad_map(float4 *pos, float4 *pw, const uint32_t *n_dev, uint32_t cap, cudaStream_t s) {
+    if (cap == 0) return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((cap + 255) / 256, 4096);
+    pad_map_kernel<<<blocks, 256, 0, s>>>(pos, pw, n_dev, cap); note_launch();
     return cudaGetLastError();
 }
 

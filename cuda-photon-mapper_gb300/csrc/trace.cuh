@@ -36,5 +36,18 @@ cudaError_t trace_photons(const PScene &S, const TraceParams &P, int sm_count, c
 // paths (device).
 cudaError_t map_extent(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint32_t *total,
                        uint32_t *scan_tmp, uint32_t target, uint32_t *extent, cudaStream_t s);
+// The same without a host round trip: scans all `cap` counts (zero beyond
+// the issued paths) and reads the issued count from issued_dev.
+cudaError_t map_extent_dev(uint32_t cap, const uint32_t *issued_dev, const uint32_t *cnt,
+                           uint32_t *off, uint32_t *total, uint32_t *scan_tmp, uint32_t target,
+                           uint32_t *extent, cudaStream_t s);
+// One persistent launch over the paths of n scenes (scenes and params are
+// device arrays; each scene's params carry its own counters and maps).
+cudaError_t trace_photons_batch(const PScene *scenes, const TraceParams *params, int n,
+                                int sm_count, cudaStream_t s);
+// Fills records [*n_dev, cap) of a map with records at infinity (never
+// within any radius), so a tree built over `cap` records serves a map of
+// *n_dev records.
+cudaError_t pad_map(float4 *pos, float4 *pw, const uint32_t *n_dev, uint32_t cap, cudaStream_t s);
 
 }  // namespace pm

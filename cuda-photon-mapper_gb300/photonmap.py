@@ -92,6 +92,11 @@ class CacheStats(_c.Structure):
                 ("ms_targets", _c.c_float), ("ms_train", _c.c_float), ("tc_status", _c.c_int)]
 
 
+class BatchTune(_c.Structure):
+    _fields_ = [("leaf_size", _c.c_int), ("tile", _c.c_int), ("collect_max", _c.c_int),
+                ("merge_min", _c.c_int)]
+
+
 CACHE_WEIGHTS = 4 * 64 * 64 + 64 * 16
 MAP_SURFACE = 0
 MAP_VOLUME = 1
@@ -157,6 +162,18 @@ PROTOTYPES = {
     "pm_cache_debug_step": (_i, [_vp, _vp, _vp, _vp, _c.c_uint32, _f, _vp, _vp, _vp, _vp, _vp]),
     "pm_cache_get_queries": (_i, [_vp, _vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
     "pm_cache_get_values": (_i, [_vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
+    "pm_batch_scene": (_i, [_i, _c.c_uint64, _c.POINTER(Scene), _c.POINTER(Config)]),
+    "pm_batch_create": (_i, [_vp, _i, _vp, _vp, _c.POINTER(_vp)]),
+    "pm_batch_destroy": (None, [_vp]),
+    "pm_batch_frame": (_i, [_vp, _vp]),
+    "pm_batch_capture": (_i, [_vp, _vp]),
+    "pm_batch_launch": (_i, [_vp, _vp]),
+    "pm_batch_image": (_i, [_vp, _i, _c.POINTER(_vp), _c.POINTER(_vp)]),
+    "pm_batch_read": (_i, [_vp, _i, _vp, _vp]),
+    "pm_batch_stats": (_i, [_vp, _i, _c.POINTER(FrameStats)]),
+    "pm_batch_set_tune": (_i, [_vp, _i, _c.POINTER(BatchTune)]),
+    "pm_batch_get_tune": (_i, [_vp, _i, _c.POINTER(BatchTune)]),
+    "pm_batch_autotune": (_i, [_vp, _c.c_char_p, _vp]),
     "pm_cache_save": (_i, [_vp, _c.c_char_p]),
     "pm_cache_load": (_i, [_vp, _c.c_char_p]),
 }
@@ -432,6 +449,83 @@ class Viewer:
             self.close()
         except Exception:
             pass
+
+
+def batch_scene(index, seed=0x5EED0005):
+    """Scene `index` of the batched benchmark workload (pm_batch_scene)."""
+    sc, cf = Scene(), Config()
+    s = load().pm_batch_scene(index, seed, _c.byref(sc), _c.byref(cf))
+    if s != PM_OK:
+        raise PMError("pm_batch_scene(%d): %s" % (index, load().pm_status_string(s).decode()))
+    return sc, cf
+
+
+class Batch:
+    """Many scenes per frame (pm_batch_*), owned by a Context."""
+
+    def __init__(self, ctx, scenes, cfgs):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.n = len(scenes)
+        arr_s = (Scene * self.n)(*scenes)
+        arr_c = (Config * self.n)(*cfgs)
+        self.cfgs = list(cfgs)
+        h = _vp()
+        ctx._check(self.lib.pm_batch_create(ctx.h, self.n, _c.addressof(arr_s), _c.addressof(arr_c),
+                                            _c.byref(h)), "pm_batch_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.pm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def frame(self, stream=0):
+        self.ctx._check(self.lib.pm_batch_frame(self.h, stream), "pm_batch_frame")
+
+    def capture(self, stream):
+        self.ctx._check(self.lib.pm_batch_capture(self.h, stream), "pm_batch_capture")
+
+    def launch(self, stream):
+        self.ctx._check(self.lib.pm_batch_launch(self.h, stream), "pm_batch_launch")
+
+    def image_ptrs(self, i):
+        r, g = _vp(), _vp()
+        self.ctx._check(self.lib.pm_batch_image(self.h, i, _c.byref(r), _c.byref(g)), "pm_batch_image")
+        return r.value, g.value
+
+    def read(self, i):
+        """(radiance float32 [pixels, 4], rgba uint8 [pixels, 4]) of scene i."""
+        cf = self.cfgs[i]
+        rad = np.zeros((cf.width * cf.height, 4), np.float32)
+        rgba = np.zeros((cf.width * cf.height, 4), np.uint8)
+        self.ctx._check(self.lib.pm_batch_read(self.h, i, rad.ctypes.data, rgba.ctypes.data),
+                        "pm_batch_read")
+        return rad, rgba
+
+    def stats(self, i):
+        st = FrameStats()
+        self.ctx._check(self.lib.pm_batch_stats(self.h, i, _c.byref(st)), "pm_batch_stats")
+        return st
+
+    def set_tune(self, i, leaf_size=32, tile=1, collect_max=128, merge_min=16):
+        t = BatchTune(leaf_size, tile, collect_max, merge_min)
+        self.ctx._check(self.lib.pm_batch_set_tune(self.h, i, _c.byref(t)), "pm_batch_set_tune")
+
+    def get_tune(self, i):
+        t = BatchTune()
+        self.ctx._check(self.lib.pm_batch_get_tune(self.h, i, _c.byref(t)), "pm_batch_get_tune")
+        return t
+
+    def autotune(self, json_path=None, stream=0):
+        self.ctx._check(self.lib.pm_batch_autotune(
+            self.h, json_path.encode() if json_path else None, stream), "pm_batch_autotune")
 
 
 def cache_default_config():

@@ -380,6 +380,54 @@ PM_API pm_status pm_cache_get_values(pm_ctx *ctx, float4 *val, uint32_t cap, uin
 PM_API pm_status pm_cache_save(pm_ctx *ctx, const char *path);
 PM_API pm_status pm_cache_load(pm_ctx *ctx, const char *path);
 
+/* ---- 7. batched scenes ---------------------------------------------------------
+ * No counterpart in the reference, which renders one scene. A batch holds
+ * many independent scenes (own maps, trees, images, k and resolution) and
+ * runs a frame of all of them as: one persistent trace launch over every
+ * scene's photon paths (counting pass), per-scene record extents without a
+ * host round trip, one persistent trace launch (writing pass), per-scene
+ * kd-tree builds on side streams, and one persistent render launch that
+ * hands out pixel chunks of all scenes dynamically. Because no step reads a
+ * count back to the host, the whole frame can be captured as a CUDA graph
+ * (pm_batch_capture) and replayed (pm_batch_launch). Every scene's image is
+ * bit-identical to a single-scene pm_emit + pm_build + pm_render with the
+ * same scene, config and path cap. */
+typedef struct pm_batch pm_batch;
+/* Search knobs of one scene that change speed, never results: records per
+ * kd leaf (32, 64, 128), pixels per warp per work chunk (1..64), records
+ * collected before the first k-list sort (32, 64, 128), and the leaf
+ * candidates at or above which insertion is one bulk merge (1..33). */
+typedef struct pm_batch_tune {
+    int leaf_size, tile, collect_max, merge_min;
+} pm_batch_tune;
+/* Scene `index` of the batched benchmark workload: 2..32 seeded spheres,
+ * sigma_s in [0, 0.2], photons log-uniform in [1e5, 4e6] (half per map),
+ * 256^2 / 512^2 / 1024^2 pixels, k of 32 / 64 / 128; scene_id = index. */
+PM_API pm_status pm_batch_scene(int index, uint64_t seed, pm_scene *scene, pm_config *cfg);
+/* cfg[i].max_paths = 0 caps scene i at 8 x its larger map target. */
+PM_API pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_config *cfgs,
+                                 pm_batch **out);
+PM_API void pm_batch_destroy(pm_batch *b);
+PM_API pm_status pm_batch_frame(pm_batch *b, cudaStream_t stream);
+/* Records one frame as a CUDA graph (the stream must not be capturing). */
+PM_API pm_status pm_batch_capture(pm_batch *b, cudaStream_t stream);
+/* Replays the captured frame. */
+PM_API pm_status pm_batch_launch(pm_batch *b, cudaStream_t stream);
+/* Device pointers of scene i's radiance (float4) and image (uchar4). */
+PM_API pm_status pm_batch_image(pm_batch *b, int scene, float4 **radiance, uchar4 **rgba);
+/* Host copies of scene i's radiance and image (nullable; synchronises). */
+PM_API pm_status pm_batch_read(pm_batch *b, int scene, float4 *radiance, uchar4 *rgba);
+/* Scene i's map sizes, paths and gathers of the last frame (synchronises). */
+PM_API pm_status pm_batch_stats(pm_batch *b, int scene, pm_frame_stats *out);
+PM_API pm_status pm_batch_set_tune(pm_batch *b, int scene, const pm_batch_tune *tune);
+PM_API pm_status pm_batch_get_tune(pm_batch *b, int scene, pm_batch_tune *tune);
+/* Autotuner: for each k of the batch, times the render of its largest scene
+ * over leaf size x tile, then collect_max x merge_min at the best of those,
+ * applies the fastest setting to every scene with that k and writes every
+ * trial and choice to json_path (nullable). Rebuilds the trees it changes;
+ * a captured graph is dropped (capture again). */
+PM_API pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t stream);
+
 /* Kernels this library has launched since it was loaded (all contexts). */
 PM_API unsigned long long pm_kernel_launches(void);
 

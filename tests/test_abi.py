@@ -84,3 +84,24 @@ def test_cache_default_config():
     cfg = photonmap.cache_default_config()
     assert (cfg.levels, cfg.log2_table, cfg.base_res, cfg.max_res) == (16, 19, 16, 2048)
     assert cfg.train_samples == 1 << 20 and cfg.batch % 128 == 0
+
+
+def test_batch_scene_generator_ranges():
+    spheres, sig, photons, res, ks = [], [], [], set(), set()
+    for i in range(64):
+        sc, cf = photonmap.batch_scene(i)
+        spheres.append(sc.num_spheres)
+        sig.append(sc.sigma_s)
+        photons.append(cf.surface_photons + cf.volume_photons if sc.sigma_s > 0 else 2 * cf.surface_photons)
+        res.add((cf.width, cf.height))
+        ks.add(cf.k)
+        assert cf.scene_id == i
+        assert cf.volume_photons == (cf.surface_photons if sc.sigma_s > 0 else 0)
+    assert 2 <= min(spheres) and max(spheres) <= 32 and len(set(spheres)) > 10
+    assert 0.0 <= min(sig) and max(sig) <= 0.2
+    assert 1e5 * 0.99 <= min(photons) and max(photons) <= 4e6
+    assert res == {(256, 256), (512, 512), (1024, 1024)}
+    assert ks == {32, 64, 128}
+    a, _ = photonmap.batch_scene(5)
+    b, _ = photonmap.batch_scene(5)
+    assert bytes(a) == bytes(b)

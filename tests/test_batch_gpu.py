@@ -1,0 +1,130 @@
+"""Batched scenes on the GPU through the C ABI: every scene of a batch
+renders exactly as the single-scene path renders it, the CUDA-graph replay
+equals the eager frame, the search knobs leave results unchanged, and the
+autotuner records its trials."""
+import json
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+import photonmap  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(n=6, seed=0x5EED0005):
+    scenes, cfgs = [], []
+    for i in range(n):
+        sc, cf = photonmap.batch_scene(i, seed)
+        # keep the workload's variety (spheres, medium, k, aspect of the
+        # photon split) at test sizes
+        f = 1.0 / 40.0
+        cf.surface_photons = max(int(cf.surface_photons * f), 2000)
+        cf.volume_photons = max(int(cf.volume_photons * f), 2000) if cf.volume_photons else 0
+        cf.width = cf.height = cf.width // 16
+        cf.max_paths = 8 * max(cf.surface_photons, cf.volume_photons)
+        scenes.append(sc)
+        cfgs.append(cf)
+    return scenes, cfgs
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def batch_images(b, cfgs):
+    return [b.read(i)[0] for i in range(len(cfgs))]
+
+
+@pytest.fixture
+def ctx():
+    c = photonmap.Context(0)
+    yield c
+    c.close()
+
+
+def single(ctx, sc, cf):
+    ctx.set_scene(sc, cf)
+    ctx.emit()
+    ctx.build()
+    rad = torch.zeros((cf.width * cf.height, 4), dtype=torch.float32, device="cuda")
+    ctx.render(rad.data_ptr(), None)
+    torch.cuda.synchronize()
+    return rad.cpu().numpy(), ctx.stats()
+
+
+def test_batch_scenes_equal_single_scene_renders(ctx):
+    scenes, cfgs = small_batch()
+    assert len({cf.k for cf in cfgs}) > 1
+    b = photonmap.Batch(ctx, scenes, cfgs)
+    b.frame()
+    imgs = batch_images(b, cfgs)
+    for i, (sc, cf) in enumerate(zip(scenes, cfgs)):
+        ref, st = single(ctx, sc, cf)
+        bs = b.stats(i)
+        assert list(bs.map_size) == list(st.map_size), i
+        assert list(bs.map_paths) == list(st.map_paths), i
+        assert bs.surface_gathers == st.surface_gathers and bs.volume_gathers == st.volume_gathers
+        np.testing.assert_array_equal(bits(imgs[i]), bits(ref), err_msg="scene %d" % i)
+        assert imgs[i][:, :3].max() > 0
+    b.close()
+
+
+def test_graph_replay_equals_eager_frame(ctx):
+    scenes, cfgs = small_batch(4)
+    b = photonmap.Batch(ctx, scenes, cfgs)
+    b.frame()
+    eager = batch_images(b, cfgs)
+    stream = torch.cuda.Stream()
+    b.capture(stream.cuda_stream)
+    l0 = ctx.lib.pm_kernel_launches()
+    for _ in range(2):
+        b.launch(stream.cuda_stream)
+    stream.synchronize()
+    assert ctx.lib.pm_kernel_launches() - l0 > 4 * 2
+    replay = batch_images(b, cfgs)
+    for a, r in zip(eager, replay):
+        np.testing.assert_array_equal(bits(a), bits(r))
+    b.close()
+
+
+def test_search_knobs_do_not_change_images(ctx):
+    scenes, cfgs = small_batch(4)
+    b = photonmap.Batch(ctx, scenes, cfgs)
+    b.frame()
+    ref = batch_images(b, cfgs)
+    for leaf, tile, collect, merge in [(64, 4, 32, 8), (128, 2, 64, 33), (32, 8, 128, 1)]:
+        for i in range(len(cfgs)):
+            b.set_tune(i, leaf, tile, collect, merge)
+        b.frame()
+        got = batch_images(b, cfgs)
+        for i, (a, r) in enumerate(zip(got, ref)):
+            np.testing.assert_array_equal(bits(a), bits(r), err_msg="scene %d %s" % (
+                i, (leaf, tile, collect, merge)))
+    b.close()
+
+
+def test_autotune_writes_its_trials(ctx, tmp_path):
+    scenes, cfgs = small_batch(6)
+    b = photonmap.Batch(ctx, scenes, cfgs)
+    b.frame()
+    ref = batch_images(b, cfgs)
+    path = str(tmp_path / "tune.json")
+    b.autotune(path)
+    doc = json.load(open(path))
+    ks = sorted({cf.k for cf in cfgs})
+    assert [c["k"] for c in doc["classes"]] == ks
+    for c in doc["classes"]:
+        assert len(c["trials"]) == 12 + 9
+        assert c["choice"]["ms"] == min(t["ms"] for t in c["trials"])
+        for i, cf in enumerate(cfgs):
+            if cf.k == c["k"]:
+                t = b.get_tune(i)
+                assert (t.leaf_size, t.tile, t.collect_max, t.merge_min) == (
+                    c["choice"]["leaf_size"], c["choice"]["tile"], c["choice"]["collect_max"],
+                    c["choice"]["merge_min"])
+    got = batch_images(b, cfgs)
+    for a, r in zip(got, ref):
+        np.testing.assert_array_equal(bits(a), bits(r))
+    b.close()
