@@ -9,7 +9,11 @@ estimate per step): pm_emit + pm_build + pm_render through the C ABI.
 
 Prints one JSON line. `value` is k-NN gathers (surface + volume radiance
 estimates) per second of whole-frame device time; photon throughput and the
-per-phase times are reported beside it.
+per-phase times are reported beside it. Two more workloads ride on the same
+line: `cache` (the learned radiance cache on the same scene: online frame
+and cached render against the k-NN render, with the cached image's error
+against the k-NN image) and `batch` (64 independent scenes per frame in
+persistent multi-scene launches, captured as a CUDA graph).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -55,6 +59,9 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache A/B")
     ap.add_argument("--cache-warm-frames", type=int, default=128)
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched frame")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -276,6 +283,67 @@ def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak):
     }
 
 
+def batch_frames(ctx, lib, args, device):
+    """The batched workload: `batch_scenes` independent scenes (2..32
+    spheres, sigma_s in [0, 0.2], 1e5..4e6 photons, 256^2..1024^2 pixels,
+    k of 32/64/128) per frame -- one persistent trace launch per pass over
+    all scenes, per-scene kd builds on side streams, one persistent render
+    launch -- captured as a CUDA graph and replayed. One eager frame is
+    timed beside the replays."""
+    import torch
+    import photonmap
+    pairs = [photonmap.batch_scene(i) for i in range(args.batch_scenes)]
+    scenes = [p[0] for p in pairs]
+    cfgs = [p[1] for p in pairs]
+    b = photonmap.Batch(ctx, scenes, cfgs)
+    st = torch.cuda.Stream()
+    sh = st.cuda_stream
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn()
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    with torch.cuda.stream(st):
+        b.frame(sh)  # warm-up (allocations, first-touch)
+        st.synchronize()
+        eager_ms = timed(lambda: b.frame(sh))
+        b.capture(sh)
+        b.launch(sh)
+        st.synchronize()
+        clocks = ClockSampler(device)
+        clocks.start()
+        l0 = lib.pm_kernel_launches()
+        graph_ms = [timed(lambda: b.launch(sh)) for _ in range(args.batch_steps)]
+        launches = lib.pm_kernel_launches() - l0
+        clk = clocks.stop()
+    gathers = paths = records = 0
+    for i in range(b.n):
+        s = b.stats(i)
+        gathers += s.surface_gathers + s.volume_gathers
+        paths += s.paths_traced
+        records += s.map_size[0] + s.map_size[1]
+    pixels = sum(c.width * c.height for c in cfgs)
+    b.close()
+    frame_s = statistics.mean(graph_ms) / 1e3
+    return {
+        "workload": "%d scenes per frame: 2..32 seeded spheres, sigma_s U[0, 0.2], photons "
+                    "log-U[1e5, 4e6] split between the maps, 256^2/512^2/1024^2 pixels, k in "
+                    "{32, 64, 128}, kd-tree per map, march 0.01" % args.batch_scenes,
+        "frame_ms_graph": statistics.mean(graph_ms), "frame_ms_eager": eager_ms,
+        "gathers_per_frame": gathers, "photon_paths_per_frame": paths,
+        "records_per_frame": records, "pixels_per_frame": pixels,
+        "gathers_per_s": gathers / frame_s, "photon_paths_per_s": paths / frame_s,
+        "graph_kernels_per_frame": launches // max(1, args.batch_steps),
+        "knobs": "defaults (leaf 32, tile 1, collect 128, merge 16); pm_batch_autotune picks per k",
+        "clocks": clk,
+    }
+
+
 def run_reference(args):
     world, rank, _ = dist_info()
     if rank != 0:
@@ -464,6 +532,8 @@ def run_ours(args):
     if not args.no_cache:
         line["cache"] = cache_ab(ctx, lib, stream, rad, flush, args, cfg,
                                  statistics.mean(render_ms), peaks_bf16())
+    if not args.no_batch:
+        line["batch"] = batch_frames(ctx, lib, args, local)
     if world == 1 and not args.no_cpu_baseline:
         r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
         line["cpu_baseline"] = {
