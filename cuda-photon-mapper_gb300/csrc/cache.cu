@@ -50,15 +50,13 @@ constexpr uint32_t kOffQ1 = kOffQ0 + kPair;            // dZ3 | dZ4
 constexpr uint32_t kOffGY = kOffQ1 + kPair;            // dL/dy, 128 x 16
 constexpr uint32_t kTrainSmem = kOffGY + 4096;
 constexpr uint32_t kPairSbo = 2048;                    // 8-sample groups in a pair buffer
-// Inference: weights + one 128 x 64 activation tile.
+// Inference: weights + one 128 x 64 activation tile per pipeline.
 constexpr uint32_t kOffAct = kWBytes;
-constexpr uint32_t kInferSmem = kOffAct + 16384;
 constexpr uint32_t kActSbo = 1024;
-constexpr int kInferCtasPerSm = 4;
 
 // TMEM columns of the training kernel.
 constexpr uint32_t kColDW01 = 128, kColDW23 = 256, kColDW4 = 384, kTrainCols = 512;
-constexpr uint32_t kInferCols = 64;
+constexpr uint32_t kInferCols = 64;  // per pipeline
 
 // Byte offset of feature f (a multiple of 8) of sample s in an activation
 // buffer whose 8-sample groups are sbo bytes apart.
@@ -86,20 +84,30 @@ __device__ __forceinline__ void ld8(const unsigned char *base, uint32_t off, flo
     }
 }
 
-// fp32 [in][out] weights -> bf16 B operands: element (out, in) of layer l at
-// l * 8192 + core_offset(out, in, 64); the output layer (16 x 64) at 32768.
-__device__ void load_weights(unsigned char *sw, const float *w) {
-    for (int i = threadIdx.x; i < kCacheWeights; i += blockDim.x) {
-        uint32_t off;
-        if (i < 4 * 4096) {
-            const int l = i >> 12, r = i & 4095;
-            off = (uint32_t)l * 8192u + core_offset(r & 63, r >> 6, 64);
-        } else {
-            const int r = i - 4 * 4096;
-            off = 32768u + core_offset(r & 15, r >> 4, 64);
-        }
-        *reinterpret_cast<__nv_bfloat16 *>(sw + off) = __float2bfloat16(w[i]);
+// Byte offset of fp32 weight i ([in][out] layers) in the bf16 B-operand
+// image: element (out, in) of layer l at l * 8192 + core_offset(out, in,
+// 64); the output layer (16 x 64) at 32768.
+__device__ __forceinline__ uint32_t weight_image_offset(int i) {
+    if (i < 4 * 4096) {
+        const int l = i >> 12, r = i & 4095;
+        return (uint32_t)l * 8192u + core_offset(r & 63, r >> 6, 64);
     }
+    const int r = i - 4 * 4096;
+    return 32768u + core_offset(r & 15, r >> 4, 64);
+}
+
+static_assert(kWBytes == kCacheWImageBytes, "weight image size");
+
+// The CTA's copy of the weight image: one bulk copy (TMA) issued by thread
+// 0 on `mbar` (phase 0), which every thread then waits for. False when the
+// bounded wait ran out.
+__device__ bool load_weight_image(unsigned char *sw, const uint4 *img, uint64_t *mbar) {
+    if (threadIdx.x == 0) {
+        mbar_init(mbar);
+        bulk_load(sw, img, kWBytes, mbar);
+    }
+    __syncthreads();
+    return mbar_wait(mbar, 0);
 }
 
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
@@ -243,6 +251,24 @@ __device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, F issu
     return ok;
 }
 
+// The same for one 128-thread pipeline of a larger CTA: named barrier `bar`
+// instead of the CTA barrier; `issuer` is the pipeline's first thread.
+template <class F>
+__device__ __forceinline__ bool tc_round_group(uint64_t *mbar, uint32_t &phase, uint32_t bar,
+                                               bool issuer, F issue) {
+    publish_smem();
+    named_sync(bar, kThreads);
+    after_sync();
+    if (issuer) {
+        issue();
+        mma_commit(mbar);
+    }
+    const bool ok = mbar_wait(mbar, phase);
+    phase ^= 1u;
+    after_sync();
+    return ok;
+}
+
 // K-major operand descriptor sequence helper: nk MMAs of K = 16.
 __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t a_step, uint32_t a_lbo,
                                           uint32_t a_sbo, uint32_t b, uint32_t b_step,
@@ -288,14 +314,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                  const uint32_t *sel, const float4 *val, uint32_t n, float inv_scale,
                  float loss_norm, float rel_eps, float *x_out, float *y_out) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar, wbar;
     __shared__ uint32_t taddr_s;
     __shared__ int abort_s;
     __shared__ float red[kThreads / 32];
     const int s = threadIdx.x, warp = s >> 5;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
 
-    load_weights(sm, p.w);
+    bool ok = load_weight_image(sm, p.w_img, &wbar);
     for (uint32_t i = s; i < kPair / 16; i += kThreads)  // the unused half of P2 stays finite
         reinterpret_cast<uint4 *>(sm + kOffP2)[i] = make_uint4(0, 0, 0, 0);
     if (s == 0) {
@@ -313,10 +339,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t aW = base, aGY = base + kOffGY;
     uint32_t phase = 0;
     float lsum = 0.0f;
-    bool first = true, ok = true;
+    bool first = true;
+    if (!ok) abort_s = 1;
+    __syncthreads();
+    if (abort_s) ok = false;
     const size_t T = (size_t)1 << g.log2_t;
 
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const uint32_t i = tile * kThreads + s;
         const bool valid = i < n;
         const uint32_t qi = valid ? (sel ? sel[i] : i) : 0u;
@@ -451,30 +480,41 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) tmem_free(taddr, kTrainCols);
 }
 
-__global__ void __launch_bounds__(kThreads)
+// Inference: kInferPipes independent 128-query pipelines per CTA share one
+// copy of the weights; each has its own activation tile, TMEM columns,
+// mbarrier and named barrier, so while one pipeline waits on the tensor core
+// or on hash-table reads the others issue.
+constexpr int kInferPipes = 4;
+constexpr uint32_t kInferSmem = kOffAct + 16384u * kInferPipes;
+
+__global__ void __launch_bounds__(kThreads * kInferPipes)
     infer_kernel(CacheGrid g, CacheParams p, PScene Sc, const float4 *qa, const float4 *qd,
                  uint32_t n, float out_scale, float4 *val) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[kInferPipes], wbar;
     __shared__ uint32_t taddr_s;
-    __shared__ int abort_s;
-    const int s = threadIdx.x, warp = s >> 5;
+    __shared__ int abort_s[kInferPipes];
+    const int pipe = threadIdx.x / kThreads, s = threadIdx.x % kThreads;
+    const int warp = threadIdx.x >> 5;
+    const uint32_t bar = 1u + (uint32_t)pipe;
+    const bool issuer = s == 0;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
-    load_weights(sm, p.w);
-    if (s == 0) {
-        mbar_init(&mbar);
-        abort_s = 0;
+    const bool wok = load_weight_image(sm, p.w_img, &wbar);
+    if (issuer) {
+        mbar_init(&mbar[pipe]);
+        abort_s[pipe] = wok ? 0 : 1;
     }
-    if (warp == 0) tmem_alloc(&taddr_s, kInferCols);
+    if (warp == 0) tmem_alloc(&taddr_s, kInferCols * kInferPipes);
     publish_smem();
     __syncthreads();
     after_sync();
-    const uint32_t taddr = taddr_s;
-    const uint32_t aW = smem_addr(sm), aA = aW + kOffAct;
-    unsigned char *act = sm + kOffAct;
+    const uint32_t taddr = taddr_s + (uint32_t)pipe * kInferCols;
+    const uint32_t aW = smem_addr(sm), aA = aW + kOffAct + (uint32_t)pipe * 16384u;
+    unsigned char *act = sm + kOffAct + pipe * 16384;
     uint32_t phase = 0;
-    bool ok = true;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    bool ok = abort_s[pipe] == 0;
+    for (uint32_t tile = blockIdx.x * kInferPipes + pipe; tile < ntiles && ok;
+         tile += gridDim.x * kInferPipes) {
         const uint32_t i = tile * kThreads + s;
         const bool valid = i < n;
         float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
@@ -484,13 +524,13 @@ __global__ void __launch_bounds__(kThreads)
         }
         encode_row(act, kActSbo, s, g, p.table_h, Sc, a, d, valid, nullptr);
         for (int l = 0; l < 4; ++l) {
-            ok &= tc_round(&mbar, phase, [&] {
+            ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, [&] {
                 mma_chain(taddr, aA, 256, 128, kActSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
                           idesc_bf16(128, 64), false);
             });
             relu_out(taddr, act, kActSbo, s);
         }
-        ok &= tc_round(&mbar, phase, [&] {
+        ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, [&] {
             mma_chain(taddr, aA, 256, 128, kActSbo, aW + 32768u, 256, 128, 1024, 4,
                       idesc_bf16(128, 16), false);
         });
@@ -499,25 +539,27 @@ __global__ void __launch_bounds__(kThreads)
         if (valid && ok)
             val[i] = make_float4(fmaxf(y[0], 0.0f) * out_scale, fmaxf(y[1], 0.0f) * out_scale,
                                  fmaxf(y[2], 0.0f) * out_scale, 0.0f);
-        if (!ok) abort_s = 1;
+        if (!ok) abort_s[pipe] = 1;
         asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        if (abort_s) {
+        named_sync(bar, kThreads);
+        if (abort_s[pipe]) {
             ok = false;
             break;
         }
     }
-    if (!ok && s == 0) atomicExch(p.status, 1);
+    if (!ok && issuer) atomicExch(p.status, 1);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) tmem_free(taddr, kInferCols);
+    if (warp == 0) tmem_free(taddr_s, kInferCols * kInferPipes);
 }
 
 __global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph, uint32_t npairs,
-                            float lr, float b1, float b2, float eps, float c1, float c2) {
+                            float lr, float b1, float b2, float eps, float c1, float c2, bool lazy,
+                            uint4 *w_img) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
-        float2 pp = reinterpret_cast<float2 *>(p)[i];
         const float2 gg = reinterpret_cast<float2 *>(gr)[i];
+        if (lazy && gg.x == 0.0f && gg.y == 0.0f) continue;
+        float2 pp = reinterpret_cast<float2 *>(p)[i];
         float2 mm = reinterpret_cast<float2 *>(m)[i];
         float2 vv = reinterpret_cast<float2 *>(v)[i];
         mm.x = b1 * mm.x + (1.0f - b1) * gg.x;
@@ -531,7 +573,19 @@ __global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph
         reinterpret_cast<float2 *>(v)[i] = vv;
         reinterpret_cast<float2 *>(gr)[i] = make_float2(0.0f, 0.0f);
         if (ph) ph[i] = __floats2half2_rn(pp.x, pp.y);
+        if (w_img) {
+            unsigned char *img = reinterpret_cast<unsigned char *>(w_img);
+            *reinterpret_cast<__nv_bfloat16 *>(img + weight_image_offset(2 * i)) = __float2bfloat16(pp.x);
+            *reinterpret_cast<__nv_bfloat16 *>(img + weight_image_offset(2 * i + 1)) = __float2bfloat16(pp.y);
+        }
     }
+}
+
+__global__ void weight_image_kernel(const float *w, uint4 *w_img) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kCacheWeights) return;
+    *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(w_img) + weight_image_offset(i)) =
+        __float2bfloat16(w[i]);
 }
 
 __global__ void init_kernel(float *p, float *gr, float *m, float *v, __half2 *ph, uint32_t npairs,
@@ -635,6 +689,11 @@ __global__ void select_kernel(uint64_t seed, uint32_t frame, uint32_t total, con
         sel[i] = (uint32_t)(((uint64_t)r.v[0] * total) >> 32);
 }
 
+__global__ void iota_kernel(uint32_t *v, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = i;
+}
+
 __global__ void value_sum_kernel(const float4 *val, uint32_t n, float *sum) {
     float acc = 0.0f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -685,6 +744,13 @@ cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const ui
     return cudaGetLastError();
 }
 
+cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    iota_kernel<<<(n + 255) / 256, 256, 0, s>>>(v, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 1024);
@@ -703,7 +769,7 @@ cudaError_t cache_init(const CacheGrid &g, const CacheParams &p, uint64_t seed, 
                                                                 kCacheWeights / 2, seed, 0x3E16u,
                                                                 4 * 4096 / 2, a, a);
     note_launch();
-    return cudaGetLastError();
+    return cache_weight_image(p, s);
 }
 
 cudaError_t cache_sync_half(const CacheGrid &g, const CacheParams &p, cudaStream_t s) {
@@ -739,11 +805,18 @@ cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float
     const float c2 = 1.0f / (1.0f - powf(beta2, (float)step));
     const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));
     adam_kernel<<<2048, 256, 0, s>>>(p.table, reinterpret_cast<float *>(p.table_grad), p.table_m,
-                                     p.table_v, p.table_h, tpairs, lr, beta1, beta2, eps, c1, c2);
+                                     p.table_v, p.table_h, tpairs, lr, beta1, beta2, eps, c1, c2, true,
+                                     nullptr);
     note_launch();
     adam_kernel<<<(kCacheWeights / 2 + 255) / 256, 256, 0, s>>>(p.w, p.w_grad, p.w_m, p.w_v, nullptr,
                                                                 kCacheWeights / 2, lr, beta1, beta2,
-                                                                eps, c1, c2);
+                                                                eps, c1, c2, false, p.w_img);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s) {
+    weight_image_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w, p.w_img);
     note_launch();
     return cudaGetLastError();
 }
@@ -754,14 +827,20 @@ cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &
     if (n == 0) return cudaSuccess;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kInferSmem);
-        if (e != cudaSuccess) return e;
+        cudaError_t ea = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)kInferSmem);
+        if (ea != cudaSuccess) return ea;
         attr = true;
     }
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
-    const uint32_t grid = std::min<uint32_t>(ntiles, (uint32_t)sm_count * kInferCtasPerSm);
-    infer_kernel<<<grid, kThreads, kInferSmem, s>>>(g, p, S, qa, qd, n, out_scale, val);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel,
+                                                                  kThreads * kInferPipes, kInferSmem);
+    if (e != cudaSuccess) return e;
+    per_sm = std::max(per_sm, 1);
+    const uint32_t ctas = (ntiles + kInferPipes - 1) / kInferPipes;
+    const uint32_t grid = std::min<uint32_t>(ctas, (uint32_t)sm_count * (uint32_t)per_sm);
+    infer_kernel<<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, n, out_scale, val);
     note_launch();
     return cudaGetLastError();
 }

@@ -27,6 +27,7 @@ constexpr int kCacheTile = 128;     // samples per tensor-core tile (one per TME
 // fp32 MLP parameters, each layer [in][out] row-major: four 64 x 64 hidden
 // layers, then 64 x 16.
 constexpr int kCacheWeights = kCacheLayers * kCacheIn * kCacheHidden + kCacheHidden * kCacheOut;
+constexpr uint32_t kCacheWImageBytes = 4 * 8192 + 2048;
 
 struct CacheGrid {
     int levels;              // <= kCacheMaxLevels
@@ -42,6 +43,7 @@ struct CacheParams {
     float2 *table_grad;
     float *table_m, *table_v;
     __half2 *table_h;      // fp16 copy read by the forward passes
+    uint4 *w_img;          // bf16 weights in the kernels' shared-memory layout (kCacheWImageBytes)
     float *loss;           // device scalar, summed over a step
     int *status;           // set when a bounded tensor-core wait runs out
 };
@@ -58,12 +60,16 @@ cudaError_t cache_write_queries(const PScene &S, const RenderParams &R, bool vol
 cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *qa,
                             const float4 *qd, const float4 *val, uint32_t npix, float exposure,
                             float4 *rad, uchar4 *rgba, cudaStream_t s);
-// k-NN estimate of query sel[i] (or i when sel is null) into val[i]:
-// diffuse queries e / (pi r^2) / pi from the surface map, volume queries
-// e / (4/3 pi r^3) with the phase function toward wo from the volume map.
+// k-NN estimate of query sel[i] (or i when sel is null) into
+// val[out_index[i]] (or val[i]): diffuse queries e / (pi r^2) / pi from the
+// surface map, volume queries e / (4/3 pi r^3) with the phase function
+// toward wo from the volume map.
 cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView &vol,
-                             const float4 *qa, const float4 *qd, const uint32_t *sel, uint32_t n,
-                             int k, float radius, float4 *val, cudaStream_t s);
+                             const float4 *qa, const float4 *qd, const uint32_t *sel,
+                             const uint32_t *out_index, uint32_t n, int k, float radius,
+                             float4 *val, cudaStream_t s);
+// v[i] = i for i < n.
+cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s);
 // Training picks from Philox(seed, frame, i): with probability surf_frac
 // uniform over the diffuse queries slist[0..ns_total), else uniform over
 // all `total` queries.
@@ -85,7 +91,12 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
                            const float4 *qa, const float4 *qd, const uint32_t *sel,
                            const float4 *val, uint32_t n, float inv_scale, float loss_norm,
                            float rel_eps, float *x_out, float *y_out, int sm_count, cudaStream_t s);
-// One Adam step over all parameters; gradients are zeroed after use.
+// Writes p.w_img from the fp32 weights.
+cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s);
+// One Adam step over all parameters; gradients are zeroed after use. The
+// table takes lazy steps: entries without a gradient this step keep their
+// value and moments (sparse updates of a hash table); the weights take full
+// steps and refresh p.w_img.
 cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float beta1,
                        float beta2, float eps, int step, cudaStream_t s);
 // val[i] = max(network(query i), 0) * out_scale for the first n queries.

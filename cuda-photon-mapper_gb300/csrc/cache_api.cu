@@ -30,6 +30,10 @@ struct CacheState {
     // training
     uint32_t *sel = nullptr;
     float4 *tgt = nullptr;
+    // the frame's picks sorted by query index (coherent k-NN targets) and
+    // their positions in the random order training reads them in
+    uint32_t *skey = nullptr, *sval = nullptr, *skey_tmp = nullptr, *sval_tmp = nullptr;
+    uint32_t *shist = nullptr, *sn = nullptr;
     float *scale_sum = nullptr;
     float target_scale = 0.0f;  // 0: set from the first training frame
     unsigned long long steps = 0, frames = 0;
@@ -53,11 +57,13 @@ void free_cache(CacheState *c) {
     if (!c) return;
     cudaFree(c->p.w); cudaFree(c->p.w_grad); cudaFree(c->p.w_m); cudaFree(c->p.w_v);
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
-    cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status);
+    cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status); cudaFree(c->p.w_img);
     cudaFree(c->cnt); cudaFree(c->off); cudaFree(c->scan_tmp);
     cudaFree(c->scnt); cudaFree(c->soff); cudaFree(c->slist);
     cudaFree(c->qa); cudaFree(c->qd); cudaFree(c->val);
     cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum);
+    cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
+    cudaFree(c->shist); cudaFree(c->sn);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->tev0) cudaEventDestroy(c->tev0);
@@ -163,12 +169,12 @@ void pm_cache_default_config(pm_cache_config *cfg) {
     cfg->max_res = 2048;
     cfg->train_samples = 1u << 20;
     cfg->batch = 1u << 14;
-    cfg->lr = 1e-2f;
+    cfg->lr = 2e-2f;
     cfg->beta1 = 0.9f;
     cfg->beta2 = 0.99f;
     cfg->eps = 1e-15f;
     cfg->lr_min = 1e-3f;
-    cfg->lr_half_life = 1000.0f;
+    cfg->lr_half_life = 1500.0f;
     cfg->loss_eps = 1.0f;
     cfg->surface_fraction = 0.5f;
     cfg->seed = 0x5EED0004ull;
@@ -215,11 +221,19 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     PM_TRY_FREE(dalloc(&p.table_m, c->table_floats));
     PM_TRY_FREE(dalloc(&p.table_v, c->table_floats));
     PM_TRY_FREE(dalloc(&p.table_h, c->table_floats / 2));
+    PM_TRY_FREE(dalloc(&p.w_img, kCacheWImageBytes / 16));
     PM_TRY_FREE(dalloc(&p.loss, 1));
     PM_TRY_FREE(dalloc(&p.status, 1));
     PM_TRY_FREE(cudaMemset(p.status, 0, sizeof(int)));
     PM_TRY_FREE(dalloc(&c->sel, cfg.train_samples));
     PM_TRY_FREE(dalloc(&c->tgt, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->skey, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->sval, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->skey_tmp, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->sval_tmp, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->shist, radix_sort_hist_words(cfg.train_samples)));
+    PM_TRY_FREE(dalloc(&c->sn, 1));
+    PM_TRY_FREE(cudaMemcpy(c->sn, &cfg.train_samples, sizeof(uint32_t), cudaMemcpyHostToDevice));
     PM_TRY_FREE(dalloc(&c->scale_sum, 1));
     for (auto &ev : c->ev) PM_TRY_FREE(cudaEventCreate(&ev));
     PM_TRY_FREE(cudaEventCreate(&c->tev0));
@@ -255,7 +269,16 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
         PM_TRY(cudaEventRecord(c->tev0, stream));
         PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, c->nq, c->slist, c->nsurf, ns,
                             c->cfg.surface_fraction, c->sel, stream));
-        PM_TRY(cache_knn_values(st->dscene, surf, vol, c->qa, c->qd, c->sel, ns, st->cfg.k,
+        // targets in query order (neighbouring warps walk the same part of
+        // the tree), written back to the random order the steps read
+        PM_TRY(cudaMemcpyAsync(c->skey, c->sel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToDevice, stream));
+        PM_TRY(cache_iota(c->sval, ns, stream));
+        int bits = 1;
+        while (bits < 32 && (c->nq >> bits) != 0u) ++bits;
+        uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
+        PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, bits,
+                                    c->shist, stream, &ok_keys, &ok_vals));
+        PM_TRY(cache_knn_values(st->dscene, surf, vol, c->qa, c->qd, ok_keys, ok_vals, ns, st->cfg.k,
                                 st->cfg.radius, c->tgt, stream));
         PM_TRY(cudaEventRecord(c->ev[5], stream));
         if (!(c->target_scale > 0.0f)) {
@@ -316,7 +339,7 @@ pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int sour
                            stream));
     } else {
         PM_TRY(cache_knn_values(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->qa, c->qd,
-                                nullptr, c->nq, st->cfg.k, st->cfg.radius, c->val, stream));
+                                nullptr, nullptr, c->nq, st->cfg.k, st->cfg.radius, c->val, stream));
     }
     PM_TRY(cudaEventRecord(c->ev[3], stream));
     PM_TRY(cache_composite(st->dscene, c->off, c->qa, c->qd, c->val, npix, st->cfg.exposure,
@@ -379,6 +402,7 @@ pm_status pm_cache_set_params(pm_ctx *ctx, const float *weights, const float *ta
         PM_TRY(cudaMemcpy(c->p.w, weights, sizeof(float) * kCacheWeights, cudaMemcpyHostToDevice));
         PM_TRY(cudaMemset(c->p.w_m, 0, sizeof(float) * kCacheWeights));
         PM_TRY(cudaMemset(c->p.w_v, 0, sizeof(float) * kCacheWeights));
+        PM_TRY(cache_weight_image(c->p, 0));
     }
     if (table) {
         PM_TRY(cudaMemcpy(c->p.table, table, sizeof(float) * c->table_floats, cudaMemcpyHostToDevice));
@@ -560,6 +584,7 @@ pm_status pm_cache_load(pm_ctx *ctx, const char *path) {
     PM_TRY(cudaMemset(c->p.w_grad, 0, sizeof(float) * nw));
     PM_TRY(cudaMemset(c->p.table_grad, 0, sizeof(float) * nt));
     PM_TRY(cache_sync_half(c->grid, c->p, 0));
+    PM_TRY(cache_weight_image(c->p, 0));
     PM_TRY(cudaDeviceSynchronize());
     c->target_scale = scale;
     c->steps = steps;

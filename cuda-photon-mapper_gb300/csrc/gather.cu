@@ -628,7 +628,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
 template <int S>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     query_knn_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
-                     const uint32_t *sel, uint32_t n, int k, float r2cap, float4 *out) {
+                     const uint32_t *sel, const uint32_t *out_index, uint32_t n, int k, float r2cap,
+                     float4 *out) {
     __shared__ WarpScratch ws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t qi = blockIdx.x * kWarpsPerBlock + wib;
@@ -657,7 +658,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             e = mk3(0.f, 0.f, 0.f);
         }
     }
-    if (lane == 0) out[qi] = make_float4(e.x, e.y, e.z, 0.0f);
+    if (lane == 0) out[out_index ? out_index[qi] : qi] = make_float4(e.x, e.y, e.z, 0.0f);
 }
 
 int slots_for(int k) { return (k + 31) / 32; }
@@ -714,16 +715,17 @@ cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vo
 }
 
 cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView &vol,
-                             const float4 *qa, const float4 *qd, const uint32_t *sel, uint32_t n,
-                             int k, float radius, float4 *val, cudaStream_t s) {
+                             const float4 *qa, const float4 *qd, const uint32_t *sel,
+                             const uint32_t *out_index, uint32_t n, int k, float radius, float4 *val,
+                             cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const float r2 = radius * radius;
     const dim3 grid((n + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
     switch (slots_for(k)) {
-        case 1: query_knn_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, n, k, r2, val); break;
-        case 2: query_knn_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, n, k, r2, val); break;
-        case 3: query_knn_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, n, k, r2, val); break;
-        default: query_knn_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, n, k, r2, val); break;
+        case 1: query_knn_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
+        case 2: query_knn_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
+        case 3: query_knn_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
+        default: query_knn_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
     }
     note_launch();
     return cudaGetLastError();

@@ -82,6 +82,26 @@ __device__ __forceinline__ void publish_smem() {
 }
 __device__ __forceinline__ void after_sync() { asm volatile("tcgen05.fence::after_thread_sync;"); }
 
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, completing on mbar: the calling thread
+// arms mbar with the byte count, the copy engine completes the phase.
+__device__ __forceinline__ void bulk_load(void *dst_smem, const void *src_gmem, uint32_t bytes,
+                                          uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst_smem)),
+        "l"(src_gmem), "r"(bytes), "r"(smem_addr(mbar))
+        : "memory");
+}
+
+// Barrier over the `count` threads of named barrier `id` (1..15).
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 // One tcgen05.mma of kind::f16 (K = 16): D (TMEM) = A * B^T, or D += A * B^T
 // when accumulate is set.
 __device__ __forceinline__ void mma_bf16(uint32_t taddr, uint64_t adesc, uint64_t bdesc,
@@ -117,9 +137,11 @@ __device__ __forceinline__ void mma_issue(uint32_t taddr, uint32_t a, uint32_t b
         smem_addr(mbar)));
 }
 
-// This thread's accumulator row (TMEM lane = threadIdx.x), 16 columns from col.
+// This thread's accumulator row, 16 columns from col. A warp reaches the
+// TMEM lanes of its quarter of the SM sub-partitions: lanes 32 * (warp % 4)
+// onward, so thread t of a 128-thread group reads row t % 128.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, int col, float *v) {
-    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t warp = (threadIdx.x >> 5) & 3u;
     const uint32_t a = taddr + ((warp * 32u) << 16) + (uint32_t)col;
     uint32_t r[16];
     asm volatile(

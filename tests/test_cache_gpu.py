@@ -168,18 +168,18 @@ def test_cache_file_round_trip(ctx, tmp_path):
 
 def test_cached_render_against_float64_at_bench_scale(ctx):
     """The A/B of the benchmark scene (preset 2: 1M + 1M photons, 1024^2,
-    k = 100): the cached render after 128 online training frames and the
+    k = 100): the cached render after 192 online training frames and the
     k-NN render, both against the FP64 oracle render on 8192 random pixels.
     The target: the cached render within 1e-2 relative RMSE of the FP64
     render (the k-NN render's own error is ~0.3 %). Training adds gradients
     with float atomics, so the cached image varies slightly from run to run
-    (0.87-1.0 % from the k-NN image in recorded runs)."""
+    (0.7-1.0 % from the k-NN image in recorded runs)."""
     import oracle
     sc, cf = photonmap.preset(2, 0x5EED0002)
     frame(ctx, sc, cf)
     knn = render(ctx, cf)
     ctx.cache_enable()
-    ctx.cache_train(128)
+    ctx.cache_train(192)
     cached = render(ctx, cf, cached=0)
     assert ctx.cache_stats().tc_status == 0
     rng = np.random.default_rng(2024)
