@@ -447,7 +447,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
         }
     }
-    // weight gradients of this CTA -> global
+    // weight gradients of this CTA -> its row of partial sums (every CTA
+    // has at least one tile: the grid is at most the tile count)
+    float *part = p.w_part + (size_t)blockIdx.x * kCacheWeights;
     if (!first && ok) {
         const int half = warp >> 1;
         const int in = s & 63;
@@ -460,16 +462,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                 float v[16];
                 tmem_ld16(taddr, (int)col + c, v);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) atomicAdd(&p.w_grad[l * 4096 + in * 64 + c + j], v[j]);
+                float4 *dst = reinterpret_cast<float4 *>(part + l * 4096 + in * 64 + c);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
             }
         }
         if (warp < 2) {
             float v[16];
             tmem_ld16(taddr, (int)kColDW4, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) atomicAdd(&p.w_grad[4 * 4096 + s * 16 + j], v[j]);
+            float4 *dst = reinterpret_cast<float4 *>(part + 4 * 4096 + s * 16);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         }
     }
+    if (first || !ok)  // no valid gradient: the row must not carry stale sums
+        for (int i = s; i < kCacheWeights; i += kThreads) part[i] = 0.0f;
     if (!ok && s == 0) atomicExch(p.status, 1);
 #pragma unroll
     for (int off = 16; off; off >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
@@ -579,6 +589,15 @@ __global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph
             *reinterpret_cast<__nv_bfloat16 *>(img + weight_image_offset(2 * i + 1)) = __float2bfloat16(pp.y);
         }
     }
+}
+
+// w_grad[i] += sum over the CTAs' partial rows (fixed order: deterministic).
+__global__ void wgrad_reduce_kernel(const float *part, int parts, float *w_grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kCacheWeights) return;
+    float acc = 0.0f;
+    for (int b = 0; b < parts; ++b) acc += part[(size_t)b * kCacheWeights + i];
+    w_grad[i] += acc;
 }
 
 __global__ void weight_image_kernel(const float *w, uint4 *w_img) {
@@ -792,9 +811,12 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
         attr = true;
     }
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
-    const uint32_t grid = std::min<uint32_t>(ntiles, (uint32_t)sm_count);
+    const uint32_t grid = std::min<uint32_t>(
+        ntiles, (uint32_t)std::min(sm_count, p.parts_cap));
     train_kernel<<<grid, kThreads, kTrainSmem, s>>>(g, p, S, qa, qd, sel, val, n, inv_scale, loss_norm,
                                                     rel_eps, x_out, y_out);
+    note_launch();
+    wgrad_reduce_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w_part, (int)grid, p.w_grad);
     note_launch();
     return cudaGetLastError();
 }

@@ -39,6 +39,8 @@ struct CacheGrid {
 struct CacheParams {
     float *w;              // fp32 master weights (kCacheWeights)
     float *w_grad, *w_m, *w_v;
+    float *w_part;         // per-CTA weight-gradient rows of one backward pass (parts_cap rows)
+    int parts_cap;
     float *table;          // fp32 master table, levels * 2^log2_t * 2
     float2 *table_grad;
     float *table_m, *table_v;

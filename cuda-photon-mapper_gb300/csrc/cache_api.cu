@@ -56,6 +56,7 @@ cudaError_t dalloc(T **p, size_t count) {
 void free_cache(CacheState *c) {
     if (!c) return;
     cudaFree(c->p.w); cudaFree(c->p.w_grad); cudaFree(c->p.w_m); cudaFree(c->p.w_v);
+    cudaFree(c->p.w_part);
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
     cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status); cudaFree(c->p.w_img);
     cudaFree(c->cnt); cudaFree(c->off); cudaFree(c->scan_tmp);
@@ -214,6 +215,8 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     CacheParams &p = c->p;
     PM_TRY_FREE(dalloc(&p.w, kCacheWeights));
     PM_TRY_FREE(dalloc(&p.w_grad, kCacheWeights));
+    p.parts_cap = c->sm_count;
+    PM_TRY_FREE(dalloc(&p.w_part, (size_t)p.parts_cap * kCacheWeights));
     PM_TRY_FREE(dalloc(&p.w_m, kCacheWeights));
     PM_TRY_FREE(dalloc(&p.w_v, kCacheWeights));
     PM_TRY_FREE(dalloc(&p.table, c->table_floats));
