@@ -62,6 +62,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched frame")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--no-legacy", action="store_true", help="skip the legacy-mode frames")
     return ap.parse_args()
 
 
@@ -344,6 +345,55 @@ def batch_frames(ctx, lib, args, device):
     }
 
 
+def legacy_frames(ctx, args, with_cpu):
+    """The reference's own frame, through its drop-in exports' explicit-
+    context twins: photon emission into the 32^3 voxel grid and a 512x512
+    render, media and interpolation on (the slowest of the reference's
+    modes), bit-exact with the reference. CPU baseline: the C restatement of
+    the same frame on one host thread (the reference's code is serial)."""
+    import torch
+    import photonmap
+    flags = photonmap.PM_LEGACY_INTERPOLATE | photonmap.PM_LEGACY_MEDIA
+    img = torch.zeros((512, 512, 4), dtype=torch.uint8, device="cuda")
+    st = torch.cuda.Stream()
+    sh = st.cuda_stream
+    with torch.cuda.stream(st):
+        ctx.legacy_init_random(sh)
+        for i in range(args.warmup):
+            ctx.legacy_emit(0.01 * i, flags, sh)
+            ctx.legacy_render(img.data_ptr(), 512, 512, 0.01 * i, flags, stream=sh)
+        st.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        n = max(args.steps, 5)
+        e0.record(st)
+        for i in range(n):
+            ctx.legacy_emit(0.01 * i, flags, sh)
+            ctx.legacy_render(img.data_ptr(), 512, 512, 0.01 * i, flags, stream=sh)
+        e1.record(st)
+        e1.synchronize()
+    gpu_ms = e0.elapsed_time(e1) / n
+    out = {"workload": "reference frame: 10,000 photons into the 32^3 grid, 512x512 render with the "
+                       "media march and the bilinear blend ('p' and 'i' keys on)",
+           "frame_ms": gpu_ms, "frames": n}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        ora = oracle.LegacyOracle()
+        ora.init_random()
+        t0 = time.perf_counter()
+        cpu_n = 2
+        for i in range(cpu_n):
+            ora.emit(0.01 * i, 1, 1)
+            ora.render(512, 512, 0.01 * i, 1, 1)
+        cpu_ms = (time.perf_counter() - t0) * 1e3 / cpu_n
+        out["cpu_baseline"] = {"frame_ms": cpu_ms, "cores": 1, "kind": "port",
+                               "sample": "%d full frames of the C restatement (bit-exact with the "
+                                         "reference's serial semantics)" % cpu_n}
+        out["speedup_vs_cpu"] = cpu_ms / gpu_ms
+    return out
+
+
 def run_reference(args):
     world, rank, _ = dist_info()
     if rank != 0:
@@ -534,6 +584,8 @@ def run_ours(args):
                                  statistics.mean(render_ms), peaks_bf16())
     if not args.no_batch:
         line["batch"] = batch_frames(ctx, lib, args, local)
+    if not args.no_legacy:
+        line["legacy"] = legacy_frames(ctx, args, with_cpu=(world == 1 and not args.no_cpu_baseline))
     if world == 1 and not args.no_cpu_baseline:
         r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
         line["cpu_baseline"] = {
