@@ -803,13 +803,10 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
                            const float4 *val, uint32_t n, float inv_scale, float loss_norm,
                            float rel_eps, float *x_out, float *y_out, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kTrainSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // the opt-in is per device: set it on every call (a host-side attribute write)
+    cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kTrainSmem);
+    if (e != cudaSuccess) return e;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
     const uint32_t grid = std::min<uint32_t>(
         ntiles, (uint32_t)std::min(sm_count, p.parts_cap));
@@ -847,13 +844,9 @@ cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &
                         const float4 *qa, const float4 *qd, uint32_t n, float out_scale,
                         float4 *val, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t ea = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)kInferSmem);
-        if (ea != cudaSuccess) return ea;
-        attr = true;
-    }
+    cudaError_t ea = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kInferSmem);
+    if (ea != cudaSuccess) return ea;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel,

@@ -15,6 +15,8 @@
 // k-th candidate, so a photon at exactly that distance with a smaller index
 // is still found: the result equals a brute-force sort by (distance, index).
 #include "launch_count.cuh"
+
+#include <atomic>
 #include "cache.cuh"
 #include "eye_path.cuh"
 
@@ -682,13 +684,19 @@ cudaError_t knn_query(const MapView &m, const float4 *q, uint32_t nq, int k, flo
 cudaError_t render_batch(const BatchRenderScene *scenes, const uint32_t *chunk_prefix, int nscenes,
                          uint32_t *work, int sm_count, cudaStream_t s) {
     if (nscenes <= 0) return cudaSuccess;
-    static int per_sm = 0;  // resident blocks per SM (queried once, outside any capture)
-    cudaError_t e;
+    // resident blocks per SM, per device (kept from the first eager call so
+    // that graph capture issues no query)
+    static std::atomic<int> per_sm_of[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    int per_sm = dev < 64 ? per_sm_of[dev].load() : 0;
     if (per_sm == 0) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel,
                                                           kWarpsPerBlock * 32, 0);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
+        if (dev < 64) per_sm_of[dev].store(per_sm);
     }
     e = cudaMemsetAsync(work, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
