@@ -399,23 +399,42 @@ __global__ void __launch_bounds__(256) emit_kernel(Scene sc, const float4 *__res
     if (!offsets) counts[p] = d.n;
 }
 
+// Deposit values in sorted order (one parallel gather), so that each
+// voxel's sum below streams a contiguous range.
+__global__ void gather_deposits_kernel(const uint32_t *__restrict__ sidx,
+                                       const float4 *__restrict__ vals, const uint32_t *total,
+                                       float4 *sorted) {
+    const uint32_t n = *total;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        sorted[j] = vals[sidx[j]];
+}
+
+__device__ __forceinline__ uint32_t first_at_least(const uint32_t *__restrict__ keys, uint32_t n,
+                                                   uint32_t v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (keys[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
 // Sums each voxel's deposits in photon order and writes both grid layouts.
+// The range is known before the loop, so the loads run ahead of the
+// (necessarily serial) additions.
 __global__ void __launch_bounds__(256) reduce_kernel(const uint32_t *__restrict__ skeys,
-                                                     const uint32_t *__restrict__ sidx,
-                                                     const float4 *__restrict__ vals,
+                                                     const float4 *__restrict__ sorted,
                                                      const uint32_t *total, float *grid3,
                                                      float4 *grid4) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= kLegacyVoxels) return;
-    uint32_t n = *total;
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (skeys[mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
-    }
+    const uint32_t n = *total;
+    const uint32_t lo = first_at_least(skeys, n, (uint32_t)v);
+    const uint32_t hi = first_at_least(skeys, n, (uint32_t)v + 1u);
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    for (uint32_t j = lo; j < n && skeys[j] == (uint32_t)v; ++j) {
-        float4 e = vals[sidx[j]];
+#pragma unroll 8
+    for (uint32_t j = lo; j < hi; ++j) {
+        const float4 e = __ldg(&sorted[j]);
         ax = ax + e.x;
         ay = ay + e.y;
         az = az + e.z;
@@ -530,6 +549,7 @@ cudaError_t legacy_alloc(LegacyState &st) {
     PM_ALLOC(st.idx, sizeof(uint32_t) * kLegacyMaxDeposits);
     PM_ALLOC(st.idx_tmp, sizeof(uint32_t) * kLegacyMaxDeposits);
     PM_ALLOC(st.dep, sizeof(float4) * kLegacyMaxDeposits);
+    PM_ALLOC(st.sdep, sizeof(float4) * kLegacyMaxDeposits);
     PM_ALLOC(st.hist, sizeof(uint32_t) * radix_sort_hist_words(kLegacyMaxDeposits));
 #undef PM_ALLOC
     // A fresh module starts with a zero table and grid (static __device__
@@ -544,7 +564,7 @@ cudaError_t legacy_alloc(LegacyState &st) {
 void legacy_free(LegacyState &st) {
     cudaFree(st.table); cudaFree(st.grid3); cudaFree(st.grid4); cudaFree(st.counts);
     cudaFree(st.offsets); cudaFree(st.total); cudaFree(st.keys); cudaFree(st.keys_tmp);
-    cudaFree(st.idx); cudaFree(st.idx_tmp); cudaFree(st.dep); cudaFree(st.hist);
+    cudaFree(st.idx); cudaFree(st.idx_tmp); cudaFree(st.dep); cudaFree(st.sdep); cudaFree(st.hist);
     st = LegacyState();
 }
 
@@ -573,7 +593,8 @@ cudaError_t legacy_emit(LegacyState &st, float anim_time, int flags, cudaStream_
     e = radix_sort_pairs_u32(st.keys, st.idx, st.keys_tmp, st.idx_tmp, st.total, kLegacyMaxDeposits,
                              0, 16, st.hist, s, &sk, &si);
     if (e != cudaSuccess) return e;
-    reduce_kernel<<<(kLegacyVoxels + 255) / 256, 256, 0, s>>>(sk, si, st.dep, st.total, st.grid3,
+    gather_deposits_kernel<<<512, 256, 0, s>>>(si, st.dep, st.total, st.sdep); note_launch();
+    reduce_kernel<<<(kLegacyVoxels + 255) / 256, 256, 0, s>>>(sk, st.sdep, st.total, st.grid3,
                                                              st.grid4); note_launch();
     if (media) st.rng_draws += 9ull * kLegacyPhotons;
     return cudaGetLastError();

@@ -35,6 +35,7 @@ struct LegacyState {
     uint32_t *keys = nullptr, *keys_tmp = nullptr;
     uint32_t *idx = nullptr, *idx_tmp = nullptr;
     float4 *dep = nullptr;        // deposit values in photon order
+    float4 *sdep = nullptr;       // the same, in (voxel, photon order) order
     uint32_t *hist = nullptr;
     uint64_t rng_draws = 0;       // draws taken from the shared generator so far
     bool table_written = false;

@@ -128,3 +128,24 @@ def test_autotune_writes_its_trials(ctx, tmp_path):
     for a, r in zip(got, ref):
         np.testing.assert_array_equal(bits(a), bits(r))
     b.close()
+
+
+def test_batch_of_the_three_presets(ctx):
+    """Presets 1-3 side by side (preset 3's heterogeneous medium included):
+    each scene of the batch equals its single-scene render."""
+    scenes, cfgs = [], []
+    for i, p in enumerate((1, 2, 3)):
+        sc, cf = photonmap.preset(p, 0x5EED0001 + p)
+        cf.surface_photons = cf.volume_photons = 15000
+        cf.width, cf.height = 40, 30
+        cf.scene_id = i
+        cf.max_paths = 8 * 15000
+        scenes.append(sc)
+        cfgs.append(cf)
+    b = photonmap.Batch(ctx, scenes, cfgs)
+    b.frame()
+    imgs = batch_images(b, cfgs)
+    for i, (sc, cf) in enumerate(zip(scenes, cfgs)):
+        ref, _ = single(ctx, sc, cf)
+        np.testing.assert_array_equal(bits(imgs[i]), bits(ref), err_msg="preset %d" % (i + 1))
+    b.close()

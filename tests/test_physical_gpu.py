@@ -235,3 +235,12 @@ def test_radius_gather_matches_reference_weighting(ctx):
         scale = np.abs(ref).max()
         assert scale > 0
         np.testing.assert_allclose(got, ref, rtol=1e-4, atol=1e-6 * scale)
+
+
+@pytest.mark.parametrize("leaf", [64, 128])
+def test_leaf_size_does_not_change_the_render(ctx, leaf):
+    sc, cf = small(2, 30000, 30000, (40, 32))
+    a, _ = gpu_frame(ctx, sc, cf)
+    cf.leaf_size = leaf
+    b, _ = gpu_frame(ctx, sc, cf)
+    np.testing.assert_array_equal(bits(b), bits(a))
