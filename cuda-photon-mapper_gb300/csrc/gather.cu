@@ -459,7 +459,7 @@ __device__ __forceinline__ void render_pixel(const PScene &Sc, const MapView &su
     bool glass = false;
     uint32_t nsurf = 0, nvol = 0;
     for (int depth = 0; depth < kMaxSpecular; ++depth) {
-        PHit h = intersect(Sc, o, d, 3.0e38f);
+        PHit h = intersect_fast(Sc, o, d, 3.0e38f);
         const float tend = h.obj != kNone ? h.t : 3.0e38f;
         if (R.step > 0.0f && Sc.sigma_max > 0.0f && !glass) {
             float t0, t1;

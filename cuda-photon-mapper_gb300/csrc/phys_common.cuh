@@ -16,6 +16,7 @@
 namespace pm {
 
 constexpr float kRayEps = 1e-4f;     // minimum hit distance
+constexpr int kGridMax = 8;          // sphere grid cells per axis, at most
 constexpr float kOffset = 1e-4f;     // origin offset along the normal after an interaction
 
 // The scene as the kernels read it: passed by value as a kernel parameter
@@ -38,6 +39,12 @@ struct PScene {
     float sigma_max;                 // majorant of sigma_t
     const float *het;                // het_res^3 sigma_s values (device)
     float cam[3], focal;
+    // Uniform grid over the box for the sphere tests (grid_res = 0: none):
+    // bit i of cell_mask[(z * G + y) * G + x] is set when sphere i's
+    // bounding box, slightly enlarged, overlaps cell (x, y, z).
+    int grid_res;
+    float grid_inv[3];                   // G / box extent per axis
+    uint64_t cell_mask[kGridMax * kGridMax * kGridMax];
 };
 
 struct PHit {
@@ -48,24 +55,37 @@ constexpr int kNone = 0x7fffffff;
 
 PM_HD float vget(v3 v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
-// Nearest hit with t in (kRayEps, tmax). d must be unit length.
+// Distance to the first crossing of sphere s beyond kRayEps along (o, d),
+// or -1 when the line misses it.
+__device__ __forceinline__ float sphere_t(float4 s, v3 o, v3 d) {
+    v3 oc = mk3(o.x - s.x, o.y - s.y, o.z - s.z);
+    float b = dot(oc, d);
+    float c = dot(oc, oc) - s.w * s.w;
+    float disc = b * b - c;
+    if (!(disc > 0.0f)) return -1.0f;
+    float sq = sqrtf(disc);
+    float t = -b - sq;
+    if (!(t > kRayEps)) t = -b + sq;
+    return t;
+}
+
+__device__ __forceinline__ void plane_hits(const PScene &S, v3 o, v3 d, PHit &h);
+
+// Nearest hit with t in (kRayEps, tmax). d must be unit length. Spheres
+// are tested in index order; equal distances keep the lower index.
 __device__ __forceinline__ PHit intersect(const PScene &S, v3 o, v3 d, float tmax) {
     PHit h;
     h.t = tmax;
     h.obj = kNone;
     for (int i = 0; i < S.ns; ++i) {
-        float4 s = S.sph[i];
-        v3 oc = mk3(o.x - s.x, o.y - s.y, o.z - s.z);
-        float b = dot(oc, d);
-        float c = dot(oc, oc) - s.w * s.w;
-        float disc = b * b - c;
-        if (disc > 0.0f) {
-            float sq = sqrtf(disc);
-            float t = -b - sq;
-            if (!(t > kRayEps)) t = -b + sq;
-            if (t > kRayEps && t < h.t) { h.t = t; h.obj = i; }
-        }
+        const float t = sphere_t(S.sph[i], o, d);
+        if (t > kRayEps && t < h.t) { h.t = t; h.obj = i; }
     }
+    plane_hits(S, o, d, h);
+    return h;
+}
+
+__device__ __forceinline__ void plane_hits(const PScene &S, v3 o, v3 d, PHit &h) {
     for (int i = 0; i < S.np; ++i) {
         int a = S.pl_axis[i];
         float da = vget(d, a);
@@ -82,6 +102,74 @@ __device__ __forceinline__ PHit intersect(const PScene &S, v3 o, v3 d, float tma
             }
         }
     }
+}
+
+PM_HD void box_span(const PScene &S, v3 o, v3 d, float *t0, float *t1);
+
+// The same nearest hit as intersect(), with the spheres found through the
+// grid: cells are visited in ray order (3D-DDA from the box entry) and each
+// sphere is tested once; the walk stops when the best hit lies before the
+// current cell's exit. Sphere bounding boxes are enlarged when binned, so a
+// hit near a cell boundary is always in a visited cell. Equal distances keep
+// the lower index, as in intersect(). Falls back to intersect() without a
+// grid. For warp-uniform rays (one eye ray per warp); lanes that walk
+// different rays diverge in the cell and sphere loops.
+__device__ __forceinline__ PHit intersect_fast(const PScene &S, v3 o, v3 d, float tmax) {
+    const int G = S.grid_res;
+    if (G <= 0) return intersect(S, o, d, tmax);
+    PHit h;
+    h.t = tmax;
+    h.obj = kNone;
+    float t0, t1;
+    box_span(S, o, d, &t0, &t1);
+    t1 = fminf(t1, tmax);
+    if (t0 < t1) {
+        const v3 p = o + d * t0;
+        int c[3], step[3];
+        float tnext[3], tdelta[3];
+        const float dv[3] = {d.x, d.y, d.z}, ov[3] = {o.x, o.y, o.z}, pv[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float cs = (S.bmax[a] - S.bmin[a]) / (float)G;
+            int ci = (int)((pv[a] - S.bmin[a]) * S.grid_inv[a]);
+            ci = min(max(ci, 0), G - 1);
+            c[a] = ci;
+            if (dv[a] > 0.0f) {
+                step[a] = 1;
+                tnext[a] = (S.bmin[a] + (float)(ci + 1) * cs - ov[a]) / dv[a];
+                tdelta[a] = cs / dv[a];
+            } else if (dv[a] < 0.0f) {
+                step[a] = -1;
+                tnext[a] = (S.bmin[a] + (float)ci * cs - ov[a]) / dv[a];
+                tdelta[a] = -cs / dv[a];
+            } else {
+                step[a] = 0;
+                tnext[a] = 3.0e38f;
+                tdelta[a] = 3.0e38f;
+            }
+        }
+        uint64_t tested = 0ull;
+        for (int it = 0; it < 3 * kGridMax + 3; ++it) {
+            uint64_t mask = S.cell_mask[(c[2] * G + c[1]) * G + c[0]] & ~tested;
+            tested |= mask;
+            while (mask) {
+                const int i = __ffsll((long long)mask) - 1;
+                mask &= mask - 1ull;
+                const float t = sphere_t(S.sph[i], o, d);
+                if (t > kRayEps && (t < h.t || (t == h.t && h.obj != kNone && i < h.obj))) {
+                    h.t = t;
+                    h.obj = i;
+                }
+            }
+            const int ax = tnext[0] < tnext[1] ? (tnext[0] < tnext[2] ? 0 : 2) : (tnext[1] < tnext[2] ? 1 : 2);
+            const float texit = tnext[ax];
+            if (h.t <= texit || texit >= t1) break;
+            c[ax] += step[ax];
+            if (c[ax] < 0 || c[ax] >= G) break;
+            tnext[ax] += tdelta[ax];
+        }
+    }
+    plane_hits(S, o, d, h);
     return h;
 }
 

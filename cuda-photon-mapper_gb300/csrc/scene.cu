@@ -246,6 +246,40 @@ PScene to_device_scene(const pm_scene &s, const float *het_dev) {
     d.het = het_dev;
     d.sigma_max = (s.het_res > 0 ? s.het_max : s.sigma_s) + s.sigma_a;
     d.focal = s.focal;
+    // Sphere grid for scenes with many spheres, all inside the box (the
+    // walk only visits the box): G = ceil(1.5 * cbrt(n)) cells per axis,
+    // each sphere's bounding box enlarged by 1e-3 of a cell when binned.
+    d.grid_res = 0;
+    bool inside = s.num_spheres >= 12;
+    for (int i = 0; i < s.num_spheres && inside; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const float c = a == 0 ? s.spheres[i].x : (a == 1 ? s.spheres[i].y : s.spheres[i].z);
+            if (c - s.spheres[i].w < s.box_min[a] || c + s.spheres[i].w > s.box_max[a]) inside = false;
+        }
+    if (inside) {
+        int G = (int)std::ceil(1.5 * std::cbrt((double)s.num_spheres));
+        G = G < 2 ? 2 : (G > kGridMax ? kGridMax : G);
+        d.grid_res = G;
+        double cs[3];
+        for (int a = 0; a < 3; ++a) {
+            d.grid_inv[a] = (float)G / (s.box_max[a] - s.box_min[a]);
+            cs[a] = ((double)s.box_max[a] - s.box_min[a]) / G;
+        }
+        for (int i = 0; i < s.num_spheres; ++i) {
+            int lo[3], hi[3];
+            for (int a = 0; a < 3; ++a) {
+                const double c = a == 0 ? s.spheres[i].x : (a == 1 ? s.spheres[i].y : s.spheres[i].z);
+                const double r = s.spheres[i].w + 1e-3 * cs[a];
+                lo[a] = (int)std::floor((c - r - s.box_min[a]) / cs[a]);
+                hi[a] = (int)std::floor((c + r - s.box_min[a]) / cs[a]);
+                lo[a] = lo[a] < 0 ? 0 : (lo[a] > G - 1 ? G - 1 : lo[a]);
+                hi[a] = hi[a] < 0 ? 0 : (hi[a] > G - 1 ? G - 1 : hi[a]);
+            }
+            for (int z = lo[2]; z <= hi[2]; ++z)
+                for (int y = lo[1]; y <= hi[1]; ++y)
+                    for (int x = lo[0]; x <= hi[0]; ++x) d.cell_mask[(z * G + y) * G + x] |= 1ull << i;
+        }
+    }
     return d;
 }
 

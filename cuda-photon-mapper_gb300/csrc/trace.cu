@@ -66,6 +66,8 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const 
     p.ev += 1;
     pm_u32x4 r = philox(P.seed, p.id, (uint32_t)p.ev, 0u, P.scene_id);
     float u0 = pm_u01(r.v[0]), u1 = pm_u01(r.v[1]), u2 = pm_u01(r.v[2]), u3 = pm_u01(r.v[3]);
+    // brute force over the spheres: the lanes of a warp trace different
+    // photons, and a uniform loop beats divergent grid walks here
     PHit h = intersect(S, p.o, p.d, 3.0e38f);
     float seg = h.obj != kNone ? h.t : box_exit(S, p.o, p.d);
     bool vol = false;
