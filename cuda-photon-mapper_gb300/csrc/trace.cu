@@ -35,6 +35,7 @@ struct Path {
     int ev;
     bool glass;
     uint32_t ns, nv;
+    uint32_t os, ov;  // writing pass: the path's first record index in each map
 };
 
 __device__ __forceinline__ void start_path(const TraceParams &P, uint32_t id, Path &p, const PScene &S) {
@@ -47,6 +48,10 @@ __device__ __forceinline__ void start_path(const TraceParams &P, uint32_t id, Pa
     p.glass = false;
     p.ns = 0;
     p.nv = 0;
+    if (P.store) {  // loaded now, used at the path's first stores
+        p.os = P.off_s[id];
+        p.ov = P.off_v[id];
+    }
 }
 
 __device__ __forceinline__ void store(float4 *pos, float4 *pw, uint32_t j, v3 x, v3 thr, v3 d,
@@ -106,7 +111,7 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const 
     }
     if (vol) {
         if (P.store) {
-            uint32_t j = P.off_v[p.id] + p.nv;
+            uint32_t j = p.ov + p.nv;
             if (j < mv.n) store(P.vpos, P.vpow, j, x, p.thr, p.d, mv.scale);
         }
         p.nv += 1;
@@ -125,7 +130,7 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const 
     v3 nf = dn < 0.0f ? n : n * -1.0f;
     if (kind == PM_MAT_DIFFUSE) {
         if (P.store) {
-            uint32_t j = P.off_s[p.id] + p.ns;
+            uint32_t j = p.os + p.ns;
             if (j < ms.n) store(P.spos, P.spow, j, hp, p.thr, p.d, ms.scale);
         }
         p.ns += 1;
@@ -158,8 +163,16 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const 
     return p.ev < P.max_bounces;
 }
 
+// Path ids come in blocks of kIdBlock per atomic. A warp always holds the
+// next block's atomic in flight (issued when it takes the current one), so
+// refilling lanes rarely waits for the counter; every block a warp takes is
+// traced in full (the ids stay a gap-free prefix, which the record extents
+// need), and the counting pass stops requesting blocks once both maps are
+// full.
+constexpr uint32_t kIdBlock = 32;
+
 // The persistent per-warp loop of one scene: keep 32 live paths, refill
-// empty lanes from the scene's path counter until no ids are left.
+// empty lanes from the warp's pool of path ids until no ids are left.
 __device__ __forceinline__ void trace_loop(const PScene &S, const TraceParams &P) {
     const int lane = threadIdx.x & 31;
     MapOut ms = {0u, 0u, 0.0f}, mv = {0u, 0u, 0.0f};
@@ -173,32 +186,58 @@ __device__ __forceinline__ void trace_loop(const PScene &S, const TraceParams &P
     }
     Path p;
     bool live = false;
-    bool exhausted = false;  // no path ids left to issue (warp-uniform)
+    // warp-uniform pool [pool, pool_end); lane 0 holds the prefetched block
+    uint32_t pool = 0, pool_end = 0, pending = 0;
+    bool has_pending = cap > 0;
+    if (has_pending && lane == 0) pending = atomicAdd(P.path_counter, kIdBlock);
     for (;;) {
-        unsigned empty = __ballot_sync(0xffffffffu, !live);
-        if (empty && !exhausted) {
-            const int leader = __ffs(empty) - 1;
-            uint32_t base = cap;
-            if (lane == leader) {
-                bool full = !P.store && *((volatile uint32_t *)P.stored_s) >= P.target_s &&
-                            *((volatile uint32_t *)P.stored_v) >= P.target_v;
-                if (!full) base = atomicAdd(P.path_counter, (uint32_t)__popc(empty));
+        const unsigned empty = __ballot_sync(0xffffffffu, !live);
+        const uint32_t need = (uint32_t)__popc(empty);
+        if (need && (pool < pool_end || has_pending)) {
+            const uint32_t avail = pool_end - pool;
+            uint32_t nb = 0;
+            bool took = false;
+            if (avail < need && has_pending) {
+                nb = __shfl_sync(0xffffffffu, pending, 0);
+                has_pending = false;
+                took = true;
+                bool more = nb < cap && cap - nb > kIdBlock;
+                if (more && !P.store) {
+                    int full = 0;
+                    if (lane == 0)
+                        full = *((volatile uint32_t *)P.stored_s) >= P.target_s &&
+                               *((volatile uint32_t *)P.stored_v) >= P.target_v;
+                    more = __shfl_sync(0xffffffffu, full, 0) == 0;
+                }
+                if (more) {
+                    if (lane == 0) pending = atomicAdd(P.path_counter, kIdBlock);
+                    has_pending = true;
+                }
             }
-            base = __shfl_sync(0xffffffffu, base, leader);
-            exhausted = base >= cap;
-            if (!live) {
-                uint32_t id = base + (uint32_t)__popc(empty & lanemask_lt());
+            const uint32_t r = (uint32_t)__popc(empty & lanemask_lt());
+            uint32_t id = cap;
+            if (r < avail) id = pool + r;
+            else if (took) id = nb + (r - avail);
+            if (took) {
+                const uint32_t used = need > avail ? need - avail : 0u;
+                pool = nb + min(used, kIdBlock);
+                pool_end = nb + kIdBlock;
+                if (nb >= cap) pool = pool_end;  // nothing left below the cap
+            } else {
+                pool += min(need, avail);
+            }
+            if (!live && id < cap) {
                 // the writing pass retraces only paths with a record in a map
                 const bool needed = !P.store || (id < ms.paths && P.cnt_s[id] > 0u) ||
                                     (id < mv.paths && P.cnt_v[id] > 0u);
-                if (base < cap && id < cap && needed) {
+                if (needed) {
                     start_path(P, id, p, S);
                     live = true;
                 }
             }
         }
         if (!__any_sync(0xffffffffu, live)) {
-            if (exhausted) break;
+            if (pool >= pool_end && !has_pending) break;
             continue;
         }
         if (live) {
