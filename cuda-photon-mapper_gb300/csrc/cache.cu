@@ -708,6 +708,29 @@ __global__ void select_kernel(uint64_t seed, uint32_t frame, uint32_t total, con
         sel[i] = (uint32_t)(((uint64_t)r.v[0] * total) >> 32);
 }
 
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void sample_keys_kernel(CacheGrid g, const float4 *qa, const uint32_t *sel, uint32_t n,
+                                   uint32_t *keys, uint32_t *vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = qa[sel[i]];
+    const QueryPos q = unit_pos(g, a);
+    const uint32_t x = min((uint32_t)(q.px * 1024.0f), 1023u);
+    const uint32_t y = min((uint32_t)(q.py * 1024.0f), 1023u);
+    const uint32_t z = min((uint32_t)(q.pz * 1024.0f), 1023u);
+    const uint32_t vol = __float_as_int(a.w) == kNone ? 1u : 0u;
+    keys[i] = (vol << 30) | (spread10(x) << 2) | (spread10(y) << 1) | spread10(z);
+    vals[i] = i;
+}
+
 __global__ void iota_kernel(uint32_t *v, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) v[i] = i;
@@ -759,6 +782,14 @@ cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const ui
                          cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     select_kernel<<<(n + 255) / 256, 256, 0, s>>>(seed, frame, total, slist, ns_total, n, surf_frac, sel);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_sample_keys(const CacheGrid &g, const float4 *qa, const uint32_t *sel, uint32_t n,
+                              uint32_t *keys, uint32_t *vals, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    sample_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(g, qa, sel, n, keys, vals);
     note_launch();
     return cudaGetLastError();
 }

@@ -70,6 +70,17 @@ cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView
                              const float4 *qa, const float4 *qd, const uint32_t *sel,
                              const uint32_t *out_index, uint32_t n, int k, float radius,
                              float4 *val, cudaStream_t s);
+// The same estimates for runs of `run` consecutive entries of `order`
+// (positions into sel), each warm-started from its predecessor in the run
+// when both read the same map; val[order[j]] receives query sel[order[j]].
+cudaError_t cache_knn_values_runs(const PScene &S, const MapView &surf, const MapView &vol,
+                                  const float4 *qa, const float4 *qd, const uint32_t *sel,
+                                  const uint32_t *order, uint32_t n, int run, int k, float radius,
+                                  float4 *val, cudaStream_t s);
+// keys[i] = (1 for a volume query, 0 for a diffuse one) << 30 | the 30-bit
+// Morton code of query sel[i]'s position in the grid box; vals[i] = i.
+cudaError_t cache_sample_keys(const CacheGrid &g, const float4 *qa, const uint32_t *sel, uint32_t n,
+                              uint32_t *keys, uint32_t *vals, cudaStream_t s);
 // v[i] = i for i < n.
 cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s);
 // Training picks from Philox(seed, frame, i): with probability surf_frac

@@ -46,6 +46,8 @@ struct CacheState {
 namespace pm {
 namespace {
 
+constexpr int kTargetRun = 8;  // training targets warm-started in runs of this length
+
 template <typename T>
 cudaError_t dalloc(T **p, size_t count) {
     *p = nullptr;
@@ -272,17 +274,15 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
         PM_TRY(cudaEventRecord(c->tev0, stream));
         PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, c->nq, c->slist, c->nsurf, ns,
                             c->cfg.surface_fraction, c->sel, stream));
-        // targets in query order (neighbouring warps walk the same part of
-        // the tree), written back to the random order the steps read
-        PM_TRY(cudaMemcpyAsync(c->skey, c->sel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToDevice, stream));
-        PM_TRY(cache_iota(c->sval, ns, stream));
-        int bits = 1;
-        while (bits < 32 && (c->nq >> bits) != 0u) ++bits;
+        // targets in spatial order -- (map, Morton code) -- in runs of
+        // kTargetRun warm-started queries per warp, written back to the
+        // random order the steps read
+        PM_TRY(cache_sample_keys(c->grid, c->qa, c->sel, ns, c->skey, c->sval, stream));
         uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
-        PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, bits,
+        PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31,
                                     c->shist, stream, &ok_keys, &ok_vals));
-        PM_TRY(cache_knn_values(st->dscene, surf, vol, c->qa, c->qd, ok_keys, ok_vals, ns, st->cfg.k,
-                                st->cfg.radius, c->tgt, stream));
+        PM_TRY(cache_knn_values_runs(st->dscene, surf, vol, c->qa, c->qd, c->sel, ok_vals, ns,
+                                     kTargetRun, st->cfg.k, st->cfg.radius, c->tgt, stream));
         PM_TRY(cudaEventRecord(c->ev[5], stream));
         if (!(c->target_scale > 0.0f)) {
             float sum = 0.0f;
@@ -481,6 +481,31 @@ pm_status pm_cache_get_queries(pm_ctx *ctx, float4 *qa, float4 *qd, uint32_t cap
     PM_TRY(cudaDeviceSynchronize());
     if (n && qa) PM_TRY(cudaMemcpy(qa, c->qa, sizeof(float4) * n, cudaMemcpyDeviceToHost));
     if (n && qd) PM_TRY(cudaMemcpy(qd, c->qd, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    return PM_OK;
+}
+
+pm_status pm_cache_debug_targets(pm_ctx *ctx, float4 *targets, uint32_t *query) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, true);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    PhysicalState *st = ctx->phys;
+    CacheState *c = ctx->cache;
+    s = ensure_queries(ctx, st, c, 0);
+    if (s != PM_OK) return s;
+    const uint32_t ns = c->cfg.train_samples;
+    cudaError_t e;
+    PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, c->nq, c->slist, c->nsurf, ns,
+                        c->cfg.surface_fraction, c->sel, 0));
+    PM_TRY(cache_sample_keys(c->grid, c->qa, c->sel, ns, c->skey, c->sval, 0));
+    uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
+    PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31, c->shist,
+                                0, &ok_keys, &ok_vals));
+    PM_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->qa, c->qd,
+                                 c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, c->tgt, 0));
+    PM_TRY(cudaDeviceSynchronize());
+    if (targets) PM_TRY(cudaMemcpy(targets, c->tgt, sizeof(float4) * ns, cudaMemcpyDeviceToHost));
+    if (query) PM_TRY(cudaMemcpy(query, c->sel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
     return PM_OK;
 }
 

@@ -162,6 +162,7 @@ PROTOTYPES = {
     "pm_cache_debug_step": (_i, [_vp, _vp, _vp, _vp, _c.c_uint32, _f, _vp, _vp, _vp, _vp, _vp]),
     "pm_cache_get_queries": (_i, [_vp, _vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
     "pm_cache_get_values": (_i, [_vp, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
+    "pm_cache_debug_targets": (_i, [_vp, _vp, _vp]),
     "pm_batch_scene": (_i, [_i, _c.c_uint64, _c.POINTER(Scene), _c.POINTER(Config)]),
     "pm_batch_create": (_i, [_vp, _i, _vp, _vp, _c.POINTER(_vp)]),
     "pm_batch_destroy": (None, [_vp]),
@@ -408,6 +409,15 @@ class Context:
         self._check(self.lib.pm_cache_get_values(self.h, v.ctypes.data, n.value, _c.byref(n)),
                     "pm_cache_get_values")
         return v
+
+    def cache_debug_targets(self):
+        """(targets [train_samples, 4], query index of each) of the next training frame."""
+        n = self.cache_cfg.train_samples
+        t = np.zeros((n, 4), np.float32)
+        q = np.zeros(n, np.uint32)
+        self._check(self.lib.pm_cache_debug_targets(self.h, t.ctypes.data, q.ctypes.data),
+                    "pm_cache_debug_targets")
+        return t, q
 
     def cache_save(self, path):
         self._check(self.lib.pm_cache_save(self.h, path.encode()), "pm_cache_save")

@@ -375,6 +375,11 @@ PM_API pm_status pm_cache_get_queries(pm_ctx *ctx, float4 *qa, float4 *qd, uint3
 /* Per-query values of the last pm_render_cached (network or k-NN, before
  * the transmittance and albedo factors), host copy. */
 PM_API pm_status pm_cache_get_values(pm_ctx *ctx, float4 *val, uint32_t cap, uint32_t *count);
+/* The k-NN targets of the next training frame, as pm_cache_train computes
+ * them (spatially sorted, warm-started runs), without training: host copies
+ * of train_samples targets and the query index of each (both nullable).
+ * For checking the targets against per-query k-NN values. */
+PM_API pm_status pm_cache_debug_targets(pm_ctx *ctx, float4 *targets, uint32_t *query);
 /* Network + table + Adam state to a file (JSON header line, then raw fp32
  * arrays) and back; load requires the same levels and log2_table. */
 PM_API pm_status pm_cache_save(pm_ctx *ctx, const char *path);

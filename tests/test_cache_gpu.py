@@ -192,3 +192,16 @@ def test_cached_render_against_float64_at_bench_scale(ctx):
     print("rel RMSE vs FP64: k-NN %.4f cached %.4f; cached vs k-NN %.4f" % (e_knn, e_cache, e_ab))
     assert e_cache < 1e-2, (e_knn, e_cache)
     assert e_ab < 1.5e-2, e_ab
+
+
+@pytest.mark.parametrize("preset", [1, 2])
+def test_training_targets_equal_per_query_knn(ctx, preset):
+    """The warm-started runs of spatially sorted samples give exactly the
+    per-query k-NN estimates (the values the k-NN render path sums)."""
+    sc, cf = small(preset, 30000, 30000, size=(48, 40))
+    frame(ctx, sc, cf)
+    ctx.cache_enable(log2_table=12, train_samples=1 << 14, batch=1 << 12)
+    render(ctx, cf, cached=1)
+    per_query = ctx.cache_values()
+    targets, query = ctx.cache_debug_targets()
+    np.testing.assert_array_equal(targets[:, :3].view(np.uint32), per_query[query, :3].view(np.uint32))
