@@ -84,8 +84,8 @@ def load_peaks():
 
 
 def load_traffic(preset):
-    """DRAM bytes per render launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "render_kernel_preset%d_traffic.txt" % preset)
+    """DRAM bytes per k-NN estimate launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "query_knn_run_kernel_preset%d_traffic.txt" % preset)
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_launch:"):
@@ -471,7 +471,7 @@ def run_ours(args):
         clocks = ClockSampler(local)
         clocks.start()
         l0 = lib.pm_kernel_launches()
-        frame_ms, emit_ms, build_ms, render_ms = [], [], [], []
+        frame_ms, emit_ms, build_ms, render_ms, gather_ms = [], [], [], [], []
         gathers = surf = vol = paths = 0
         for _ in range(args.steps):
             flush.zero_()  # L2 flush between frames, before the start event
@@ -486,6 +486,7 @@ def run_ours(args):
             emit_ms.append(st.ms_emit)
             build_ms.append(st.ms_build)
             render_ms.append(st.ms_render)
+            gather_ms.append(st.ms_gather)
             surf += st.surface_gathers
             vol += st.volume_gathers
             paths += st.paths_traced
@@ -497,7 +498,6 @@ def run_ours(args):
         map_sizes = list(st.map_size)
     gathers = surf + vol
     t_total = sum(frame_ms) / 1e3
-    t_render = sum(render_ms) / 1e3
 
     # end to end through the C ABI: per step the scene goes in from host
     # memory (pm_update_scene), the frame's radiance and 8-bit image come
@@ -529,10 +529,12 @@ def run_ours(args):
 
     peak, peak_kind = load_peaks()
     k = cfg.k
-    render_s = t_render / args.steps
+    gather_s = statistics.mean(gather_ms) / 1e3
     q_per_frame = (surf + vol) / args.steps
-    alg_bytes = q_per_frame * 32.0 * k + npix * 16.0
-    achieved = alg_bytes / render_s / 1e9
+    # per query: k records of 32 B (position + power), the 32 B query record,
+    # its 4 B index in spatial order and the 16 B value written
+    alg_bytes = q_per_frame * (32.0 * k + 52.0)
+    achieved = alg_bytes / gather_s / 1e9
     traffic = load_traffic(args.preset)
     line = {
         "metric": "gathers/s",
@@ -557,7 +559,8 @@ def run_ours(args):
         },
         "phases": {
             "emit_ms": statistics.mean(emit_ms), "build_ms": statistics.mean(build_ms),
-            "render_ms": statistics.mean(render_ms), "frame_ms": statistics.mean(frame_ms),
+            "render_ms": statistics.mean(render_ms), "gather_ms": statistics.mean(gather_ms),
+            "frame_ms": statistics.mean(frame_ms),
             "paths_per_frame": paths / args.steps / world,
             "photons_per_s": paths / (sum(emit_ms) / 1e3) / world,
             "records_per_s": sum(map_sizes) * args.steps / (sum(emit_ms) / 1e3),
@@ -569,13 +572,13 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(photonmap.ctypes.sizeof(photonmap.Scene)),
                 "d2h_bytes_per_step": int(npix * (16 + 4)),
                 "steps": args.e2e_steps},
-        "roofline": {"bound": "hbm", "kernel": "render_kernel", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "query_knn_run_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
                      "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "formula": "gathers x 32 B x k + pixels x 16 B, over the render "
-                                "kernel's CUDA-event time"},
+                     "formula": "gathers x (32 B x k + 52 B), over the k-NN estimate "
+                                "kernel's CUDA-event time (events on the render stream)"},
         "gpu_launches": int(launches),
         "clocks": clk,
     }

@@ -697,6 +697,40 @@ __global__ void composite_kernel(PScene Sc, const uint32_t *off, const float4 *q
                                 to_u8_sat((double)(L.z * exposure) * 255.0), 255);
 }
 
+// Same per-pixel loop, from raw values, with the render kernel's
+// operations and order: volume scale = (T * dt) * (1 / (4/3 pi r^3)),
+// L += e * scale; diffuse scale = (T * (1 / (pi r^2))) * (1 / pi),
+// L += albedo * (e * scale).
+__global__ void composite_exact_kernel(PScene Sc, const uint32_t *off, const float4 *qa,
+                                       const float4 *qd, const float4 *raw, uint32_t npix,
+                                       float exposure, float4 *rad, uchar4 *rgba) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    v3 L = mk3(0.f, 0.f, 0.f);
+    const uint32_t end = off[pix + 1];
+    for (uint32_t i = off[pix]; i < end; ++i) {
+        const float4 v = raw[i];
+        if (!(v.w >= 0.0f)) continue;
+        const float r2 = v.w;
+        const v3 e = mk3(v.x, v.y, v.z);
+        const float w = qd[i].w;
+        const int obj = __float_as_int(qa[i].w);
+        if (obj == kNone) {
+            const float scale = w * (1.0f / (4.18879020f * r2 * sqrtf(r2)));
+            L = L + e * scale;
+        } else {
+            const v3 a = material_albedo(Sc, obj);
+            const float scale = w * (1.0f / (3.14159265f * r2)) * 0.318309886f;
+            L = L + mk3(a.x * (e.x * scale), a.y * (e.y * scale), a.z * (e.z * scale));
+        }
+    }
+    if (rad) rad[pix] = make_float4(L.x, L.y, L.z, 1.0f);
+    if (rgba)
+        rgba[pix] = make_uchar4(to_u8_sat((double)(L.x * exposure) * 255.0),
+                                to_u8_sat((double)(L.y * exposure) * 255.0),
+                                to_u8_sat((double)(L.z * exposure) * 255.0), 255);
+}
+
 __global__ void select_kernel(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
                               uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -721,7 +755,7 @@ __global__ void sample_keys_kernel(CacheGrid g, const float4 *qa, const uint32_t
                                    uint32_t *keys, uint32_t *vals) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 a = qa[sel[i]];
+    const float4 a = qa[sel ? sel[i] : i];
     const QueryPos q = unit_pos(g, a);
     const uint32_t x = min((uint32_t)(q.px * 1024.0f), 1023u);
     const uint32_t y = min((uint32_t)(q.py * 1024.0f), 1023u);
@@ -773,6 +807,16 @@ cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *
                             float4 *rad, uchar4 *rgba, cudaStream_t s) {
     if (npix == 0) return cudaSuccess;
     composite_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, off, qa, qd, val, npix, exposure, rad, rgba);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 *qa,
+                             const float4 *qd, const float4 *raw, uint32_t npix, float exposure,
+                             float4 *rad, uchar4 *rgba, cudaStream_t s) {
+    if (npix == 0) return cudaSuccess;
+    composite_exact_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, off, qa, qd, raw, npix, exposure, rad,
+                                                              rgba);
     note_launch();
     return cudaGetLastError();
 }

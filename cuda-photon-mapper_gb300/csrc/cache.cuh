@@ -76,9 +76,17 @@ cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView
 cudaError_t cache_knn_values_runs(const PScene &S, const MapView &surf, const MapView &vol,
                                   const float4 *qa, const float4 *qd, const uint32_t *sel,
                                   const uint32_t *order, uint32_t n, int run, int k, float radius,
-                                  float4 *val, cudaStream_t s);
+                                  bool raw, float4 *val, cudaStream_t s);
+// The render's radiance from raw per-query values (flux sum, squared radius
+// or -1): per pixel, in query order, with exactly the arithmetic of the
+// single-kernel render (transmittance factors from the query records), so
+// the image is bit-identical to render_frame's.
+cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 *qa,
+                             const float4 *qd, const float4 *raw, uint32_t npix, float exposure,
+                             float4 *rad, uchar4 *rgba, cudaStream_t s);
 // keys[i] = (1 for a volume query, 0 for a diffuse one) << 30 | the 30-bit
-// Morton code of query sel[i]'s position in the grid box; vals[i] = i.
+// Morton code of query sel[i]'s (or query i's, sel null) position in the
+// grid box; vals[i] = i.
 cudaError_t cache_sample_keys(const CacheGrid &g, const float4 *qa, const uint32_t *sel, uint32_t n,
                               uint32_t *keys, uint32_t *vals, cudaStream_t s);
 // v[i] = i for i < n.

@@ -19,14 +19,7 @@ struct CacheState {
     pm::CacheParams p;
     size_t table_floats = 0;
     int sm_count = 148;
-    // query list of the current camera
-    uint32_t npix_cap = 0;
-    uint32_t *cnt = nullptr, *off = nullptr, *scan_tmp = nullptr;
-    uint32_t *scnt = nullptr, *soff = nullptr, *slist = nullptr;  // diffuse queries
-    float4 *qa = nullptr, *qd = nullptr, *val = nullptr;
-    uint32_t qcap = 0, nq = 0, nsurf = 0;
-    uint64_t qgen = 0;
-    int qflags = -1;  // bit 0: volume queries, bit 1: diffuse queries
+    // the query list itself lives in the physical state (shared with pm_render)
     // training
     uint32_t *sel = nullptr;
     float4 *tgt = nullptr;
@@ -61,9 +54,6 @@ void free_cache(CacheState *c) {
     cudaFree(c->p.w_part);
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
     cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status); cudaFree(c->p.w_img);
-    cudaFree(c->cnt); cudaFree(c->off); cudaFree(c->scan_tmp);
-    cudaFree(c->scnt); cudaFree(c->soff); cudaFree(c->slist);
-    cudaFree(c->qa); cudaFree(c->qd); cudaFree(c->val);
     cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
     cudaFree(c->shist); cudaFree(c->sn);
@@ -84,61 +74,18 @@ void set_grid_box(CacheGrid &g, const pm_scene &sc) {
     }
 }
 
-// Builds the query list of the installed camera unless it is current.
-pm_status ensure_queries(pm_ctx *ctx, PhysicalState *st, CacheState *c, cudaStream_t stream) {
-    const MapView surf = view_of(st->map[0]), vol = view_of(st->map[1]);
-    const int flags = (vol.n > 0 ? 1 : 0) | (surf.n > 0 ? 2 : 0);
-    if (c->qgen == st->gen && c->qflags == flags) return PM_OK;
-    cudaError_t e;
-#define PM_TRY(x) do { e = (x); if (e != cudaSuccess) return check_cuda(ctx, e, #x); } while (0)
-    const uint32_t npix = (uint32_t)st->cfg.width * (uint32_t)st->cfg.height;
-    if (npix > c->npix_cap) {
-        cudaFree(c->cnt); cudaFree(c->off); cudaFree(c->scan_tmp);
-        cudaFree(c->scnt); cudaFree(c->soff); cudaFree(c->slist);
-        c->cnt = c->off = c->scan_tmp = c->scnt = c->soff = c->slist = nullptr;
-        c->npix_cap = 0;
-        PM_TRY(dalloc(&c->cnt, npix));
-        PM_TRY(dalloc(&c->off, (size_t)npix + 1));
-        PM_TRY(dalloc(&c->scnt, npix));
-        PM_TRY(dalloc(&c->soff, (size_t)npix + 1));
-        PM_TRY(dalloc(&c->slist, npix));
-        PM_TRY(dalloc(&c->scan_tmp, scan_tile_count(npix) + 1));
-        c->npix_cap = npix;
-    }
-    const RenderParams R = render_params(st);
-    PM_TRY(cudaEventRecord(c->ev[0], stream));
-    PM_TRY(cache_count_queries(st->dscene, R, flags & 1, flags & 2, c->cnt, c->scnt, stream));
-    PM_TRY(exclusive_scan_u32_large(c->cnt, c->off, npix, c->off + npix, c->scan_tmp, stream));
-    PM_TRY(exclusive_scan_u32_large(c->scnt, c->soff, npix, c->soff + npix, c->scan_tmp, stream));
-    uint32_t totals[2] = {0, 0};
-    PM_TRY(cudaMemcpyAsync(&totals[0], c->off + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-    PM_TRY(cudaMemcpyAsync(&totals[1], c->soff + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-    PM_TRY(cudaStreamSynchronize(stream));
-    const uint32_t total = totals[0];
-    if (total > c->qcap) {
-        cudaFree(c->qa); cudaFree(c->qd); cudaFree(c->val);
-        c->qa = c->qd = c->val = nullptr;
-        c->qcap = 0;
-        const uint32_t cap = total + total / 8;
-        PM_TRY(dalloc(&c->qa, cap));
-        PM_TRY(dalloc(&c->qd, cap));
-        PM_TRY(dalloc(&c->val, cap));
-        c->qcap = cap;
-    }
-    PM_TRY(cache_write_queries(st->dscene, R, flags & 1, flags & 2, c->off, c->soff, c->qa, c->qd,
-                               c->slist, stream));
-    PM_TRY(cudaEventRecord(c->ev[1], stream));
-    PM_TRY(cudaEventSynchronize(c->ev[1]));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
-    c->stats.ms_queries = ms;
-    c->nq = total;
-    c->nsurf = totals[1];
-    c->qgen = st->gen;
-    c->qflags = flags;
+// Builds the query list of the installed camera unless it is current
+// (force: always) and points the cache's grid box at the scene.
+pm_status ensure_queries(pm_ctx *ctx, PhysicalState *st, CacheState *c, cudaStream_t stream,
+                         bool force = false) {
+    cudaError_t e = query_list_build(st, force, stream);
+    if (e != cudaSuccess) return check_cuda(ctx, e, "query_list_build");
+    c->stats.ms_queries = 0.0f;
     set_grid_box(c->grid, st->scene);
     return PM_OK;
 }
+
+#define PM_TRY(x) do { e = (x); if (e != cudaSuccess) return check_cuda(ctx, e, #x); } while (0)
 
 pm_status need_cache(pm_ctx *ctx, bool need_maps) {
     if (!ctx->cache) return fail(ctx, PM_ERR_STATE, "radiance cache not enabled");
@@ -265,24 +212,24 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
     CacheState *c = ctx->cache;
     s = ensure_queries(ctx, st, c, stream);
     if (s != PM_OK) return s;
-    if (c->nq == 0 || frames == 0) return PM_OK;
+    if (st->ql.nq == 0 || frames == 0) return PM_OK;
     cudaError_t e;
     const uint32_t ns = c->cfg.train_samples, batch = c->cfg.batch;
     const uint32_t nb = (ns + batch - 1) / batch;
     const MapView surf = view_of(st->map[0]), vol = view_of(st->map[1]);
     for (int f = 0; f < frames; ++f) {
         PM_TRY(cudaEventRecord(c->tev0, stream));
-        PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, c->nq, c->slist, c->nsurf, ns,
+        PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, st->ql.nq, st->ql.slist, st->ql.nsurf, ns,
                             c->cfg.surface_fraction, c->sel, stream));
         // targets in spatial order -- (map, Morton code) -- in runs of
         // kTargetRun warm-started queries per warp, written back to the
         // random order the steps read
-        PM_TRY(cache_sample_keys(c->grid, c->qa, c->sel, ns, c->skey, c->sval, stream));
+        PM_TRY(cache_sample_keys(c->grid, st->ql.qa, c->sel, ns, c->skey, c->sval, stream));
         uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
         PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31,
                                     c->shist, stream, &ok_keys, &ok_vals));
-        PM_TRY(cache_knn_values_runs(st->dscene, surf, vol, c->qa, c->qd, c->sel, ok_vals, ns,
-                                     kTargetRun, st->cfg.k, st->cfg.radius, c->tgt, stream));
+        PM_TRY(cache_knn_values_runs(st->dscene, surf, vol, st->ql.qa, st->ql.qd, c->sel, ok_vals, ns,
+                                     kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt, stream));
         PM_TRY(cudaEventRecord(c->ev[5], stream));
         if (!(c->target_scale > 0.0f)) {
             float sum = 0.0f;
@@ -296,7 +243,7 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
         PM_TRY(cudaMemsetAsync(c->p.loss, 0, sizeof(float), stream));
         for (uint32_t b = 0; b < nb; ++b) {
             const uint32_t o = b * batch, n = std::min(batch, ns - o);
-            PM_TRY(cache_backward(c->grid, c->p, st->dscene, c->qa, c->qd, c->sel + o, c->tgt + o, n,
+            PM_TRY(cache_backward(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, c->sel + o, c->tgt + o, n,
                                   1.0f / c->target_scale, 1.0f / (3.0f * (float)n), c->cfg.loss_eps,
                                   nullptr, nullptr, c->sm_count, stream));
             float lr = c->cfg.lr;
@@ -331,24 +278,30 @@ pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int sour
     DeviceGuard g(ctx->device);
     PhysicalState *st = ctx->phys;
     CacheState *c = ctx->cache;
-    s = ensure_queries(ctx, st, c, stream);
+    // the list is rebuilt on every render call, like pm_render's
+    s = ensure_queries(ctx, st, c, stream, true);
     if (s != PM_OK) return s;
     cudaError_t e;
     const uint32_t npix = (uint32_t)st->cfg.width * (uint32_t)st->cfg.height;
     PM_TRY(cudaEventRecord(c->ev[2], stream));
     if (source == 0) {
         const float scale = c->target_scale > 0.0f ? c->target_scale : 1.0f;
-        PM_TRY(cache_infer(c->grid, c->p, st->dscene, c->qa, c->qd, c->nq, scale, c->val, c->sm_count,
-                           stream));
+        PM_TRY(cache_infer(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, st->ql.nq, scale,
+                           st->ql.val, c->sm_count, stream));
+        PM_TRY(cudaEventRecord(c->ev[3], stream));
+        PM_TRY(cache_composite(st->dscene, st->ql.off, st->ql.qa, st->ql.qd, st->ql.val, npix,
+                               st->cfg.exposure, radiance, rgba, stream));
     } else {
-        PM_TRY(cache_knn_values(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->qa, c->qd,
-                                nullptr, nullptr, c->nq, st->cfg.k, st->cfg.radius, c->val, stream));
+        // the k-NN render through the list (pm_render's path): raw values,
+        // then the exact composite
+        PM_TRY(knn_values_raw(st, stream));
+        PM_TRY(cudaEventRecord(c->ev[3], stream));
+        PM_TRY(render_composite(st->dscene, st->ql.off, st->ql.qa, st->ql.qd, st->ql.val, npix,
+                                st->cfg.exposure, radiance, rgba, stream));
     }
-    PM_TRY(cudaEventRecord(c->ev[3], stream));
-    PM_TRY(cache_composite(st->dscene, c->off, c->qa, c->qd, c->val, npix, st->cfg.exposure,
-                           radiance, rgba, stream));
     PM_TRY(cudaEventRecord(c->ev[4], stream));
-    c->stats.queries = c->nq;
+    st->ql.val_owner = 2;
+    c->stats.queries = st->ql.nq;
     c->rendered = true;
     return PM_OK;
 }
@@ -472,15 +425,16 @@ pm_status pm_cache_get_queries(pm_ctx *ctx, float4 *qa, float4 *qd, uint32_t cap
     pm_status s = need_cache(ctx, true);
     if (s != PM_OK) return s;
     DeviceGuard g(ctx->device);
+    PhysicalState *st = ctx->phys;
     CacheState *c = ctx->cache;
-    s = ensure_queries(ctx, ctx->phys, c, 0);
+    s = ensure_queries(ctx, st, c, 0);
     if (s != PM_OK) return s;
-    if (count) *count = c->nq;
-    const uint32_t n = std::min(cap, c->nq);
+    if (count) *count = st->ql.nq;
+    const uint32_t n = std::min(cap, st->ql.nq);
     cudaError_t e;
     PM_TRY(cudaDeviceSynchronize());
-    if (n && qa) PM_TRY(cudaMemcpy(qa, c->qa, sizeof(float4) * n, cudaMemcpyDeviceToHost));
-    if (n && qd) PM_TRY(cudaMemcpy(qd, c->qd, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    if (n && qa) PM_TRY(cudaMemcpy(qa, st->ql.qa, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    if (n && qd) PM_TRY(cudaMemcpy(qd, st->ql.qd, sizeof(float4) * n, cudaMemcpyDeviceToHost));
     return PM_OK;
 }
 
@@ -495,14 +449,15 @@ pm_status pm_cache_debug_targets(pm_ctx *ctx, float4 *targets, uint32_t *query) 
     if (s != PM_OK) return s;
     const uint32_t ns = c->cfg.train_samples;
     cudaError_t e;
-    PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, c->nq, c->slist, c->nsurf, ns,
+    PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, st->ql.nq, st->ql.slist, st->ql.nsurf, ns,
                         c->cfg.surface_fraction, c->sel, 0));
-    PM_TRY(cache_sample_keys(c->grid, c->qa, c->sel, ns, c->skey, c->sval, 0));
+    PM_TRY(cache_sample_keys(c->grid, st->ql.qa, c->sel, ns, c->skey, c->sval, 0));
     uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
     PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31, c->shist,
                                 0, &ok_keys, &ok_vals));
-    PM_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->qa, c->qd,
-                                 c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, c->tgt, 0));
+    PM_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), st->ql.qa, st->ql.qd,
+                                 c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt,
+                                 0));
     PM_TRY(cudaDeviceSynchronize());
     if (targets) PM_TRY(cudaMemcpy(targets, c->tgt, sizeof(float4) * ns, cudaMemcpyDeviceToHost));
     if (query) PM_TRY(cudaMemcpy(query, c->sel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
@@ -514,13 +469,15 @@ pm_status pm_cache_get_values(pm_ctx *ctx, float4 *val, uint32_t cap, uint32_t *
     pm_status s = need_cache(ctx, false);
     if (s != PM_OK) return s;
     CacheState *c = ctx->cache;
-    if (!c->rendered) return fail(ctx, PM_ERR_STATE, "pm_cache_get_values before pm_render_cached");
+    PhysicalState *st = ctx->phys;
+    if (!c->rendered || st->ql.val_owner != 2)
+        return fail(ctx, PM_ERR_STATE, "pm_cache_get_values without a pm_render_cached since the last render");
     DeviceGuard g(ctx->device);
-    if (count) *count = c->nq;
-    const uint32_t n = std::min(cap, c->nq);
+    if (count) *count = st->ql.nq;
+    const uint32_t n = std::min(cap, st->ql.nq);
     cudaError_t e;
     PM_TRY(cudaDeviceSynchronize());
-    if (n && val) PM_TRY(cudaMemcpy(val, c->val, sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    if (n && val) PM_TRY(cudaMemcpy(val, st->ql.val, sizeof(float4) * n, cudaMemcpyDeviceToHost));
     return PM_OK;
 }
 

@@ -664,16 +664,18 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 }
 
 // k-NN estimates of runs of spatially sorted queries: warp w takes queries
-// order[w * run .. (w + 1) * run) (indices into sel), each warm-started from
-// the previous query's list when both read the same map and the previous
-// one found k records -- the march's warm start, applied to neighbouring
-// training samples. Results land at out[order[j]]; each is the exact
-// estimate query_knn_kernel computes.
+// order[w * run .. (w + 1) * run) (indices into sel, or the queries
+// themselves when sel is null), each warm-started from the previous query's
+// list when both read the same map and the previous one found k records --
+// the march's warm start, applied to spatial neighbours. Results land at
+// out[order[j]]: the exact estimate query_knn_kernel computes, or with raw
+// set the flux sum and the squared radius (-1 when nothing was found), from
+// which the render's own arithmetic finishes the estimate.
 template <int S>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     query_knn_run_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
                          const uint32_t *sel, const uint32_t *order, uint32_t n, int run, int k,
-                         float r2cap, float4 *out) {
+                         float r2cap, bool raw, float4 *out) {
     __shared__ WarpScratch ws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t first = (blockIdx.x * kWarpsPerBlock + wib) * (uint32_t)run;
@@ -686,7 +688,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     bool warm = false;
     for (uint32_t j = first; j < last; ++j) {
         const uint32_t i = order[j];
-        const uint32_t src = sel[i];
+        const uint32_t src = sel ? sel[i] : i;
         const float4 a = qa[src], d = qd[src];
         const int obj = __float_as_int(a.w);
         const v3 x = mk3(a.x, a.y, a.z), wo = mk3(d.x, d.y, d.z);
@@ -694,6 +696,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const int kind = surface ? 0 : 1;
         const MapView &m = surface ? surf : vol;
         v3 e = mk3(0.f, 0.f, 0.f);
+        float r2out = -1.0f;
         bool found_k = false;
         if (m.n > 0) {
             const bool use_warm = warm && kind == prev_kind;
@@ -706,14 +709,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             e = flux_sum<S>(kn, m, lane, surface ? 0 : 1, dirv, Sc.g, cap, r2cap, &found, &r2);
             found_k = found == k;
             if (found > 0) {
-                const float sc = surface ? (1.0f / (3.14159265f * r2)) * 0.318309886f
-                                         : 1.0f / (4.18879020f * r2 * sqrtf(r2));
-                e = e * sc;
+                r2out = r2;
+                if (!raw) {
+                    const float sc = surface ? (1.0f / (3.14159265f * r2)) * 0.318309886f
+                                             : 1.0f / (4.18879020f * r2 * sqrtf(r2));
+                    e = e * sc;
+                }
             } else {
                 e = mk3(0.f, 0.f, 0.f);
             }
         }
-        if (lane == 0) out[i] = make_float4(e.x, e.y, e.z, 0.0f);
+        if (lane == 0) out[i] = make_float4(e.x, e.y, e.z, raw ? r2out : 0.0f);
         warm = found_k;
         prev_kind = kind;
     }
@@ -798,16 +804,16 @@ cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView
 cudaError_t cache_knn_values_runs(const PScene &S, const MapView &surf, const MapView &vol,
                                   const float4 *qa, const float4 *qd, const uint32_t *sel,
                                   const uint32_t *order, uint32_t n, int run, int k, float radius,
-                                  float4 *val, cudaStream_t s) {
+                                  bool raw, float4 *val, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const float r2 = radius * radius;
     const uint32_t warps = (n + (uint32_t)run - 1) / (uint32_t)run;
     const dim3 grid((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
     switch (slots_for(k)) {
-        case 1: query_knn_run_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, val); break;
-        case 2: query_knn_run_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, val); break;
-        case 3: query_knn_run_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, val); break;
-        default: query_knn_run_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, val); break;
+        case 1: query_knn_run_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
+        case 2: query_knn_run_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
+        case 3: query_knn_run_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
+        default: query_knn_run_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
     }
     note_launch();
     return cudaGetLastError();

@@ -4,6 +4,31 @@
 #include "gather.cuh"
 #include "pm.h"
 
+// The frame as a list of radiance queries (every volume march sample and
+// every diffuse hit of every eye path, as the render visits them; see
+// eye_path.cuh), shared by the k-NN render and the learned cache.
+struct QueryList {
+    uint32_t npix_cap = 0;
+    uint32_t *cnt = nullptr, *off = nullptr;    // per pixel: queries, exclusive scan (+ total)
+    uint32_t *scnt = nullptr, *soff = nullptr;  // per pixel: diffuse queries (0 or 1), scan
+    uint32_t *slist = nullptr;                  // indices of the diffuse queries
+    uint32_t *scan_tmp = nullptr;
+    float4 *qa = nullptr, *qd = nullptr;        // query records
+    float4 *val = nullptr;                      // per-query values of the last pass
+    int val_owner = 0;                          // who wrote val: 0 nobody, 1 pm_render, 2 cache
+    uint32_t qcap = 0, nq = 0, nsurf = 0;
+    uint64_t gen = 0;                           // scene generation the list was built for
+    int flags = -1;                             // bit 0: volume queries, bit 1: diffuse
+    // spatial order: (map, Morton code) sort of the queries
+    uint32_t *key = nullptr, *ord = nullptr, *key_tmp = nullptr, *ord_tmp = nullptr;
+    uint32_t *hist = nullptr, *n_dev = nullptr;
+    uint32_t *order = nullptr;                  // points at the sorted query indices
+    uint32_t sort_cap = 0;
+    bool sorted = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float ms_build = 0.0f;
+};
+
 struct PhysicalState {
     pm_scene scene;
     pm_config cfg;
@@ -27,12 +52,15 @@ struct PhysicalState {
     uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
     uint32_t sort_cap = 0;
     unsigned long long *gctr = nullptr;
-    cudaEvent_t ev[6] = {};  // emit, build, render: start/stop
+    cudaEvent_t ev[8] = {};  // emit, build, render, k-NN estimates within the render: start/stop
     pm_frame_stats stats;
     bool emitted = false;
     bool rendered = false;
+    bool gathers_on_host = false;    // last render counted its gathers on the host
+    uint64_t host_gathers[2] = {0, 0};
     int sm_count = 148;
     uint64_t gen = 0;  // bumped whenever the scene or the camera changes
+    QueryList ql;
 };
 
 namespace pm {
@@ -48,6 +76,18 @@ inline MapView view_of(const PhysicalState::Map &m) {
     v.leaf_shift = m.leaf_shift;
     return v;
 }
+
+// Builds the query list of the installed camera (always when `force`, else
+// only when the scene changed since); synchronises the stream once to size
+// the list. Resets the spatial order.
+cudaError_t query_list_build(PhysicalState *st, bool force, cudaStream_t s);
+// Sorts the list by (map, Morton code of the position in the scene box)
+// into ql.order, unless already sorted.
+cudaError_t query_list_sort(PhysicalState *st, cudaStream_t s);
+void query_list_free(QueryList &ql);
+// Exact k-NN values of every query, raw (flux sum, squared radius or -1),
+// into ql.val: the list in spatial order, warm-started runs of queries.
+cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s);
 
 // The render parameters pm_render passes for the installed configuration.
 inline RenderParams render_params(const PhysicalState *st) {

@@ -1,5 +1,6 @@
 // physical.cu -- the physically based mode behind the pm_* C ABI: scene
 // installation, photon emission, kd-tree build, render and queries.
+#include "cache.cuh"
 #include "gather.cuh"
 #include "kdtree.cuh"
 #include "launch_count.cuh"
@@ -27,6 +28,7 @@ cudaError_t dalloc(T **p, size_t count) {
 
 void free_state(PhysicalState *st) {
     if (!st) return;
+    query_list_free(st->ql);
     cudaFree(st->het);
     for (auto &p : st->cnt) cudaFree(p);
     for (auto &p : st->off) cudaFree(p);
@@ -258,12 +260,43 @@ pm_status pm_render(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStream_t st
         return fail(ctx, PM_ERR_STATE, "pm_render before pm_build");
     DeviceGuard g(ctx->device);
     cudaError_t e;
+    // The frame as its list of radiance queries (rebuilt on every call),
+    // estimated in spatial order by warm-started runs, then summed per pixel
+    // in march order with the single-kernel render's arithmetic: the image
+    // is bit-identical to render_frame's.
+    PM_TRY(cudaEventRecord(st->ev[4], stream));
+    PM_TRY(query_list_build(st, true, stream));
+    PM_TRY(query_list_sort(st, stream));
+    PM_TRY(cudaEventRecord(st->ev[6], stream));
+    PM_TRY(knn_values_raw(st, stream));
+    PM_TRY(cudaEventRecord(st->ev[7], stream));
+    const uint32_t npix = (uint32_t)st->cfg.width * (uint32_t)st->cfg.height;
+    PM_TRY(render_composite(st->dscene, st->ql.off, st->ql.qa, st->ql.qd, st->ql.val, npix,
+                            st->cfg.exposure, radiance, rgba, stream));
+    PM_TRY(cudaEventRecord(st->ev[5], stream));
+    st->ql.val_owner = 1;
+    // one gather per query; the counts are known on the host
+    st->host_gathers[0] = st->ql.nsurf;
+    st->host_gathers[1] = (uint64_t)st->ql.nq - st->ql.nsurf;
+    st->gathers_on_host = true;
+    st->rendered = true;
+    return PM_OK;
+}
+
+pm_status pm_render_single_kernel(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStream_t stream) {
+    if (!ctx) return PM_ERR_INVALID;
+    PhysicalState *st = ctx->phys;
+    if (!st || !st->map[0].built || !st->map[1].built)
+        return fail(ctx, PM_ERR_STATE, "pm_render_single_kernel before pm_build");
+    DeviceGuard g(ctx->device);
+    cudaError_t e;
     RenderParams R = render_params(st);
     R.counters = st->gctr;
     PM_TRY(cudaMemsetAsync(st->gctr, 0, 2 * sizeof(unsigned long long), stream));
     PM_TRY(cudaEventRecord(st->ev[4], stream));
     PM_TRY(render_frame(st->dscene, view_of(st->map[0]), view_of(st->map[1]), R, radiance, rgba, stream));
     PM_TRY(cudaEventRecord(st->ev[5], stream));
+    st->gathers_on_host = false;
     st->rendered = true;
     return PM_OK;
 }
@@ -337,13 +370,21 @@ pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out) {
     cudaError_t e;
     if (st->rendered) {
         PM_TRY(cudaEventSynchronize(st->ev[5]));
-        unsigned long long c[2] = {0, 0};
-        PM_TRY(cudaMemcpy(c, st->gctr, sizeof(c), cudaMemcpyDeviceToHost));
-        st->stats.surface_gathers = c[0];
-        st->stats.volume_gathers = c[1];
         float ms = 0.f;
         PM_TRY(cudaEventElapsedTime(&ms, st->ev[4], st->ev[5]));
         st->stats.ms_render = ms;
+        if (st->gathers_on_host) {
+            st->stats.surface_gathers = st->host_gathers[0];
+            st->stats.volume_gathers = st->host_gathers[1];
+            PM_TRY(cudaEventElapsedTime(&ms, st->ev[6], st->ev[7]));
+            st->stats.ms_gather = ms;
+        } else {
+            unsigned long long c[2] = {0, 0};
+            PM_TRY(cudaMemcpy(c, st->gctr, sizeof(c), cudaMemcpyDeviceToHost));
+            st->stats.surface_gathers = c[0];
+            st->stats.volume_gathers = c[1];
+            st->stats.ms_gather = ms;
+        }
     }
     *out = st->stats;
     return PM_OK;

@@ -65,7 +65,7 @@ class FrameStats(_c.Structure):
         ("paths_traced", _c.c_uint64), ("map_size", _c.c_uint32 * 2),
         ("map_paths", _c.c_uint32 * 2), ("surface_gathers", _c.c_uint64),
         ("volume_gathers", _c.c_uint64), ("ms_emit", _c.c_float), ("ms_build", _c.c_float),
-        ("ms_render", _c.c_float), ("_pad", _c.c_byte * 4),
+        ("ms_render", _c.c_float), ("ms_gather", _c.c_float),
     ]
 
 
@@ -134,6 +134,7 @@ PROTOTYPES = {
     "pm_emit": (_i, [_vp, _vp]),
     "pm_build": (_i, [_vp, _vp]),
     "pm_render": (_i, [_vp, _vp, _vp, _vp]),
+    "pm_render_single_kernel": (_i, [_vp, _vp, _vp, _vp]),
     "pm_knn": (_i, [_vp, _i, _vp, _c.c_uint32, _i, _f, _vp, _vp, _vp]),
     "pm_radius_gather": (_i, [_vp, _i, _vp, _vp, _c.c_uint32, _f, _f, _vp, _vp]),
     "pm_get_photons": (_i, [_vp, _i, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
@@ -284,6 +285,10 @@ class Context:
 
     def render(self, radiance=None, rgba=None, stream=0):
         self._check(self.lib.pm_render(self.h, radiance, rgba, stream), "pm_render")
+
+    def render_single_kernel(self, radiance=None, rgba=None, stream=0):
+        self._check(self.lib.pm_render_single_kernel(self.h, radiance, rgba, stream),
+                    "pm_render_single_kernel")
 
     def knn(self, map_id, queries, nq, k, radius, idx, d2, stream=0):
         self._check(self.lib.pm_knn(self.h, map_id, queries, nq, k, radius, idx, d2, stream),

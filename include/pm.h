@@ -183,6 +183,8 @@ typedef struct pm_frame_stats {
     uint64_t surface_gathers;           /* k-NN queries on the surface map */
     uint64_t volume_gathers;            /* k-NN queries on the volume map (march steps) */
     float ms_emit, ms_build, ms_render; /* device time of the last emit / build / render */
+    float ms_gather;                    /* of ms_render: the k-NN estimates (the whole
+                                           kernel for pm_render_single_kernel) */
 } pm_frame_stats;
 
 /* Fills *scene and *cfg with one of the benchmark presets:
@@ -209,6 +211,15 @@ PM_API pm_status pm_build(pm_ctx *ctx, cudaStream_t stream);
  * surface radiance estimate. radiance (nullable, device): width*height
  * float4 (rgb, alpha = 1); rgba (nullable, device): width*height uchar4. */
 PM_API pm_status pm_render(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStream_t stream);
+/* The same image from one kernel launch (a warp per pixel marching its eye
+ * path, each k-NN warm-started from the previous march sample), without the
+ * query list: no host synchronisation, slower on large frames. pm_render
+ * builds the frame's query list (one stream synchronisation to size it),
+ * estimates the queries in spatial order -- each warm-started from its
+ * neighbour -- and sums them per pixel with this kernel's arithmetic, so the
+ * two are bit-identical. */
+PM_API pm_status pm_render_single_kernel(pm_ctx *ctx, float4 *radiance, uchar4 *rgba,
+                                         cudaStream_t stream);
 /* k nearest photons of map `map` for nq query points (device float4
  * xyz), within radius; idx_out / d2_out (device, nq*k) receive photon
  * indices and squared distances sorted by (distance, index); missing
@@ -372,8 +383,10 @@ PM_API pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4
 /* Query list of the current camera (host copies, nullable; *count always). */
 PM_API pm_status pm_cache_get_queries(pm_ctx *ctx, float4 *qa, float4 *qd, uint32_t cap,
                                       uint32_t *count);
-/* Per-query values of the last pm_render_cached (network or k-NN, before
- * the transmittance and albedo factors), host copy. */
+/* Per-query values of the last pm_render_cached, host copy. Source 0: the
+ * network's radiance before the transmittance and albedo factors. Source 1:
+ * the k-NN flux sum (xyz) and the squared gather radius (w; -1 where no
+ * record was found). PM_ERR_STATE after a pm_render, which reuses them. */
 PM_API pm_status pm_cache_get_values(pm_ctx *ctx, float4 *val, uint32_t cap, uint32_t *count);
 /* The k-NN targets of the next training frame, as pm_cache_train computes
  * them (spatially sorted, warm-started runs), without training: host copies

@@ -162,6 +162,26 @@ def test_render_bit_exact(ctx, preset, size):
     assert st.surface_gathers > 0 and st.volume_gathers > 0
 
 
+@pytest.mark.parametrize("preset,size,k", [(1, (48, 40), None), (2, (64, 48), None),
+                                           (3, (64, 36), None), (2, (40, 30), 1), (3, (40, 30), 64)])
+def test_query_list_render_equals_single_kernel(ctx, preset, size, k):
+    """pm_render (query list, queries in spatial order) and
+    pm_render_single_kernel (warp-per-pixel march) give the same bits, the
+    same 8-bit image and the same gather counts."""
+    sc, cf = small(preset, 20000, 20000, size, k=k)
+    rad, rgba = gpu_frame(ctx, sc, cf)
+    st = ctx.stats()
+    rad1 = torch.zeros_like(torch.from_numpy(rad)).cuda()
+    rgba1 = torch.zeros_like(torch.from_numpy(rgba)).cuda()
+    ctx.render_single_kernel(rad1.data_ptr(), rgba1.data_ptr())
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(rad1.cpu().numpy()), bits(rad))
+    np.testing.assert_array_equal(rgba1.cpu().numpy(), rgba)
+    st1 = ctx.stats()
+    assert (st1.surface_gathers, st1.volume_gathers) == (st.surface_gathers, st.volume_gathers)
+    assert st.surface_gathers > 0
+
+
 def test_render_against_float64(ctx):
     sc, cf = small(2, 30000, 30000, (40, 40))
     rad, _ = gpu_frame(ctx, sc, cf)
