@@ -76,6 +76,7 @@ struct pm_batch {
     std::vector<float *> het;
     struct Map {
         float4 *pos = nullptr, *pow = nullptr, *tpos = nullptr, *tpow = nullptr;
+        float4 *tdir = nullptr;
         float4 *lo = nullptr, *hi = nullptr;
         uint32_t cap = 0;
     };
@@ -116,7 +117,7 @@ void free_batch(pm_batch *b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (auto &m : b->maps) {
-        cudaFree(m.pos); cudaFree(m.pow); cudaFree(m.tpos); cudaFree(m.tpow);
+        cudaFree(m.pos); cudaFree(m.pow); cudaFree(m.tpos); cudaFree(m.tpow); cudaFree(m.tdir);
         cudaFree(m.lo); cudaFree(m.hi);
     }
     for (float *h : b->het) cudaFree(h);
@@ -149,6 +150,7 @@ BatchRenderScene render_desc(const pm_batch *b, int s) {
         MapView v;
         v.pos = mp.tpos;
         v.pow = mp.tpow;
+        v.dir = mp.tdir;
         v.lo = mp.lo;
         v.hi = mp.hi;
         v.n = mp.cap;
@@ -219,6 +221,7 @@ cudaError_t build_scene(pm_batch *b, int s, cudaStream_t st, const pm_batch::Sor
         a.pow_in = mp.pow;
         a.pos_out = mp.tpos;
         a.pow_out = mp.tpow;
+        a.dir_out = mp.tdir;
         a.node_lo = mp.lo;
         a.node_hi = mp.hi;
         a.keys = so.keys; a.keys_tmp = so.keys_tmp;
@@ -325,6 +328,7 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
             C_TRY(dalloc(&mp.pow, mp.cap));
             C_TRY(dalloc(&mp.tpos, mp.cap));
             C_TRY(dalloc(&mp.tpow, mp.cap));
+            C_TRY(dalloc(&mp.tdir, mp.cap));
             C_TRY(dalloc(&mp.lo, tree_nodes(mp.cap)));
             C_TRY(dalloc(&mp.hi, tree_nodes(mp.cap)));
         }

@@ -1,422 +1,19 @@
-// gather.cu -- warp-cooperative k-nearest-photon search, radiance estimates
-// and the frame render (eye rays, specular chains, volume march).
-//
-// One warp answers one query. The k best candidates so far live in
-// registers as a list sorted by (squared distance, photon index), spread
-// across the warp: lane l holds list positions l*S .. l*S+S-1 (S = k/32
-// rounded up). Inserting a candidate is one shuffle from the previous lane
-// plus S compare-selects per lane. The tree is walked 32 children at a time:
-// the implicit layout puts the descendants five levels below node n at
-// n*32 .. n*32+31, so each lane tests one child box with one coalesced
-// load; surviving children are pushed far-to-near onto a per-warp stack in
-// shared memory. Leaves are 32 consecutive records, one per lane.
-//
-// A node is skipped only when its box is strictly farther than the current
-// k-th candidate, so a photon at exactly that distance with a smaller index
-// is still found: the result equals a brute-force sort by (distance, index).
+// gather.cu -- the k-NN queries of pm_knn, the single-kernel frame render
+// (eye rays, specular chains, volume march; one warp per pixel), the batched
+// multi-scene render, and the k-NN estimates of query lists. The warp k-NN
+// search and the estimate sum live in knn_core.cuh.
 #include "launch_count.cuh"
 
 #include <atomic>
 #include "cache.cuh"
 #include "eye_path.cuh"
+#include "knn_core.cuh"
 
 namespace pm {
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-constexpr int kStackCap = 192;     // 32 entries per wide level, 6 levels: depth <= 29
 constexpr int kWarpsPerBlock = 4;
-
-
-// Per-warp shared memory: the traversal stack and the staging areas of the
-// bulk merge (the k-list and the sorted leaf candidates).
-struct WarpScratch {
-    uint32_t st_node[kStackCap];
-    float st_d2[kStackCap];
-    uint64_t lk[128];
-    uint32_t la[128];
-    uint64_t ck[32];
-    uint32_t ca[32];
-};
-
-
-__device__ __forceinline__ uint64_t make_key(float d2, uint32_t idx) {
-    return ((uint64_t)__float_as_uint(d2) << 32) | idx;
-}
-__device__ __forceinline__ float key_d2(uint64_t k) { return __uint_as_float((uint32_t)(k >> 32)); }
-
-template <int S>
-struct Knn {
-    uint64_t key[S];
-    uint32_t at[S];  // tree position of the record
-    uint64_t worst;
-    int k;
-
-    __device__ __forceinline__ void reset(uint64_t cap, int kk) {
-        k = kk;
-#pragma unroll
-        for (int s = 0; s < S; ++s) { key[s] = cap; at[s] = 0xffffffffu; }
-        worst = cap;
-    }
-    __device__ __forceinline__ void update_worst() {
-        const int kl = (k - 1) / S, ks = (k - 1) % S;
-        uint64_t w = key[0];
-#pragma unroll
-        for (int s = 1; s < S; ++s)
-            if (s == ks) w = key[s];
-        worst = __shfl_sync(kFull, w, kl);
-    }
-    // Inserts x (< worst) keeping the list sorted.
-    __device__ __forceinline__ void insert(uint64_t x, uint32_t xa, int lane) {
-        uint64_t pk = __shfl_up_sync(kFull, key[S - 1], 1);
-        uint32_t pa = __shfl_up_sync(kFull, at[S - 1], 1);
-#pragma unroll
-        for (int s = S - 1; s >= 0; --s) {
-            uint64_t below = s > 0 ? key[s - 1] : pk;
-            uint32_t below_at = s > 0 ? at[s - 1] : pa;
-            bool first = (s == 0) && (lane == 0);
-            if (key[s] >= x) {
-                if (first || below < x) { key[s] = x; at[s] = xa; }
-                else { key[s] = below; at[s] = below_at; }
-            }
-        }
-        update_worst();
-    }
-    // Merges the candidates of the lanes in `mask` (each lane's `x` / `xa`,
-    // all below worst) into the list at once: every list entry moves up by
-    // the number of candidates below it, every candidate lands at its rank
-    // among the candidates plus the number of list entries below it. Keys
-    // are unique (photon indices), so the new positions are a permutation.
-    __device__ __forceinline__ void merge(uint64_t x, uint32_t xa, unsigned mask, int lane,
-                                          WarpScratch &w) {
-        constexpr int K = 32 * S;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            w.lk[lane * S + s] = key[s];
-            w.la[lane * S + s] = at[s];
-        }
-        const int n = __popc(mask);
-        int rc = 0;
-        for (unsigned mm = mask; mm; mm &= mm - 1) {
-            const int j = __ffs(mm) - 1;
-            rc += __shfl_sync(kFull, x, j) < x ? 1 : 0;
-        }
-        if ((mask >> lane) & 1u) {
-            w.ck[rc] = x;
-            w.ca[rc] = xa;
-        }
-        __syncwarp();
-        int lpos[S];
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            int lo = 0, hi = n;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (w.ck[mid] < key[s]) lo = mid + 1; else hi = mid;
-            }
-            lpos[s] = lane * S + s + lo;
-        }
-        int cpos = K;
-        uint64_t cv = 0;
-        uint32_t cav = 0;
-        if (lane < n) {
-            cv = w.ck[lane];
-            cav = w.ca[lane];
-            int lo = 0, hi = K;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (w.lk[mid] < cv) lo = mid + 1; else hi = mid;
-            }
-            cpos = lane + lo;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-            if (lpos[s] < K) {
-                w.lk[lpos[s]] = key[s];
-                w.la[lpos[s]] = at[s];
-            }
-        if (cpos < K) {
-            w.lk[cpos] = cv;
-            w.la[cpos] = cav;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            key[s] = w.lk[lane * S + s];
-            at[s] = w.la[lane * S + s];
-        }
-        __syncwarp();
-        update_worst();
-    }
-};
-
-__device__ __forceinline__ float box_d2(float4 lo, float4 hi, v3 q) {
-    float dx = fmaxf(fmaxf(lo.x - q.x, q.x - hi.x), 0.0f);
-    float dy = fmaxf(fmaxf(lo.y - q.y, q.y - hi.y), 0.0f);
-    float dz = fmaxf(fmaxf(lo.z - q.z, q.z - hi.z), 0.0f);
-    return dx * dx + dy * dy + dz * dz;
-}
-
-// Sorts lk/la[0..P) ascending by key (bitonic network over shared memory);
-// P is a power of two in [32, 128].
-__device__ __forceinline__ void warp_sort_smem(WarpScratch &w, int P, int lane) {
-    for (int size = 2; size <= P; size <<= 1) {
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < (P >> 1); t += 32) {
-                // pair (i, i + stride) of the t-th compare-exchange (stride is
-                // a power of two: no division)
-                const int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
-                const int j = i + stride;
-                const bool up = (i & size) == 0;
-                const uint64_t a = w.lk[i], b = w.lk[j];
-                if ((a > b) == up) {
-                    w.lk[i] = b;
-                    w.lk[j] = a;
-                    const uint32_t x = w.la[i];
-                    w.la[i] = w.la[j];
-                    w.la[j] = x;
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
-// Sorts the `count` collected candidates (count <= 128) in lk/la and loads
-// the first 32*S of them into the k-list; empty slots hold cap.
-template <int S>
-__device__ __forceinline__ void load_sorted(Knn<S> &kn, WarpScratch &w, int count, uint64_t cap,
-                                            int lane) {
-    int P = 32;
-    while (P < count) P <<= 1;
-    for (int i = count + lane; i < P; i += 32) {
-        w.lk[i] = cap;
-        w.la[i] = 0xffffffffu;
-    }
-    __syncwarp();
-    warp_sort_smem(w, P, lane);
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const int j = lane * S + s;
-        kn.key[s] = j < P ? w.lk[j] : cap;
-        kn.at[s] = j < P ? w.la[j] : 0xffffffffu;
-    }
-    __syncwarp();
-    kn.update_worst();
-}
-
-// k nearest records of q, sorted by (squared distance, index), within the
-// radius cap held in kn.worst at entry. The walk starts in collect mode:
-// every record within the cap is appended to a shared buffer, children are
-// pushed in any order and nothing is kept sorted. If more than 128 records
-// turn up, the buffer is sorted into the k-list and the walk continues in
-// list mode, pruning with the current k-th distance and inserting (bulk
-// merge or one at a time). A walk that stays in collect mode sorts its
-// buffer once at the end. A warm walk (the next sample of a march) starts
-// in list mode from the re-scored previous list and skips the records the
-// list already holds. All modes produce the same exact list.
-template <int S>
-__device__ void knn_search(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, int lane,
-                           uint64_t cap, bool warm = false, KnnTune tune = KnnTune()) {
-    if (m.n == 0) return;
-    const int collect_max = tune.collect_max;
-    uint32_t *st_node = ws.st_node;
-    float *st_d2 = ws.st_d2;
-    const uint32_t first_leaf = 1u << m.depth;
-    const int chunks = 1 << m.leaf_shift;
-    bool collect = !warm;
-    int count = 0;
-    int top = 1;
-    if (lane == 0) { st_node[0] = 1u; st_d2[0] = 0.0f; }
-    __syncwarp();
-    while (top > 0) {
-        --top;
-        const uint32_t node = st_node[top];
-        const float nd2 = st_d2[top];
-        __syncwarp();
-        const float wd2 = key_d2(kn.worst);
-        if (nd2 > wd2) continue;
-        const int dn = 31 - __clz(node);
-        if (dn == m.depth) {
-            // a leaf: 32 << leaf_shift records, 32 at a time
-            for (int c = 0; c < chunks; ++c) {
-                const uint32_t base = ((node - first_leaf) << (5 + m.leaf_shift)) + ((uint32_t)c << 5);
-                const uint32_t r = base + lane;
-                uint64_t key = ~0ull;
-                if (r < m.n) {
-                    float4 p = __ldg(&m.pos[r]);
-                    float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                    key = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
-                }
-                unsigned mask = __ballot_sync(kFull, key < kn.worst);
-                if (!mask) continue;
-                if (warm) {
-                    // drop records the list already holds: list entries carry
-                    // their tree positions, so the chunk's duplicates are one
-                    // OR over the warp of the entries that fall in it
-                    unsigned held = 0u;
-#pragma unroll
-                    for (int t = 0; t < S; ++t)
-                        if ((kn.at[t] >> 5) == (base >> 5)) held |= 1u << (kn.at[t] & 31u);
-                    mask &= ~__reduce_or_sync(kFull, held);
-                    if (!mask) continue;
-                }
-                if (collect) {
-                    const int add = __popc(mask);
-                    if (count + add <= collect_max) {
-                        if ((mask >> lane) & 1u) {
-                            const int at = count + __popc(mask & ((1u << lane) - 1u));
-                            ws.lk[at] = key;
-                            ws.la[at] = r;
-                        }
-                        count += add;
-                        __syncwarp();
-                        continue;
-                    }
-                    load_sorted<S>(kn, ws, count, cap, lane);
-                    collect = false;
-                    mask = __ballot_sync(kFull, key < kn.worst);
-                }
-                if (__popc(mask) >= tune.merge_min) {
-                    kn.merge(key, r, mask, lane, ws);
-                } else {
-                    while (mask) {
-                        const int src = __ffs(mask) - 1;
-                        uint64_t x = __shfl_sync(kFull, key, src);
-                        kn.insert(x, base + src, lane);
-                        mask &= mask - 1;
-                        mask &= __ballot_sync(kFull, key < kn.worst);
-                    }
-                }
-            }
-        } else {
-            int w = (m.depth - dn) % 5;
-            if (w == 0) w = 5;
-            const int nc = 1 << w;
-            const uint32_t child = (node << w) + lane;
-            float bd2 = __int_as_float(0x7f800000);
-            if (lane < nc) bd2 = box_d2(__ldg(&m.lo[child]), __ldg(&m.hi[child]), q);
-            const bool ok = (lane < nc) && (bd2 <= wd2);
-            const unsigned mask = __ballot_sync(kFull, ok);
-            int rank;
-            if (collect || warm) {
-                // any order: collect mode sorts at the end, and a warm start
-                // already holds a tight k-th distance
-                rank = __popc(mask & ((1u << lane) - 1u));
-            } else {
-                // far-to-near: survivors farther than this lane (ties: higher lane farther)
-                rank = 0;
-                for (unsigned mm = mask; mm; mm &= mm - 1) {
-                    const int j = __ffs(mm) - 1;
-                    float o = __shfl_sync(kFull, bd2, j);
-                    rank += (o > bd2 || (o == bd2 && j > lane)) ? 1 : 0;
-                }
-            }
-            if (ok && top + rank < kStackCap) {
-                st_node[top + rank] = child;
-                st_d2[top + rank] = bd2;
-            }
-            top = min(top + __popc(mask), kStackCap);
-            __syncwarp();
-        }
-    }
-    if (collect) load_sorted<S>(kn, ws, count, cap, lane);
-}
-
-// Warm start for the next sample of a march: the list of the previous
-// sample, re-scored at q (entries beyond the cap dropped) and sorted. The
-// search that follows only has to find records closer than its k-th entry.
-template <int S>
-__device__ void rescore(const MapView &m, v3 q, Knn<S> &kn, WarpScratch &ws, uint64_t cap,
-                        int lane) {
-    constexpr int K = 32 * S;
-    constexpr int P = K <= 32 ? 32 : (K <= 64 ? 64 : 128);
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const int j = lane * S + s;
-        uint64_t nk = cap;
-        uint32_t na = 0xffffffffu;
-        if (kn.at[s] != 0xffffffffu) {
-            const float4 p = __ldg(&m.pos[kn.at[s]]);
-            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-            const uint64_t k2 = make_key(dx * dx + dy * dy + dz * dz, __float_as_uint(p.w));
-            if (k2 < cap) {
-                nk = k2;
-                na = kn.at[s];
-            }
-        }
-        ws.lk[j] = nk;
-        ws.la[j] = na;
-    }
-    for (int i = K + lane; i < P; i += 32) {
-        ws.lk[i] = cap;
-        ws.la[i] = 0xffffffffu;
-    }
-    __syncwarp();
-    warp_sort_smem(ws, P, lane);
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        kn.key[s] = ws.lk[lane * S + s];
-        kn.at[s] = ws.la[lane * S + s];
-    }
-    __syncwarp();
-    kn.update_worst();
-}
-
-// Kahan sum within a lane, then a compensated butterfly across the warp:
-// every lane ends with the same value.
-__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
-    float y = x - comp;
-    float t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-}
-__device__ __forceinline__ float warp_csum(float sum, float comp) {
-    float s = sum, e = -comp;
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-        float s2 = __shfl_xor_sync(kFull, s, off);
-        float e2 = __shfl_xor_sync(kFull, e, off);
-        float t = s + s2;
-        float bb = t - s;
-        float err = (s - (t - bb)) + (s2 - bb);
-        e = (e + e2) + err;
-        s = t;
-    }
-    return s + e;
-}
-
-// Radiance-estimate numerator: sum of photon flux times weight over the
-// k-NN list. mode 0: surface (weight 1 for photons arriving on the side nf
-// faces, else 0); mode 1: volume (HG phase toward wo). Returns found count
-// and the squared radius in *r2.
-template <int S>
-__device__ v3 flux_sum(const Knn<S> &kn, const MapView &m, int lane, int mode, v3 dirv, float g,
-                       uint64_t cap, float r2cap, int *found, float *r2) {
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    int cnt = 0;
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const int j = lane * S + s;
-        if (j < kn.k && kn.key[s] != cap) {
-            ++cnt;
-            float4 pw = __ldg(&m.pow[kn.at[s]]);
-            v3 dir = oct_decode(__float_as_uint(pw.w));
-            float w;
-            if (mode == 0) w = dot(dirv, dir) < 0.0f ? 1.0f : 0.0f;
-            else w = hg_phase(g, dot(dir, dirv));
-            kahan_add(sx, cx, pw.x * w);
-            kahan_add(sy, cy, pw.y * w);
-            kahan_add(sz, cz, pw.z * w);
-        }
-    }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) cnt += __shfl_xor_sync(kFull, cnt, off);
-    *found = cnt;
-    *r2 = cnt == kn.k ? key_d2(kn.worst) : r2cap;
-    return mk3(warp_csum(sx, cx), warp_csum(sy, cy), warp_csum(sz, cz));
-}
+using namespace wknn;
 
 template <int S>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) knn_kernel(MapView m, const float4 *q,

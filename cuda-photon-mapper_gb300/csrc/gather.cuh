@@ -8,6 +8,7 @@ namespace pm {
 struct MapView {
     const float4 *pos;   // xyz + record index bits
     const float4 *pow;   // rgb flux + octahedral direction bits
+    const float4 *dir;   // the decoded directions (xyz)
     const float4 *lo, *hi;
     uint32_t n;
     int depth;

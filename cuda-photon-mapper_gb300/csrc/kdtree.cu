@@ -98,12 +98,19 @@ __global__ void iota_kernel(uint32_t *v, uint32_t n) {
 
 __global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
                                const float4 *__restrict__ pos_in, const float4 *__restrict__ pow_in,
-                               float4 *pos_out, float4 *pow_out) {
+                               float4 *pos_out, float4 *pow_out, float4 *dir_out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t s = order[i];
     pos_out[i] = pos_in[s];
-    if (pow_in) pow_out[i] = pow_in[s];
+    if (pow_in) {
+        const float4 pw = pow_in[s];
+        pow_out[i] = pw;
+        if (dir_out) {
+            const v3 d = oct_decode(__float_as_uint(pw.w));
+            dir_out[i] = make_float4(d.x, d.y, d.z, 0.0f);
+        }
+    }
 }
 
 // One warp per leaf slot: box of its (up to) 32 << leaf_shift records.
@@ -208,7 +215,8 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         split_cell_kernel<<<(nodes + 255) / 256, 256, 0, s>>>(a.pos_in, va, n, l, span, nodes,
                                                                a.node_lo, a.node_hi); note_launch();
     }
-    permute_kernel<<<blocks, 256, 0, s>>>(va, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out); note_launch();
+    permute_kernel<<<blocks, 256, 0, s>>>(va, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out, a.dir_out);
+    note_launch();
     const uint32_t first_leaf = 1u << D;
     leaf_box_kernel<<<(first_leaf * 32 + 255) / 256, 256, 0, s>>>(a.pos_out, n, first_leaf, first_leaf,
                                                                  a.leaf_shift, a.node_lo, a.node_hi);

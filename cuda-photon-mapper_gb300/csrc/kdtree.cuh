@@ -17,6 +17,7 @@ struct KdBuildArgs {
     const float *box_dev;       // nullable: root cell read from device memory (6 floats)
     const float4 *pos_in, *pow_in;   // records in index order (pow_in nullable)
     float4 *pos_out, *pow_out;       // records in tree order (pow_out nullable)
+    float4 *dir_out = nullptr;       // nullable: decoded directions (xyz) in tree order
     float4 *node_lo, *node_hi;       // tree_nodes(n) boxes
     uint64_t *keys, *keys_tmp;       // n each
     uint32_t *vals, *vals_tmp;       // n each

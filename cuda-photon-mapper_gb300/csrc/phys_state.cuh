@@ -27,6 +27,10 @@ struct QueryList {
     bool sorted = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float ms_build = 0.0f;
+    unsigned long long *gather_stats = nullptr;  // counters of the last estimate pass
+    float *anchor_d = nullptr;                   // per warp chunk of the estimate pass
+    uint32_t *defer_n = nullptr;
+    uint32_t anchor_cap = 0;
 };
 
 struct PhysicalState {
@@ -42,6 +46,7 @@ struct PhysicalState {
     uint32_t *words = nullptr;  // [0] path counter [1] stored_s [2] stored_v [3] total [4..7] extents
     struct Map {
         float4 *pos = nullptr, *pow = nullptr, *tpos = nullptr, *tpow = nullptr;
+        float4 *tdir = nullptr;  // decoded directions in tree order
         float4 *lo = nullptr, *hi = nullptr;
         uint32_t cap = 0, n = 0, paths = 0;
         int depth = 0;
@@ -69,6 +74,7 @@ inline MapView view_of(const PhysicalState::Map &m) {
     MapView v;
     v.pos = m.tpos;
     v.pow = m.tpow;
+    v.dir = m.tdir;
     v.lo = m.lo;
     v.hi = m.hi;
     v.n = m.built ? m.n : 0;
@@ -88,6 +94,23 @@ void query_list_free(QueryList &ql);
 // Exact k-NN values of every query, raw (flux sum, squared radius or -1),
 // into ql.val: the list in spatial order, warm-started runs of queries.
 cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s);
+constexpr int kGatherStats = 7;
+// Scratch of knn_values_tiles: anchor_d[tile_chunks(n)], defer[n], one
+// defer_n word; stats: kGatherStats counters added (nullable).
+struct TileBuffers {
+    float *anchor_d;
+    uint32_t *defer;
+    uint32_t *defer_n;
+    unsigned long long *stats;
+};
+uint32_t tile_chunks(uint32_t n);
+// k-NN estimates of the queries in spatial order (order[0..n) indexes qa/qd
+// and val), one shared candidate set per group of neighbours
+// (tile_gather.cu); raw as cache_knn_values_runs.
+cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView &vol,
+                             const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
+                             int k, float radius, bool raw, float4 *val, const TileBuffers &buf,
+                             int sm_count, cudaStream_t s);
 
 // The render parameters pm_render passes for the installed configuration.
 inline RenderParams render_params(const PhysicalState *st) {

@@ -35,7 +35,7 @@ void free_state(PhysicalState *st) {
     cudaFree(st->scan_tmp);
     cudaFree(st->words);
     for (auto &m : st->map) {
-        cudaFree(m.pos); cudaFree(m.pow); cudaFree(m.tpos); cudaFree(m.tpow);
+        cudaFree(m.pos); cudaFree(m.pow); cudaFree(m.tpos); cudaFree(m.tpow); cudaFree(m.tdir);
         cudaFree(m.lo); cudaFree(m.hi);
     }
     cudaFree(st->keys); cudaFree(st->keys_tmp); cudaFree(st->vals); cudaFree(st->vals_tmp);
@@ -102,6 +102,7 @@ pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg)
         PM_TRY(dalloc(&mp.pow, mp.cap));
         PM_TRY(dalloc(&mp.tpos, mp.cap));
         PM_TRY(dalloc(&mp.tpow, mp.cap));
+        PM_TRY(dalloc(&mp.tdir, mp.cap));
         PM_TRY(dalloc(&mp.lo, tree_nodes(mp.cap)));
         PM_TRY(dalloc(&mp.hi, tree_nodes(mp.cap)));
     }
@@ -235,6 +236,7 @@ pm_status pm_build(pm_ctx *ctx, cudaStream_t stream) {
         a.pow_in = mp.pow;
         a.pos_out = mp.tpos;
         a.pow_out = mp.tpow;
+        a.dir_out = mp.tdir;
         a.node_lo = mp.lo;
         a.node_hi = mp.hi;
         a.keys = st->keys; a.keys_tmp = st->keys_tmp;
@@ -362,6 +364,20 @@ pm_status pm_get_photons(pm_ctx *ctx, int map, pm_photon_record *out, uint32_t c
     return PM_OK;
 }
 
+pm_status pm_get_gather_stats(pm_ctx *ctx, uint64_t *out, int n) {
+    if (!ctx || !out || n < 0 || n > kGatherStats) return PM_ERR_INVALID;
+    PhysicalState *st = ctx->phys;
+    if (!st || !st->ql.gather_stats || !st->gathers_on_host)
+        return fail(ctx, PM_ERR_STATE, "pm_get_gather_stats before a pm_render");
+    DeviceGuard g(ctx->device);
+    cudaError_t e;
+    unsigned long long c[kGatherStats];
+    PM_TRY(cudaEventSynchronize(st->ev[5]));
+    PM_TRY(cudaMemcpy(c, st->ql.gather_stats, sizeof(c), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) out[i] = c[i];
+    return PM_OK;
+}
+
 pm_status pm_get_stats(pm_ctx *ctx, pm_frame_stats *out) {
     if (!ctx || !out) return PM_ERR_INVALID;
     PhysicalState *st = ctx->phys;
@@ -400,13 +416,13 @@ pm_status pm_set_photons(pm_ctx *ctx, int map, const float4 *pos, const float4 *
     auto &mp = st->map[map];
     PM_TRY(cudaDeviceSynchronize());
     if (n > mp.cap) {
-        cudaFree(mp.pos); cudaFree(mp.pow); cudaFree(mp.tpos); cudaFree(mp.tpow);
+        cudaFree(mp.pos); cudaFree(mp.pow); cudaFree(mp.tpos); cudaFree(mp.tpow); cudaFree(mp.tdir);
         cudaFree(mp.lo); cudaFree(mp.hi);
         const int ls = mp.leaf_shift;
         mp = PhysicalState::Map();
         mp.leaf_shift = ls;
         PM_TRY(dalloc(&mp.pos, n)); PM_TRY(dalloc(&mp.pow, n));
-        PM_TRY(dalloc(&mp.tpos, n)); PM_TRY(dalloc(&mp.tpow, n));
+        PM_TRY(dalloc(&mp.tpos, n)); PM_TRY(dalloc(&mp.tpow, n)); PM_TRY(dalloc(&mp.tdir, n));
         PM_TRY(dalloc(&mp.lo, tree_nodes(n))); PM_TRY(dalloc(&mp.hi, tree_nodes(n)));
         mp.cap = n;
         if (n > st->sort_cap) {

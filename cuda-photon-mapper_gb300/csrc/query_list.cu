@@ -10,8 +10,6 @@
 namespace pm {
 namespace {
 
-constexpr int kQueryRun = 32;  // queries per warp, each warm-started from the previous one
-
 template <typename T>
 cudaError_t dalloc(T **p, size_t count) {
     *p = nullptr;
@@ -25,7 +23,8 @@ void query_list_free(QueryList &ql) {
     cudaFree(ql.cnt); cudaFree(ql.off); cudaFree(ql.scnt); cudaFree(ql.soff); cudaFree(ql.slist);
     cudaFree(ql.scan_tmp); cudaFree(ql.qa); cudaFree(ql.qd); cudaFree(ql.val);
     cudaFree(ql.key); cudaFree(ql.ord); cudaFree(ql.key_tmp); cudaFree(ql.ord_tmp);
-    cudaFree(ql.hist); cudaFree(ql.n_dev);
+    cudaFree(ql.hist); cudaFree(ql.n_dev); cudaFree(ql.gather_stats);
+    cudaFree(ql.anchor_d); cudaFree(ql.defer_n);
     if (ql.ev0) cudaEventDestroy(ql.ev0);
     if (ql.ev1) cudaEventDestroy(ql.ev1);
     ql = QueryList();
@@ -130,9 +129,22 @@ cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s) {
     QueryList &ql = st->ql;
     cudaError_t e;
     QL_TRY(query_list_sort(st, s));
-    QL_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), ql.qa, ql.qd,
-                                 nullptr, ql.order, ql.nq, kQueryRun, st->cfg.k, st->cfg.radius, true,
-                                 ql.val, s));
+    if (!ql.gather_stats) {
+        QL_TRY(dalloc(&ql.gather_stats, kGatherStats));
+        QL_TRY(dalloc(&ql.defer_n, 1));
+    }
+    if (tile_chunks(ql.nq) > ql.anchor_cap) {
+        cudaFree(ql.anchor_d);
+        ql.anchor_d = nullptr;
+        ql.anchor_cap = 0;
+        QL_TRY(dalloc(&ql.anchor_d, tile_chunks(ql.qcap)));
+        ql.anchor_cap = tile_chunks(ql.qcap);
+    }
+    QL_TRY(cudaMemsetAsync(ql.gather_stats, 0, sizeof(unsigned long long) * kGatherStats, s));
+    // the sort's other index array is free again: the deferred-query list
+    const TileBuffers buf{ql.anchor_d, ql.order == ql.ord ? ql.ord_tmp : ql.ord, ql.defer_n, ql.gather_stats};
+    QL_TRY(knn_values_tiles(st->dscene, view_of(st->map[0]), view_of(st->map[1]), ql.qa, ql.qd, ql.order,
+                            ql.nq, st->cfg.k, st->cfg.radius, true, ql.val, buf, st->sm_count, s));
 #undef QL_TRY
     return cudaSuccess;
 }

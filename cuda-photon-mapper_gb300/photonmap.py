@@ -135,6 +135,7 @@ PROTOTYPES = {
     "pm_build": (_i, [_vp, _vp]),
     "pm_render": (_i, [_vp, _vp, _vp, _vp]),
     "pm_render_single_kernel": (_i, [_vp, _vp, _vp, _vp]),
+    "pm_get_gather_stats": (_i, [_vp, _vp, _i]),
     "pm_knn": (_i, [_vp, _i, _vp, _c.c_uint32, _i, _f, _vp, _vp, _vp]),
     "pm_radius_gather": (_i, [_vp, _i, _vp, _vp, _c.c_uint32, _f, _f, _vp, _vp]),
     "pm_get_photons": (_i, [_vp, _i, _vp, _c.c_uint32, _c.POINTER(_c.c_uint32)]),
@@ -285,6 +286,13 @@ class Context:
 
     def render(self, radiance=None, rgba=None, stream=0):
         self._check(self.lib.pm_render(self.h, radiance, rgba, stream), "pm_render")
+
+    def gather_stats(self):
+        """Counters of the last render's k-NN estimates (pm_get_gather_stats)."""
+        out = (_c.c_uint64 * 7)()
+        self._check(self.lib.pm_get_gather_stats(self.h, out, 7), "pm_get_gather_stats")
+        names = ("tiled", "list", "shrunk", "violations", "groups", "candidates", "halvings")
+        return dict(zip(names, [int(v) for v in out]))
 
     def render_single_kernel(self, radiance=None, rgba=None, stream=0):
         self._check(self.lib.pm_render_single_kernel(self.h, radiance, rgba, stream),

@@ -215,11 +215,20 @@ PM_API pm_status pm_render(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, cudaStre
  * path, each k-NN warm-started from the previous march sample), without the
  * query list: no host synchronisation, slower on large frames. pm_render
  * builds the frame's query list (one stream synchronisation to size it),
- * estimates the queries in spatial order -- each warm-started from its
- * neighbour -- and sums them per pixel with this kernel's arithmetic, so the
- * two are bit-identical. */
+ * estimates the queries in spatial order from one shared candidate set per
+ * group of 32 neighbours, and sums them per pixel with this kernel's
+ * arithmetic; the k-NN sets are exact and the estimate sum is independent
+ * of the order of the records, so the two are bit-identical. */
 PM_API pm_status pm_render_single_kernel(pm_ctx *ctx, float4 *radiance, uchar4 *rgba,
                                          cudaStream_t stream);
+/* Counters of the last pm_render's k-NN estimates (n <= 7 of them):
+ * [0] queries estimated from a shared candidate set, [1] by the list
+ * search, [2] single queries whose radius was narrowed to fit their set,
+ * [3] results that contradicted their upper bound and were redone by the
+ * list search (0 while the bounds hold), [4] candidate sets collected,
+ * [5] candidates collected, [6] segments halved because their set did not
+ * fit in shared memory. */
+PM_API pm_status pm_get_gather_stats(pm_ctx *ctx, uint64_t *out, int n);
 /* k nearest photons of map `map` for nq query points (device float4
  * xyz), within radius; idx_out / d2_out (device, nq*k) receive photon
  * indices and squared distances sorted by (distance, index); missing

@@ -89,6 +89,8 @@ def _phys_protos(lib):
     vp, u32, i, f = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_float
     lib.pmo_emit.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.pmo_emit.restype = i
+    lib.pmo_fixed_sum.argtypes = [vp, i]
+    lib.pmo_fixed_sum.restype = f
     lib.pmo_knn.argtypes = [vp, u32, vp, u32, i, f, vp, vp]
     lib.pmo_knn.restype = None
     lib.pmo_render.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp]
@@ -176,6 +178,12 @@ def emit(scene, cfg, het=None, double=False):
        vpos.ctypes.data, vpow.ctypes.data, sizes.ctypes.data, paths.ctypes.data)
     return PhysicalMaps(spos[:sizes[0]], spow[:sizes[0]], vpos[:sizes[1]], vpow[:sizes[1]], sizes,
                         paths)
+
+
+def fixed_sum(terms):
+    """The estimate sum of non-negative float32 terms (order-independent)."""
+    t = np.ascontiguousarray(terms, np.float32)
+    return np.float32(phys_lib().pmo_fixed_sum(t.ctypes.data, len(t)))
 
 
 def knn(pos, queries, k, radius):

@@ -522,56 +522,58 @@ void pmo_knn(const float (*pos)[4], uint32_t n, const float (*queries)[4], uint3
 
 /* ---- radiance estimate (GPU: gather.cu flux_sum) ------------------------ */
 
-static void kahan_add(float *sum, float *comp, float x) {
-    float y = x - *comp;
-    float t = *sum + y;
-    *comp = (t - *sum) - y;
-    *sum = t;
+/* Order-independent sum of non-negative float terms (GPU: knn_core.cuh
+ * warp_fixed_sum). With E the largest exponent field of the terms (at least
+ * 1), each term becomes floor(t * 2^(182 - E)): its 24-bit significand
+ * shifted left by 32 - (E - e) bits, or right (truncating) when that is
+ * negative. The integers add exactly in 64 bits and the total times
+ * 2^(E - 182) is rounded to float once (nearest even); the power-of-two
+ * scale is split in two steps when it is below 2^-126. */
+static float scale_pow2(float f, int n) {
+    if (n < -126) {
+        f *= u2f((uint32_t)(127 - 64) << 23);
+        n += 64;
+    }
+    return f * u2f((uint32_t)(n + 127) << 23);
 }
 
-/* The GPU's summation tree: lane l sums list positions l*S..l*S+S-1 with
- * Kahan compensation, then lanes combine pairwise at distances 16, 8, 4, 2,
- * 1 with an exact two-sum. */
-static float warp_csum(const float *sum, const float *comp) {
-    float s[32], e[32], s2[32], e2[32];
-    for (int l = 0; l < 32; ++l) { s[l] = sum[l]; e[l] = -comp[l]; }
-    for (int off = 16; off; off >>= 1) {
-        for (int l = 0; l < 32; ++l) {
-            float a = s[l], b = s[l ^ off];
-            float t = a + b;
-            float bb = t - a;
-            float err = (a - (t - bb)) + (b - bb);
-            e2[l] = (e[l] + e[l ^ off]) + err;
-            s2[l] = t;
-        }
-        memcpy(s, s2, sizeof(s));
-        memcpy(e, e2, sizeof(e));
+static float fixed_sum(const float *t, int n) {
+    uint32_t emax = 1;
+    for (int i = 0; i < n; ++i) {
+        const uint32_t e = f2u(t[i]) >> 23;
+        if (e > emax) emax = e;
     }
-    return s[0] + e[0];
+    uint64_t acc = 0;
+    for (int i = 0; i < n; ++i) {
+        const uint32_t b = f2u(t[i]);
+        const uint32_t e = b >> 23;
+        const uint32_t m = (b & 0x7fffffu) | (e ? 0x800000u : 0u);
+        const int sh = 32 - (int)(emax - (e ? e : 1u));
+        if (sh >= 0) acc += (uint64_t)m << sh;
+        else if (sh > -24) acc += (uint64_t)(m >> -sh);
+    }
+    return scale_pow2((float)acc, (int)emax - 182);
 }
+
+float pmo_fixed_sum(const float *t, int n) { return fixed_sum(t, n); }
 
 static v3 flux_sum(const uint64_t *keys, int cnt, int k, const float (*pow)[4], int mode, v3 dirv,
                    float g, float r2cap, int *found, float *r2) {
-    const int S = (k + 31) / 32;
-    float sx[32], sy[32], sz[32], cx[32], cy[32], cz[32];
-    for (int l = 0; l < 32; ++l) { sx[l] = sy[l] = sz[l] = cx[l] = cy[l] = cz[l] = 0.0f; }
-    for (int l = 0; l < 32; ++l)
-        for (int s = 0; s < S; ++s) {
-            int j = l * S + s;
-            if (j < k && j < cnt) {
-                const float *pw = pow[(uint32_t)keys[j]];
-                v3 dir = oct_decode(f2u(pw[3]));
-                float w;
-                if (mode == 0) w = dot3(dirv, dir) < 0.0f ? 1.0f : 0.0f;
-                else w = hg_phase(g, dot3(dir, dirv));
-                kahan_add(&sx[l], &cx[l], pw[0] * w);
-                kahan_add(&sy[l], &cy[l], pw[1] * w);
-                kahan_add(&sz[l], &cz[l], pw[2] * w);
-            }
-        }
+    float tx[128], ty[128], tz[128];
+    const int n = cnt < k ? cnt : k;
+    for (int j = 0; j < n; ++j) {
+        const float *pw = pow[(uint32_t)keys[j]];
+        v3 dir = oct_decode(f2u(pw[3]));
+        float w;
+        if (mode == 0) w = dot3(dirv, dir) < 0.0f ? 1.0f : 0.0f;
+        else w = hg_phase(g, dot3(dir, dirv));
+        tx[j] = pw[0] * w;
+        ty[j] = pw[1] * w;
+        tz[j] = pw[2] * w;
+    }
     *found = cnt;
     *r2 = cnt == k ? u2f((uint32_t)(keys[k - 1] >> 32)) : r2cap;
-    return mk(warp_csum(sx, cx), warp_csum(sy, cy), warp_csum(sz, cz));
+    return mk(fixed_sum(tx, n), fixed_sum(ty, n), fixed_sum(tz, n));
 }
 
 /* ---- render (GPU: gather.cu render_kernel) ------------------------------ */

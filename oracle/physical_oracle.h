@@ -66,6 +66,8 @@ int pmo_emit(const pmo_scene *scene, const pmo_config *cfg, const float *het, fl
 pmo_grid *pmo_grid_build(const float (*pos)[4], uint32_t n, float radius);
 void pmo_grid_free(pmo_grid *g);
 int pmo_grid_knn(const pmo_grid *g, const float q[3], int k, float r2, uint64_t *keys);
+/* The estimate sum: order-independent fixed-point sum of n >= 0 float terms. */
+float pmo_fixed_sum(const float *t, int n);
 void pmo_knn(const float (*pos)[4], uint32_t n, const float (*queries)[4], uint32_t nq, int k,
              float radius, uint32_t *idx_out, float *d2_out);
 void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,

@@ -162,13 +162,17 @@ def test_render_bit_exact(ctx, preset, size):
     assert st.surface_gathers > 0 and st.volume_gathers > 0
 
 
-@pytest.mark.parametrize("preset,size,k", [(1, (48, 40), None), (2, (64, 48), None),
-                                           (3, (64, 36), None), (2, (40, 30), 1), (3, (40, 30), 64)])
-def test_query_list_render_equals_single_kernel(ctx, preset, size, k):
-    """pm_render (query list, queries in spatial order) and
-    pm_render_single_kernel (warp-per-pixel march) give the same bits, the
-    same 8-bit image and the same gather counts."""
-    sc, cf = small(preset, 20000, 20000, size, k=k)
+@pytest.mark.parametrize("preset,size,k,radius,photons", [
+    (1, (48, 40), None, None, 20000), (2, (64, 48), None, None, 20000),
+    (3, (64, 36), None, None, 20000), (2, (40, 30), 1, None, 20000), (3, (40, 30), 64, None, 20000),
+    (2, (48, 40), 100, 0.02, 20000),   # the radius cap binds: fewer than k found
+    (2, (40, 30), 32, None, 300),      # tiny maps
+    (2, (96, 72), 100, None, 60000)])
+def test_query_list_render_equals_single_kernel(ctx, preset, size, k, radius, photons):
+    """pm_render (query list in spatial order, shared candidate sets) and
+    pm_render_single_kernel (warp-per-pixel march with the list search)
+    give the same bits, the same 8-bit image and the same gather counts."""
+    sc, cf = small(preset, photons, photons, size, k=k, radius=radius)
     rad, rgba = gpu_frame(ctx, sc, cf)
     st = ctx.stats()
     rad1 = torch.zeros_like(torch.from_numpy(rad)).cuda()
@@ -180,6 +184,19 @@ def test_query_list_render_equals_single_kernel(ctx, preset, size, k):
     st1 = ctx.stats()
     assert (st1.surface_gathers, st1.volume_gathers) == (st.surface_gathers, st.volume_gathers)
     assert st.surface_gathers > 0
+
+
+def test_gather_stats_of_the_shared_candidate_sets(ctx):
+    """The k-NN estimates of a frame mostly come from shared candidate
+    sets, and no result contradicts its distance bound."""
+    sc, cf = small(2, 100000, 100000, (128, 96))
+    gpu_frame(ctx, sc, cf)
+    g = ctx.gather_stats()
+    st = ctx.stats()
+    assert g["tiled"] + g["list"] == st.surface_gathers + st.volume_gathers
+    assert g["violations"] == 0
+    assert g["tiled"] > 0.9 * (g["tiled"] + g["list"]), g
+    assert g["groups"] > 0 and g["candidates"] >= 50 * g["groups"]
 
 
 def test_render_against_float64(ctx):

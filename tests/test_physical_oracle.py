@@ -307,3 +307,32 @@ def test_presets(which, ns):
         assert kinds.count(photonmap.MAT_DIFFUSE) >= 1
     again = photonmap.preset(which, 0x5EED0000 + which)[0]
     assert bytes(again) == bytes(sc)
+
+
+def test_fixed_sum_is_order_independent_and_close_to_exact():
+    """The estimate sum: any order of the terms gives the same bits, within
+    one rounding of the exact sum (here within 1 ulp of the correctly rounded
+    float of the exact rational sum)."""
+    from fractions import Fraction
+    rng = np.random.default_rng(7)
+    for trial in range(200):
+        n = int(rng.integers(0, 129))
+        scale = 10.0 ** rng.uniform(-30, 3)
+        t = (rng.exponential(1.0, n) * scale).astype(np.float32)
+        if trial % 5 == 0 and n:
+            t[rng.integers(0, n, max(1, n // 4))] = 0.0  # back-facing photons
+        if trial % 7 == 0 and n:
+            t[0] = np.float32(1e-41)  # a subnormal term
+        s = oracle.fixed_sum(t)
+        for _ in range(3):
+            assert oracle.fixed_sum(rng.permutation(t)).view(np.uint32) == s.view(np.uint32)
+        exact = sum((Fraction(float(x)) for x in t), Fraction(0))
+        ref = np.float32(float(exact))
+        if ref == 0:
+            assert s == 0
+        else:
+            assert abs(int(s.view(np.int32)) - int(ref.view(np.int32))) <= 1, (trial, s, ref)
+    assert oracle.fixed_sum(np.zeros(0, np.float32)) == 0.0
+    assert oracle.fixed_sum(np.zeros(5, np.float32)) == 0.0
+    one = np.ones(100, np.float32)
+    assert oracle.fixed_sum(one) == np.float32(100.0)
