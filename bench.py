@@ -58,7 +58,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache A/B")
-    ap.add_argument("--cache-warm-frames", type=int, default=192)
+    ap.add_argument("--cache-warm-frames", type=int, default=768)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched frame")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2)
@@ -85,7 +85,7 @@ def load_peaks():
 
 def load_traffic(preset):
     """DRAM bytes per k-NN estimate launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "query_knn_run_kernel_preset%d_traffic.txt" % preset)
+    p = os.path.join(ROOT, "profiles", "query_knn_tile_kernel_preset%d_traffic.txt" % preset)
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_launch:"):
@@ -572,13 +572,14 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(photonmap.ctypes.sizeof(photonmap.Scene)),
                 "d2h_bytes_per_step": int(npix * (16 + 4)),
                 "steps": args.e2e_steps},
-        "roofline": {"bound": "hbm", "kernel": "query_knn_run_kernel", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "query_knn_tile_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
                      "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "formula": "gathers x (32 B x k + 52 B), over the k-NN estimate "
-                                "kernel's CUDA-event time (events on the render stream)"},
+                     "formula": "gathers x (32 B x k + 52 B), over the CUDA-event time of the "
+                                "k-NN estimate pass (anchor, shared-candidate and deferred "
+                                "launches; events on the render stream)"},
         "gpu_launches": int(launches),
         "clocks": clk,
     }

@@ -62,17 +62,13 @@ cudaError_t cache_write_queries(const PScene &S, const RenderParams &R, bool vol
 cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *qa,
                             const float4 *qd, const float4 *val, uint32_t npix, float exposure,
                             float4 *rad, uchar4 *rgba, cudaStream_t s);
-// k-NN estimate of query sel[i] (or i when sel is null) into
-// val[out_index[i]] (or val[i]): diffuse queries e / (pi r^2) / pi from the
-// surface map, volume queries e / (4/3 pi r^3) with the phase function
-// toward wo from the volume map.
-cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView &vol,
-                             const float4 *qa, const float4 *qd, const uint32_t *sel,
-                             const uint32_t *out_index, uint32_t n, int k, float radius,
-                             float4 *val, cudaStream_t s);
-// The same estimates for runs of `run` consecutive entries of `order`
-// (positions into sel), each warm-started from its predecessor in the run
-// when both read the same map; val[order[j]] receives query sel[order[j]].
+// k-NN estimates of queries sel[order[j]] (order[j] when sel is null) into
+// val[order[j]], warp w taking the run order[w * run .. (w + 1) * run), each
+// query warm-started from its predecessor in the run when both read the
+// same map (for sparse sorted picks, where shared candidate sets do not
+// pay): diffuse queries e / (pi r^2) / pi, volume queries e / (4/3 pi r^3)
+// with the phase function toward wo; with raw set, e and r^2 (-1 when
+// nothing was found).
 cudaError_t cache_knn_values_runs(const PScene &S, const MapView &surf, const MapView &vol,
                                   const float4 *qa, const float4 *qd, const uint32_t *sel,
                                   const uint32_t *order, uint32_t n, int run, int k, float radius,

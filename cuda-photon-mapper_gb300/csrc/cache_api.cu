@@ -23,8 +23,8 @@ struct CacheState {
     // training
     uint32_t *sel = nullptr;
     float4 *tgt = nullptr;
-    // the frame's picks sorted by query index (coherent k-NN targets) and
-    // their positions in the random order training reads them in
+    // the frame's picks sorted by (map, Morton code) for coherent k-NN
+    // targets, and their positions in the random order training reads
     uint32_t *skey = nullptr, *sval = nullptr, *skey_tmp = nullptr, *sval_tmp = nullptr;
     uint32_t *shist = nullptr, *sn = nullptr;
     float *scale_sum = nullptr;
@@ -40,6 +40,28 @@ namespace pm {
 namespace {
 
 constexpr int kTargetRun = 8;  // training targets warm-started in runs of this length
+
+// The frame's training picks c->sel[0..ns) (uniform, stratified between
+// diffuse and volume queries) and their k-NN targets in c->tgt: the picks
+// sorted by (map, Morton code) and estimated in runs of kTargetRun
+// warm-started list searches (picks this sparse are too far apart to share
+// candidate sets), written back in pick order.
+cudaError_t pick_and_target(PhysicalState *st, CacheState *c, cudaStream_t stream) {
+    const uint32_t ns = c->cfg.train_samples;
+    cudaError_t e;
+#define CT_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    CT_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, st->ql.nq, st->ql.slist, st->ql.nsurf, ns,
+                        c->cfg.surface_fraction, c->sel, stream));
+    CT_TRY(cache_sample_keys(c->grid, st->ql.qa, c->sel, ns, c->skey, c->sval, stream));
+    uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
+    CT_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31, c->shist,
+                                stream, &ok_keys, &ok_vals));
+    CT_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), st->ql.qa, st->ql.qd,
+                                 c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt,
+                                 stream));
+#undef CT_TRY
+    return cudaSuccess;
+}
 
 template <typename T>
 cudaError_t dalloc(T **p, size_t count) {
@@ -117,7 +139,7 @@ void pm_cache_default_config(pm_cache_config *cfg) {
     cfg->log2_table = 19;
     cfg->base_res = 16;
     cfg->max_res = 2048;
-    cfg->train_samples = 1u << 20;
+    cfg->train_samples = 1u << 18;  // 8 steps per frame: online training
     cfg->batch = 1u << 15;
     cfg->lr = 3e-2f;
     cfg->beta1 = 0.9f;
@@ -216,20 +238,9 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
     cudaError_t e;
     const uint32_t ns = c->cfg.train_samples, batch = c->cfg.batch;
     const uint32_t nb = (ns + batch - 1) / batch;
-    const MapView surf = view_of(st->map[0]), vol = view_of(st->map[1]);
     for (int f = 0; f < frames; ++f) {
         PM_TRY(cudaEventRecord(c->tev0, stream));
-        PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, st->ql.nq, st->ql.slist, st->ql.nsurf, ns,
-                            c->cfg.surface_fraction, c->sel, stream));
-        // targets in spatial order -- (map, Morton code) -- in runs of
-        // kTargetRun warm-started queries per warp, written back to the
-        // random order the steps read
-        PM_TRY(cache_sample_keys(c->grid, st->ql.qa, c->sel, ns, c->skey, c->sval, stream));
-        uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
-        PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31,
-                                    c->shist, stream, &ok_keys, &ok_vals));
-        PM_TRY(cache_knn_values_runs(st->dscene, surf, vol, st->ql.qa, st->ql.qd, c->sel, ok_vals, ns,
-                                     kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt, stream));
+        PM_TRY(pick_and_target(st, c, stream));
         PM_TRY(cudaEventRecord(c->ev[5], stream));
         if (!(c->target_scale > 0.0f)) {
             float sum = 0.0f;
@@ -449,15 +460,7 @@ pm_status pm_cache_debug_targets(pm_ctx *ctx, float4 *targets, uint32_t *query) 
     if (s != PM_OK) return s;
     const uint32_t ns = c->cfg.train_samples;
     cudaError_t e;
-    PM_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, st->ql.nq, st->ql.slist, st->ql.nsurf, ns,
-                        c->cfg.surface_fraction, c->sel, 0));
-    PM_TRY(cache_sample_keys(c->grid, st->ql.qa, c->sel, ns, c->skey, c->sval, 0));
-    uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
-    PM_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31, c->shist,
-                                0, &ok_keys, &ok_vals));
-    PM_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), st->ql.qa, st->ql.qd,
-                                 c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt,
-                                 0));
+    PM_TRY(pick_and_target(st, c, 0));
     PM_TRY(cudaDeviceSynchronize());
     if (targets) PM_TRY(cudaMemcpy(targets, c->tgt, sizeof(float4) * ns, cudaMemcpyDeviceToHost));
     if (query) PM_TRY(cudaMemcpy(query, c->sel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));

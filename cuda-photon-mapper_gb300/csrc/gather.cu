@@ -221,45 +221,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
     }
 }
 
-// k-NN radiance estimate of one render query (warp per query): the same
-// search, flux sum and normalisation the render kernel applies at that
-// point, without the transmittance and albedo factors.
-template <int S>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    query_knn_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
-                     const uint32_t *sel, const uint32_t *out_index, uint32_t n, int k, float r2cap,
-                     float4 *out) {
-    __shared__ WarpScratch ws[kWarpsPerBlock];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t qi = blockIdx.x * kWarpsPerBlock + wib;
-    if (qi >= n) return;
-    const uint32_t src = sel ? sel[qi] : qi;
-    const float4 a = qa[src], d = qd[src];
-    const int obj = __float_as_int(a.w);
-    const v3 x = mk3(a.x, a.y, a.z), wo = mk3(d.x, d.y, d.z);
-    const bool surface = obj != kNone;
-    const MapView &m = surface ? surf : vol;
-    v3 e = mk3(0.f, 0.f, 0.f);
-    if (m.n > 0) {
-        const uint64_t cap = make_key(r2cap, 0xffffffffu);
-        Knn<S> kn;
-        kn.reset(cap, k);
-        knn_search<S>(m, x, kn, ws[wib], lane, cap);
-        int found;
-        float r2;
-        const v3 dirv = surface ? facing_normal(Sc, obj, x, wo) : wo;
-        e = flux_sum<S>(kn, m, lane, surface ? 0 : 1, dirv, Sc.g, cap, r2cap, &found, &r2);
-        if (found > 0) {
-            const float sc = surface ? (1.0f / (3.14159265f * r2)) * 0.318309886f
-                                     : 1.0f / (4.18879020f * r2 * sqrtf(r2));
-            e = e * sc;
-        } else {
-            e = mk3(0.f, 0.f, 0.f);
-        }
-    }
-    if (lane == 0) out[out_index ? out_index[qi] : qi] = make_float4(e.x, e.y, e.z, 0.0f);
-}
-
 // k-NN estimates of runs of spatially sorted queries: warp w takes queries
 // order[w * run .. (w + 1) * run) (indices into sel, or the queries
 // themselves when sel is null), each warm-started from the previous query's
@@ -378,23 +339,6 @@ cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vo
         case 3: render_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); note_launch(); break;
         default: render_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, R, rad, rgba); note_launch(); break;
     }
-    return cudaGetLastError();
-}
-
-cudaError_t cache_knn_values(const PScene &S, const MapView &surf, const MapView &vol,
-                             const float4 *qa, const float4 *qd, const uint32_t *sel,
-                             const uint32_t *out_index, uint32_t n, int k, float radius, float4 *val,
-                             cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    const float r2 = radius * radius;
-    const dim3 grid((n + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
-    switch (slots_for(k)) {
-        case 1: query_knn_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
-        case 2: query_knn_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
-        case 3: query_knn_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
-        default: query_knn_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, out_index, n, k, r2, val); break;
-    }
-    note_launch();
     return cudaGetLastError();
 }
 

@@ -95,22 +95,27 @@ void query_list_free(QueryList &ql);
 // into ql.val: the list in spatial order, warm-started runs of queries.
 cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s);
 constexpr int kGatherStats = 7;
-// Scratch of knn_values_tiles: anchor_d[tile_chunks(n)], defer[n], one
-// defer_n word; stats: kGatherStats counters added (nullable).
+// Scratch of knn_values_tiles: anchor_d[tile_chunks(n, groups)], defer[n],
+// one defer_n word; stats: kGatherStats counters added (nullable).
 struct TileBuffers {
     float *anchor_d;
     uint32_t *defer;
     uint32_t *defer_n;
     unsigned long long *stats;
 };
-uint32_t tile_chunks(uint32_t n);
+// Warps of an estimate pass over n queries, `groups` groups of 32 per warp.
+uint32_t tile_chunks(uint32_t n, int groups);
 // k-NN estimates of the queries in spatial order (order[0..n) indexes qa/qd
-// and val), one shared candidate set per group of neighbours
-// (tile_gather.cu); raw as cache_knn_values_runs.
+// and val), one shared candidate set per group of 32 neighbours, `groups`
+// (1-4) consecutive groups per warp of which the later ones are bounded by
+// the earlier (tile_gather.cu; use 1 when the groups are not neighbours): diffuse queries e / (pi r^2) / pi from the surface map,
+// volume queries e / (4/3 pi r^3) with the phase function toward wo from
+// the volume map; with raw set, the flux sum e and r^2 (-1 when nothing
+// was found) instead.
 cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView &vol,
                              const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
-                             int k, float radius, bool raw, float4 *val, const TileBuffers &buf,
-                             int sm_count, cudaStream_t s);
+                             int groups, int k, float radius, bool raw, float4 *val,
+                             const TileBuffers &buf, int sm_count, cudaStream_t s);
 
 // The render parameters pm_render passes for the installed configuration.
 inline RenderParams render_params(const PhysicalState *st) {

@@ -133,18 +133,18 @@ cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s) {
         QL_TRY(dalloc(&ql.gather_stats, kGatherStats));
         QL_TRY(dalloc(&ql.defer_n, 1));
     }
-    if (tile_chunks(ql.nq) > ql.anchor_cap) {
+    if (tile_chunks(ql.nq, 4) > ql.anchor_cap) {
         cudaFree(ql.anchor_d);
         ql.anchor_d = nullptr;
         ql.anchor_cap = 0;
-        QL_TRY(dalloc(&ql.anchor_d, tile_chunks(ql.qcap)));
-        ql.anchor_cap = tile_chunks(ql.qcap);
+        QL_TRY(dalloc(&ql.anchor_d, tile_chunks(ql.qcap, 4)));
+        ql.anchor_cap = tile_chunks(ql.qcap, 4);
     }
     QL_TRY(cudaMemsetAsync(ql.gather_stats, 0, sizeof(unsigned long long) * kGatherStats, s));
     // the sort's other index array is free again: the deferred-query list
     const TileBuffers buf{ql.anchor_d, ql.order == ql.ord ? ql.ord_tmp : ql.ord, ql.defer_n, ql.gather_stats};
     QL_TRY(knn_values_tiles(st->dscene, view_of(st->map[0]), view_of(st->map[1]), ql.qa, ql.qd, ql.order,
-                            ql.nq, st->cfg.k, st->cfg.radius, true, ql.val, buf, st->sm_count, s));
+                            ql.nq, 4, st->cfg.k, st->cfg.radius, true, ql.val, buf, st->sm_count, s));
 #undef QL_TRY
     return cudaSuccess;
 }

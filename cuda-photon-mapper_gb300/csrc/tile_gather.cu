@@ -1,8 +1,8 @@
 // tile_gather.cu -- k-NN radiance estimates of a query list in spatial
 // order, one candidate set per group of neighbouring queries.
 //
-// A warp takes 4 consecutive groups of 32 queries of the (map, Morton code)
-// order. The k-th-neighbour distance d(x) (capped at the gather radius) is
+// A warp takes 1 to 4 consecutive groups of 32 queries of the (map, Morton
+// code) order. The k-th-neighbour distance d(x) (capped at the gather radius) is
 // 1-Lipschitz in the query position, so exact distances d_j at points x_j
 // bound it everywhere:
 //     max_j (d_j - |x - x_j|)  <=  d(x)  <=  min_j (d_j + |x - x_j|).
@@ -38,8 +38,6 @@ namespace {
 using namespace wknn;
 
 constexpr int kTileWarps = 4;
-constexpr int kGroupsPerWarp = 4;
-constexpr int kChunk = 32 * kGroupsPerWarp;  // queries per warp
 constexpr int kAnchorAt = 15;                // the anchor: query 15 of a warp's chunk
 constexpr int kTileCap = 384;                // candidate records per warp (slots fit 16 bits)
 constexpr float kRel = 2e-4f;                // relative and absolute margins of the distance bounds
@@ -499,8 +497,8 @@ __device__ __forceinline__ void tighten(const Query &q, unsigned mask, float d_l
 template <int S>
 __global__ void __launch_bounds__(kTileWarps * 32, 5)
     query_knn_tile_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
-                          const uint32_t *order, uint32_t n, const float *anchor_d, int k, float r2cap,
-                          bool raw, float4 *out, uint32_t *defer_list, uint32_t *defer_n,
+                          const uint32_t *order, uint32_t n, int groups, const float *anchor_d, int k,
+                          float r2cap, bool raw, float4 *out, uint32_t *defer_list, uint32_t *defer_n,
                           unsigned long long *stats) {
     const int lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -520,7 +518,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
     if (lane < kStCount) ts.st[lane] = 0;
     __syncthreads();
     const uint32_t chunk = blockIdx.x * kTileWarps + (threadIdx.x >> 5);
-    const uint32_t wfirst = chunk * (uint32_t)kChunk;
+    const uint32_t wfirst = chunk * (uint32_t)(32 * groups);
     if (wfirst >= n) return;
     const float rcap = sqrtf(r2cap);
     // exact distances known so far (lane j: one point; kd < 0: none): the
@@ -538,7 +536,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
             kd = anchor_d[chunk];
         }
     }
-    for (int g = 0; g < kGroupsPerWarp; ++g) {
+    for (int g = 0; g < groups; ++g) {
         const uint32_t first = wfirst + (uint32_t)(32 * g);
         if (first >= n) break;
         const uint32_t cnt = min(32u, n - first);
@@ -613,11 +611,11 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
 template <int S>
 __global__ void __launch_bounds__(128)
     anchor_kernel(MapView surf, MapView vol, const float4 *qa, const uint32_t *order, uint32_t n,
-                  int k, float r2cap, float *anchor_d) {
+                  int groups, int k, float r2cap, float *anchor_d) {
     __shared__ WarpScratch ws[4];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t chunk = blockIdx.x * 4 + wib;
-    const uint32_t wfirst = chunk * (uint32_t)kChunk;
+    const uint32_t wfirst = chunk * (uint32_t)(32 * groups);
     if (wfirst >= n) return;
     const float4 a = qa[order[wfirst + min((uint32_t)kAnchorAt, n - 1 - wfirst)]];
     const MapView &m = __float_as_int(a.w) != kNone ? surf : vol;
@@ -658,21 +656,22 @@ __global__ void __launch_bounds__(128)
 
 cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView &vol,
                              const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
-                             int k, float radius, bool raw, float4 *val, const TileBuffers &buf,
-                             int sm_count, cudaStream_t s) {
+                             int groups, int k, float radius, bool raw, float4 *val,
+                             const TileBuffers &buf, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    if (groups < 1 || groups > 4) return cudaErrorInvalidValue;
     const float r2 = radius * radius;
-    const uint32_t chunks = (n + kChunk - 1) / kChunk;
+    const uint32_t chunks = tile_chunks(n, groups);
     const dim3 grid((chunks + kTileWarps - 1) / kTileWarps), block(kTileWarps * 32);
     const int smem = (int)(kTileWarps * sizeof(TileScratch));
     const dim3 dgrid(std::max(sm_count, 1) * 8);
     cudaError_t e = cudaMemsetAsync(buf.defer_n, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
 #define PM_TILE_LAUNCH(SL)                                                                              \
-    anchor_kernel<SL><<<grid, block, 0, s>>>(surf, vol, qa, order, n, k, r2, buf.anchor_d);              \
+    anchor_kernel<SL><<<grid, block, 0, s>>>(surf, vol, qa, order, n, groups, k, r2, buf.anchor_d);      \
     e = cudaFuncSetAttribute(query_knn_tile_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
     if (e != cudaSuccess) return e;                                                                     \
-    query_knn_tile_kernel<SL><<<grid, block, smem, s>>>(S, surf, vol, qa, qd, order, n, buf.anchor_d, k, \
+    query_knn_tile_kernel<SL><<<grid, block, smem, s>>>(S, surf, vol, qa, qd, order, n, groups, buf.anchor_d, k, \
                                                         r2, raw, val, buf.defer, buf.defer_n, buf.stats); \
     deferred_kernel<SL><<<dgrid, 128, 0, s>>>(S, surf, vol, qa, qd, buf.defer, buf.defer_n, k, r2, raw, val)
     switch ((k + 31) / 32) {
@@ -686,6 +685,6 @@ cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView
     return cudaGetLastError();
 }
 
-uint32_t tile_chunks(uint32_t n) { return (n + kChunk - 1) / kChunk; }
+uint32_t tile_chunks(uint32_t n, int groups) { return (n + 32u * groups - 1) / (32u * groups); }
 
 }  // namespace pm
