@@ -58,7 +58,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache A/B")
-    ap.add_argument("--cache-warm-frames", type=int, default=768)
+    ap.add_argument("--cache-warm-frames", type=int, default=384)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched frame")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2)

@@ -168,7 +168,7 @@ def test_cache_file_round_trip(ctx, tmp_path):
 
 def test_cached_render_against_float64_at_bench_scale(ctx):
     """The A/B of the benchmark scene (preset 2: 1M + 1M photons, 1024^2,
-    k = 100): the cached render after 768 online training frames (2^18
+    k = 100): the cached render after 384 online training frames (2^20
     samples and 8 Adam steps each) and the
     k-NN render, both against the FP64 oracle render on 8192 random pixels.
     The target: the cached render within 1e-2 relative RMSE of the FP64
@@ -180,7 +180,7 @@ def test_cached_render_against_float64_at_bench_scale(ctx):
     frame(ctx, sc, cf)
     knn = render(ctx, cf)
     ctx.cache_enable()
-    ctx.cache_train(768)
+    ctx.cache_train(384)
     cached = render(ctx, cf, cached=0)
     assert ctx.cache_stats().tc_status == 0
     rng = np.random.default_rng(2024)
