@@ -391,6 +391,29 @@ def legacy_frames(ctx, args, with_cpu):
                                "sample": "%d full frames of the C restatement (bit-exact with the "
                                          "reference's serial semantics)" % cpu_n}
         out["speedup_vs_cpu"] = cpu_ms / gpu_ms
+        # the reference's own CUDA kernels on this GPU, when their module was
+        # built (it needs the reference checkout at build time)
+        try:
+            ref = oracle.ReferenceGPU()
+        except OSError as e:
+            out["reference_gpu"] = {"unavailable": str(e)}
+            return out
+        ref.init_random()
+        for i in range(args.warmup):
+            ref.frame(512, 512, 0.01 * i, 1, 1)
+        emit_ms, render_ms = [], []
+        for i in range(n):
+            a, b = ref.frame(512, 512, 0.01 * i, 1, 1)
+            emit_ms.append(a)
+            render_ms.append(b)
+        ref_ms = statistics.mean(emit_ms) + statistics.mean(render_ms)
+        out["reference_gpu"] = {
+            "frame_ms": ref_ms, "emit_ms": statistics.mean(emit_ms),
+            "render_ms": statistics.mean(render_ms), "frames": n,
+            "source": "the reference's photonMappingKernel.cu compiled unmodified for sm_103a "
+                      "(cutil shims), launched with its own grid shapes and synchronisations, "
+                      "CUDA events; its output is racy and not compared"}
+        out["speedup_vs_reference_gpu"] = ref_ms / gpu_ms
     return out
 
 

@@ -64,18 +64,47 @@ def build_oracle(force=False):
     return ORACLE_LIB
 
 
+REF_CUBIN = os.path.join(ORACLE_DIR, "_ref", "ref_kernels.cubin")
+REF_GPU_LIB = os.path.join(ORACLE_DIR, "_ref", "libpmref_gpu.so")
+
+
 def build_reference():
-    """Compiles the reference's own code into oracle/_ref (needs the checkout)."""
+    """Compiles the reference's own code into oracle/_ref (needs the checkout):
+    its photon-mapping code as serial host C++ (the legacy oracle's pin) and
+    its CUDA file unmodified as an sm_103a module (the measured reference-GPU
+    bar; the module travels to GPU hosts, the checkout does not)."""
     if not os.path.isdir(REF_DIR):
         return None
     _run(["make", "-s", "-C", ROOT, "-f", "oracle/ref.mk", "REF=" + REF_DIR])
+    src = os.path.join(REF_DIR, "photonMappingKernel.cu")
+    shims = glob.glob(os.path.join(ORACLE_DIR, "ref_gpu", "*.h"))
+    if _newer(REF_CUBIN, [src] + shims):
+        _run([NVCC] + ARCH + ["-O3", "-cubin", "-w", "-I", os.path.join(ORACLE_DIR, "ref_gpu"), "-o",
+                              REF_CUBIN, src])
     return os.path.join(ORACLE_DIR, "_ref", "libpmref.so")
+
+
+def build_ref_gpu_runner():
+    """The loader that times the reference's GPU module (oracle/ref_gpu_runner.cpp)."""
+    src = os.path.join(ORACLE_DIR, "ref_gpu_runner.cpp")
+    if not _newer(REF_GPU_LIB, [src]):
+        return REF_GPU_LIB
+    os.makedirs(os.path.dirname(REF_GPU_LIB), exist_ok=True)
+    cuda = os.path.dirname(os.path.dirname(NVCC))
+    _run(["g++", "-O2", "-fPIC", "-shared", "-I", os.path.join(cuda, "include"), src, "-o", REF_GPU_LIB,
+          "-L", os.path.join(cuda, "lib64"), "-L", os.path.join(cuda, "lib64", "stubs"), "-lcudart",
+          "-lcuda"])
+    return REF_GPU_LIB
 
 
 def build_all(force=False):
     build_library(force)
     build_oracle(force)
     build_reference()
+    try:
+        build_ref_gpu_runner()
+    except RuntimeError as e:  # measurement infrastructure: never fails the product build
+        print("build: reference-GPU runner not built:", str(e).splitlines()[0], file=sys.stderr)
 
 
 if __name__ == "__main__":

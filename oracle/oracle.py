@@ -265,3 +265,41 @@ def radius_gather(pos, pw, points, normals, sq_radius, exposure):
                             pts.ctypes.data, nrm.ctypes.data, len(pts), sq_radius, exposure,
                             out.ctypes.data)
     return out
+
+
+# ---- the reference's own GPU kernels (measurement only) ---------------------
+
+class ReferenceGPU:
+    """The reference's photonMappingKernel.cu, compiled unmodified for the GPU
+    (oracle/_ref/ref_kernels.cubin), replayed through its three launch
+    wrappers by oracle/_ref/libpmref_gpu.so (ref_gpu_runner.cpp) and timed.
+    Its kernels are racy by design (shared generator, non-atomic grid
+    adds): timed, never compared. Raises OSError when either file is
+    missing."""
+
+    def __init__(self):
+        d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref")
+        cubin = os.path.join(d, "ref_kernels.cubin")
+        if not os.path.exists(cubin):
+            raise OSError("the reference's GPU module was not built (needs the reference checkout)")
+        self.lib = ctypes.CDLL(os.path.join(d, "libpmref_gpu.so"))
+        f, u, i = ctypes.c_float, ctypes.c_uint, ctypes.c_int
+        self.lib.pmref_gpu_load.argtypes = [ctypes.c_char_p]
+        self.lib.pmref_gpu_init_rng.argtypes = [ctypes.POINTER(f)]
+        self.lib.pmref_gpu_frame.argtypes = [u, u, f, i, i, i, ctypes.POINTER(f), ctypes.POINTER(f)]
+        if self.lib.pmref_gpu_load(cubin.encode()) != 0:
+            raise OSError("loading the reference's GPU module failed")
+
+    def init_random(self):
+        ms = ctypes.c_float()
+        if self.lib.pmref_gpu_init_rng(ctypes.byref(ms)) != 0:
+            raise OSError("init_random_numbers_kernel failed")
+        return ms.value
+
+    def frame(self, w, h, anim_time, interpolate, media, emit=True):
+        """(emit ms, render ms) of one frame."""
+        me, mr = ctypes.c_float(), ctypes.c_float()
+        if self.lib.pmref_gpu_frame(w, h, anim_time, int(interpolate), int(media), int(emit),
+                                    ctypes.byref(me), ctypes.byref(mr)) != 0:
+            raise OSError("reference frame failed")
+        return me.value, mr.value
