@@ -179,8 +179,73 @@ __device__ __forceinline__ float alpha_of(v3 p, v3 a, v3 b, int ax) {  // getAlp
     return (axis_of(p, ax) - axis_of(a, ax)) / (axis_of(b, ax) - axis_of(a, ax));
 }
 
+// integrateVolumePhotons (:831-870) at voxel wp (getVoxelCoordinates of
+// the march point).
+__device__ v3 integrate_volume(const float4 *__restrict__ g, I3 wp) {
+    v3 acc = mk3(0.0f, 0.0f, 0.0f);
+    int x0 = lo_edge(wp.x, 1), y0 = lo_edge(wp.y, 1), z0 = lo_edge(wp.z, 1);
+    int x1 = hi_edge(wp.x, G - 1), y1 = hi_edge(wp.y, G - 1), z1 = hi_edge(wp.z, G - 1);
+    for (int i = x0; i < x1; ++i)
+        for (int j = y0; j < y1; ++j)
+            for (int k = z0; k < z1; ++k) acc = acc + grid_at(g, i, j, k);
+    return acc;
+}
+
+// Both window sums start from zero and depend only on integer voxel
+// coordinates, so a frame computes each distinct window once -- in the loop
+// order above, so the values are the same bits -- and the render looks them
+// up. A coordinate's window is empty outside [kWinLo, kWinLo + kVolN) (volume)
+// or [kWinLo, kWinLo + kSlabN) (slab).
+constexpr int kWinLo = -2, kVolN = 36, kSlabN = 37;
+constexpr int kVolWindows = kVolN * kVolN * kVolN, kSlabWindows = 5 * kSlabN * kSlabN;
+
+__global__ void window_tables_kernel(const float4 *__restrict__ g, float4 *vol, float4 *slab) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < kVolWindows) {
+        I3 wp;
+        wp.z = t % kVolN + kWinLo;
+        wp.y = (t / kVolN) % kVolN + kWinLo;
+        wp.x = t / (kVolN * kVolN) + kWinLo;
+        const v3 acc = integrate_volume(g, wp);
+        vol[t] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+    } else if (t < kVolWindows + kSlabWindows) {
+        const int u = t - kVolWindows;
+        const int id = u / (kSlabN * kSlabN);
+        const int a = (u / kSlabN) % kSlabN + kWinLo, b = u % kSlabN + kWinLo;
+        // the plane's two free coordinates: (y, z) for 0 and 2, (x, z) for 1
+        // and 3, (x, y) for 4; the fixed one does not enter the window
+        I3 wp;
+        wp.x = id == 0 || id == 2 ? 0 : a;
+        wp.y = id == 0 || id == 2 ? a : (id == 4 ? b : 0);
+        wp.z = id == 4 ? 0 : b;
+        const v3 acc = integrate_slab(g, mk3(0.0f, 0.0f, 0.0f), wp, 1, id);
+        slab[u] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+    }
+}
+
+__device__ __forceinline__ bool in_window_range(int c, int n) { return c >= kWinLo && c < kWinLo + n; }
+
+// integrate_volume through the table.
+__device__ __forceinline__ v3 volume_window(const float4 *__restrict__ vol, v3 p) {
+    const I3 wp = voxel_of(p);
+    if (!in_window_range(wp.x, kVolN) || !in_window_range(wp.y, kVolN) || !in_window_range(wp.z, kVolN))
+        return mk3(0.0f, 0.0f, 0.0f);
+    const float4 v = __ldg(&vol[((wp.x - kWinLo) * kVolN + (wp.y - kWinLo)) * kVolN + (wp.z - kWinLo)]);
+    return mk3(v.x, v.y, v.z);
+}
+
+// integrate_slab(g, 0, wp, type, id) through the table.
+__device__ __forceinline__ v3 slab_window(const float4 *__restrict__ slab, I3 wp, int type, int id) {
+    if (type != 1 || id < 0 || id > 4) return mk3(0.0f, 0.0f, 0.0f);
+    const int a = id == 0 || id == 2 ? wp.y : wp.x;
+    const int b = id == 4 ? wp.y : wp.z;
+    if (!in_window_range(a, kSlabN) || !in_window_range(b, kSlabN)) return mk3(0.0f, 0.0f, 0.0f);
+    const float4 v = __ldg(&slab[(id * kSlabN + (a - kWinLo)) * kSlabN + (b - kWinLo)]);
+    return mk3(v.x, v.y, v.z);
+}
+
 // interpolateEnergy + bilinearInterpolate (:442-583).
-__device__ v3 interpolate_slab(const float4 *__restrict__ g, v3 p, int type, int id) {
+__device__ v3 interpolate_slab(const float4 *__restrict__ slab, v3 p, int type, int id) {
     v3 zero = mk3(0.0f, 0.0f, 0.0f);
     if (type != 1) return zero;
     int a1, a2;
@@ -196,28 +261,16 @@ __device__ v3 interpolate_slab(const float4 *__restrict__ g, v3 p, int type, int
     float c2 = axis_of(p1, a2), d2 = c_vox_dim[a2];
     float s2 = axis_of(p, a2) > c2 ? c2 + d2 : c2 - d2;
     set_axis(p2, a2, c2); set_axis(p3, a2, s2); set_axis(p4, a2, s2);
-    v3 q1 = integrate_slab(g, zero, voxel_of(p1), type, id);
-    v3 q2 = integrate_slab(g, zero, voxel_of(p2), type, id);
-    v3 q3 = integrate_slab(g, zero, voxel_of(p3), type, id);
-    v3 q4 = integrate_slab(g, zero, voxel_of(p4), type, id);
+    v3 q1 = slab_window(slab, voxel_of(p1), type, id);
+    v3 q2 = slab_window(slab, voxel_of(p2), type, id);
+    v3 q3 = slab_window(slab, voxel_of(p3), type, id);
+    v3 q4 = slab_window(slab, voxel_of(p4), type, id);
     float a = alpha_of(p, p1, p2, a1);
     v3 p12 = lerp3(p1, p2, a), q12 = lerp3(q1, q2, a);
     a = alpha_of(p, p3, p4, a1);
     v3 p34 = lerp3(p3, p4, a), q34 = lerp3(q3, q4, a);
     a = alpha_of(p, p12, p34, a2);
     return lerp3(q12, q34, a);
-}
-
-// integrateVolumePhotons (:831-870).
-__device__ v3 integrate_volume(const float4 *__restrict__ g, v3 p) {
-    v3 acc = mk3(0.0f, 0.0f, 0.0f);
-    I3 wp = voxel_of(p);
-    int x0 = lo_edge(wp.x, 1), y0 = lo_edge(wp.y, 1), z0 = lo_edge(wp.z, 1);
-    int x1 = hi_edge(wp.x, G - 1), y1 = hi_edge(wp.y, G - 1), z1 = hi_edge(wp.z, G - 1);
-    for (int i = x0; i < x1; ++i)
-        for (int j = y0; j < y1; ++j)
-            for (int k = z0; k < z1; ++k) acc = acc + grid_at(g, i, j, k);
-    return acc;
 }
 
 // ---- emission --------------------------------------------------------------
@@ -419,30 +472,50 @@ __device__ __forceinline__ uint32_t first_at_least(const uint32_t *__restrict__ 
     return lo;
 }
 
-// Sums each voxel's deposits in photon order and writes both grid layouts.
-// The range is known before the loop, so the loads run ahead of the
-// (necessarily serial) additions.
+// Sums each voxel's deposits in photon order and writes both grid layouts;
+// one warp per voxel. The lanes load 32 consecutive deposits at a time
+// (coalesced, the next 32 already in flight) and the warp adds them in
+// order through shuffles: exactly the serial additions, bound by the add
+// chain instead of one thread's load latency.
 __global__ void __launch_bounds__(256) reduce_kernel(const uint32_t *__restrict__ skeys,
                                                      const float4 *__restrict__ sorted,
                                                      const uint32_t *total, float *grid3,
                                                      float4 *grid4) {
-    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (v >= kLegacyVoxels) return;
     const uint32_t n = *total;
     const uint32_t lo = first_at_least(skeys, n, (uint32_t)v);
     const uint32_t hi = first_at_least(skeys, n, (uint32_t)v + 1u);
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
-#pragma unroll 8
-    for (uint32_t j = lo; j < hi; ++j) {
-        const float4 e = __ldg(&sorted[j]);
-        ax = ax + e.x;
-        ay = ay + e.y;
-        az = az + e.z;
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 e = lo + lane < hi ? __ldg(&sorted[lo + lane]) : zero;
+    for (uint32_t base = lo; base < hi; base += 32) {
+        const uint32_t nb = base + 32;
+        const float4 next = nb + lane < hi ? __ldg(&sorted[nb + lane]) : zero;
+        const uint32_t cnt = min(32u, hi - base);
+        if (cnt == 32) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                ax = ax + __shfl_sync(0xffffffffu, e.x, i);
+                ay = ay + __shfl_sync(0xffffffffu, e.y, i);
+                az = az + __shfl_sync(0xffffffffu, e.z, i);
+            }
+        } else {
+            for (uint32_t i = 0; i < cnt; ++i) {
+                ax = ax + __shfl_sync(0xffffffffu, e.x, i);
+                ay = ay + __shfl_sync(0xffffffffu, e.y, i);
+                az = az + __shfl_sync(0xffffffffu, e.z, i);
+            }
+        }
+        e = next;
     }
-    grid3[3 * v + 0] = ax;
-    grid3[3 * v + 1] = ay;
-    grid3[3 * v + 2] = az;
-    grid4[v] = make_float4(ax, ay, az, 0.0f);
+    if (lane == 0) {
+        grid3[3 * v + 0] = ax;
+        grid3[3 * v + 1] = ay;
+        grid3[3 * v + 2] = az;
+        grid4[v] = make_float4(ax, ay, az, 0.0f);
+    }
 }
 
 // init_random_numbers_kernel (:1483-1498): entry i holds draws 3i..3i+2
@@ -467,8 +540,8 @@ __global__ void grid_from_host_kernel(const float *grid3, float4 *grid4) {
 // ---- render ----------------------------------------------------------------
 
 // computePixelColor (:926-1017).
-__device__ v3 shade_pixel(const Scene &sc, const float4 *__restrict__ g, float x, float y,
-                          bool interp, bool media) {
+__device__ v3 shade_pixel(const Scene &sc, const float4 *__restrict__ vol,
+                          const float4 *__restrict__ slab, float x, float y, bool interp, bool media) {
     v3 rgb = mk3(0.0f, 0.0f, 0.0f);
     v3 origin = mk3(0.0f, 0.0f, 0.0f);
     Chain c;
@@ -480,7 +553,7 @@ __device__ v3 shade_pixel(const Scene &sc, const float4 *__restrict__ g, float x
         v3 at = origin;
         for (int i = 0; i < 10; ++i) {
             at = c.ray * 0.6f + at;
-            rgb = rgb + integrate_volume(g, at);
+            rgb = rgb + volume_window(vol, at);
         }
     }
     trace(sc, c.ray, origin, c.h);
@@ -489,19 +562,20 @@ __device__ v3 shade_pixel(const Scene &sc, const float4 *__restrict__ g, float x
     if (c.h.type == 0 && c.h.idx == 1) run_chain(sc, c, 1, origin);
     else if (c.h.type == 0 && c.h.idx == 0) run_chain(sc, c, 2, origin);
     if (!c.h.hit) return rgb;
-    v3 e = interp ? interpolate_slab(g, c.point, c.h.type, c.h.idx)
-                  : integrate_slab(g, mk3(0.0f, 0.0f, 0.0f), voxel_of(c.point), c.h.type, c.h.idx);
+    v3 e = interp ? interpolate_slab(slab, c.point, c.h.type, c.h.idx)
+                  : slab_window(slab, voxel_of(c.point), c.h.type, c.h.idx);
     if (media) e = e * 0.15f;
     return rgb + e;
 }
 
-__global__ void __launch_bounds__(256) render_kernel(Scene sc, const float4 *__restrict__ grid,
-                                                     uchar4 *out, unsigned width, unsigned height,
-                                                     bool interp, bool media, float *rgb_out) {
+__global__ void __launch_bounds__(256) render_kernel(Scene sc, const float4 *__restrict__ vol,
+                                                     const float4 *__restrict__ slab, uchar4 *out,
+                                                     unsigned width, unsigned height, bool interp,
+                                                     bool media, float *rgb_out) {
     unsigned index = blockIdx.x * blockDim.x + threadIdx.x;
     if (index >= width * height) return;
     unsigned x = index % width, y = index / width;
-    v3 c = shade_pixel(sc, grid, (float)x, (float)y, interp, media);
+    v3 c = shade_pixel(sc, vol, slab, (float)x, (float)y, interp, media);
     if (rgb_out) {
         rgb_out[3 * index + 0] = c.x;
         rgb_out[3 * index + 1] = c.y;
@@ -541,6 +615,8 @@ cudaError_t legacy_alloc(LegacyState &st) {
     PM_ALLOC(st.table, sizeof(float4) * kLegacyPhotons);
     PM_ALLOC(st.grid3, sizeof(float) * 3 * kLegacyVoxels);
     PM_ALLOC(st.grid4, sizeof(float4) * kLegacyVoxels);
+    PM_ALLOC(st.vol_win, sizeof(float4) * kVolWindows);
+    PM_ALLOC(st.slab_win, sizeof(float4) * kSlabWindows);
     PM_ALLOC(st.counts, sizeof(uint32_t) * kLegacyPhotons);
     PM_ALLOC(st.offsets, sizeof(uint32_t) * kLegacyPhotons);
     PM_ALLOC(st.total, sizeof(uint32_t));
@@ -563,6 +639,7 @@ cudaError_t legacy_alloc(LegacyState &st) {
 
 void legacy_free(LegacyState &st) {
     cudaFree(st.table); cudaFree(st.grid3); cudaFree(st.grid4); cudaFree(st.counts);
+    cudaFree(st.vol_win); cudaFree(st.slab_win);
     cudaFree(st.offsets); cudaFree(st.total); cudaFree(st.keys); cudaFree(st.keys_tmp);
     cudaFree(st.idx); cudaFree(st.idx_tmp); cudaFree(st.dep); cudaFree(st.sdep); cudaFree(st.hist);
     st = LegacyState();
@@ -594,8 +671,8 @@ cudaError_t legacy_emit(LegacyState &st, float anim_time, int flags, cudaStream_
                              0, 16, st.hist, s, &sk, &si);
     if (e != cudaSuccess) return e;
     gather_deposits_kernel<<<512, 256, 0, s>>>(si, st.dep, st.total, st.sdep); note_launch();
-    reduce_kernel<<<(kLegacyVoxels + 255) / 256, 256, 0, s>>>(sk, st.sdep, st.total, st.grid3,
-                                                             st.grid4); note_launch();
+    reduce_kernel<<<(kLegacyVoxels * 32 + 255) / 256, 256, 0, s>>>(sk, st.sdep, st.total, st.grid3,
+                                                                  st.grid4); note_launch();
     if (media) st.rng_draws += 9ull * kLegacyPhotons;
     return cudaGetLastError();
 }
@@ -605,7 +682,11 @@ cudaError_t legacy_render(const LegacyState &st, uchar4 *out, unsigned width, un
     Scene sc = make_scene(anim_time);
     unsigned n = width * height;
     if (n == 0) return cudaSuccess;
-    render_kernel<<<(n + 255) / 256, 256, 0, s>>>(sc, st.grid4, out, width, height,
+    // the frame's window sums, from the current grid
+    window_tables_kernel<<<(kVolWindows + kSlabWindows + 255) / 256, 256, 0, s>>>(st.grid4, st.vol_win,
+                                                                                 st.slab_win);
+    note_launch();
+    render_kernel<<<(n + 255) / 256, 256, 0, s>>>(sc, st.vol_win, st.slab_win, out, width, height,
                                                   (flags & kLegacyInterpolate) != 0,
                                                   (flags & kLegacyMedia) != 0, rgb_out); note_launch();
     return cudaGetLastError();

@@ -28,7 +28,9 @@ enum LegacyFlags { kLegacyInterpolate = 1, kLegacyMedia = 2 };
 struct LegacyState {
     float4 *table = nullptr;      // randomNumbers (:78), xyz used
     float *grid3 = nullptr;       // photons[32][32][32] float3 (:76), reference layout
-    float4 *grid4 = nullptr;      // same grid padded to float4 for the render's loads
+    float4 *grid4 = nullptr;      // same grid padded to float4
+    float4 *vol_win = nullptr;    // the render's window sums of the grid (media march)
+    float4 *slab_win = nullptr;   // (wall slabs)
     uint32_t *counts = nullptr;   // deposits per photon
     uint32_t *offsets = nullptr;  // exclusive scan of counts
     uint32_t *total = nullptr;    // total deposits (device scalar)
