@@ -63,7 +63,19 @@ def parse_args():
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-legacy", action="store_true", help="skip the legacy-mode frames")
+    ap.add_argument("--resolution", default=None,
+                    help="WxH instead of the preset's image size (small profiling cases)")
     return ap.parse_args()
+
+
+def preset_config(args):
+    """The preset's scene and configuration, with --resolution applied."""
+    import photonmap
+    scene, cfg = photonmap.preset(args.preset, args.seed)
+    if args.resolution:
+        w, h = (int(v) for v in args.resolution.lower().split("x"))
+        cfg.width, cfg.height = w, h
+    return scene, cfg
 
 
 def dist_info():
@@ -387,9 +399,12 @@ def legacy_frames(ctx, args, with_cpu):
             ora.emit(0.01 * i, 1, 1)
             ora.render(512, 512, 0.01 * i, 1, 1)
         cpu_ms = (time.perf_counter() - t0) * 1e3 / cpu_n
-        out["cpu_baseline"] = {"frame_ms": cpu_ms, "cores": 1, "kind": "port",
+        threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        out["cpu_baseline"] = {"frame_ms": cpu_ms, "cores": threads, "kind": "port",
                                "sample": "%d full frames of the C restatement (bit-exact with the "
-                                         "reference's serial semantics)" % cpu_n}
+                                         "reference's serial semantics): emission on one thread "
+                                         "(the deposits' order is the result), the render's "
+                                         "independent pixels on %d OpenMP threads" % (cpu_n, threads)}
         out["speedup_vs_cpu"] = cpu_ms / gpu_ms
         # the reference's own CUDA kernels on this GPU, when their module was
         # built (it needs the reference checkout at build time)
@@ -422,7 +437,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     import photonmap
-    scene, cfg = photonmap.preset(args.preset, args.seed)
+    scene, cfg = preset_config(args)
     threads = os.cpu_count()
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     for _ in range(args.warmup):
@@ -463,7 +478,7 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     lib = photonmap.load()
-    scene, cfg = photonmap.preset(args.preset, args.seed)
+    scene, cfg = preset_config(args)
     cfg.scene_id = rank  # each replica traces its own photon streams
     ctx = photonmap.Context(local)
     ctx.set_scene(scene, cfg)
