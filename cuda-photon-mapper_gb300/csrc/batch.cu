@@ -12,13 +12,22 @@
 //   5. per scene and map, on kBuildStreams side streams: records past the
 //      map's size are set to infinity, then the kd-tree is built over the
 //      map's capacity (so every launch size is a host constant)
-//   6. one persistent render launch over every scene's pixels
+//   6. the render: scenes in query-list mode one after another through the
+//      single-scene render's pipeline -- per-pixel query counts and scans,
+//      query records, (map, Morton) sort, the shared-candidate estimate
+//      pass, the exact composite -- on one buffer set sized at creation
+//      for the largest scene (a scene's query count depends only on its
+//      geometry and camera, so it is known then), with every count the
+//      launches need kept on the device; the other scenes in one
+//      persistent launch over their pixels
 // A scene's image equals the single-scene render of the same scene bit for
-// bit: the paths, extents and records are the same, and the k-NN lists do
+// bit: the paths, extents and records are the same, and the k-NN sets do
 // not depend on the tree (records at infinity are never within a radius).
+#include "cache.cuh"
 #include "gather.cuh"
 #include "kdtree.cuh"
 #include "launch_count.cuh"
+#include "phys_state.cuh"
 #include "pm_ctx.cuh"
 #include "radix_sort.cuh"
 #include "scene.cuh"
@@ -60,6 +69,16 @@ cudaError_t dalloc(T **p, size_t count) {
 }
 
 int shift_of(int leaf_size) { return leaf_size >= 128 ? 2 : (leaf_size >= 64 ? 1 : 0); }
+
+// A query-list scene's gather counters from its scans: diffuse queries,
+// then the rest (volume march samples).
+__global__ void query_gathers_kernel(const uint32_t *off_total, const uint32_t *soff_total,
+                                     unsigned long long *gathers) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        gathers[0] = *soff_total;
+        gathers[1] = (unsigned long long)*off_total - *soff_total;
+    }
+}
 
 }  // namespace
 }  // namespace pm
@@ -108,6 +127,19 @@ struct pm_batch {
     cudaGraphExec_t exec = nullptr;
     unsigned long long graph_kernels = 0;
     bool ran = false;
+    int n_pixel = 0;  // scenes in the persistent per-pixel launch
+    // query-list mode: one buffer set for the scenes rendered one after
+    // another, sized for the largest
+    struct Queries {
+        uint32_t *cnt = nullptr, *off = nullptr, *scnt = nullptr, *soff = nullptr, *slist = nullptr;
+        uint32_t *scan_tmp = nullptr;
+        float4 *qa = nullptr, *qd = nullptr, *val = nullptr;
+        uint32_t *key = nullptr, *ord = nullptr, *key_tmp = nullptr, *ord_tmp = nullptr, *hist = nullptr;
+        float *anchor_d = nullptr;
+        uint32_t *defer_n = nullptr;
+        size_t pix_cap = 0, q_cap = 0;
+    } q;
+    std::vector<uint32_t> nq;  // queries per scene
 };
 
 namespace {
@@ -128,6 +160,11 @@ void free_batch(pm_batch *b) {
     for (auto &s : b->sort) {
         cudaFree(s.keys); cudaFree(s.keys_tmp); cudaFree(s.vals); cudaFree(s.vals_tmp); cudaFree(s.hist);
     }
+    auto &q = b->q;
+    cudaFree(q.cnt); cudaFree(q.off); cudaFree(q.scnt); cudaFree(q.soff); cudaFree(q.slist);
+    cudaFree(q.scan_tmp); cudaFree(q.qa); cudaFree(q.qd); cudaFree(q.val); cudaFree(q.key);
+    cudaFree(q.ord); cudaFree(q.key_tmp); cudaFree(q.ord_tmp); cudaFree(q.hist); cudaFree(q.anchor_d);
+    cudaFree(q.defer_n);
     for (auto &s : b->side)
         if (s) cudaStreamDestroy(s);
     if (b->fork) cudaEventDestroy(b->fork);
@@ -202,6 +239,116 @@ std::vector<int> all_ids(const pm_batch *b) {
     return v;
 }
 
+// The scenes of the persistent per-pixel launch.
+std::vector<int> pixel_ids(const pm_batch *b) {
+    std::vector<int> v;
+    for (int i = 0; i < b->n; ++i)
+        if (!b->tune[i].query_list) v.push_back(i);
+    return v;
+}
+
+// Uploads the per-pixel launch's scene list.
+cudaError_t upload_pixel_scenes(pm_batch *b) {
+    const std::vector<int> ids = pixel_ids(b);
+    b->n_pixel = (int)ids.size();
+    if (ids.empty()) return cudaSuccess;
+    return upload_render(b, ids, b->render_dev, b->prefix_dev);
+}
+
+// The scene's surface / volume queries exist when its map has capacity
+// (the render's rule: records past a map's size sit at infinity).
+void query_flags(const pm_batch *b, int s, bool *vol_on, bool *surf_on) {
+    *surf_on = b->maps[2 * s].cap > 0;
+    *vol_on = b->maps[2 * s + 1].cap > 0;
+}
+
+// Scene s through the single-scene render's pipeline on the query buffers.
+cudaError_t enqueue_query_scene(pm_batch *b, int s, cudaStream_t st) {
+    auto &q = b->q;
+    const BatchRenderScene d = render_desc(b, s);
+    const pm_config &c = b->cfgs[s];
+    const uint32_t npix = (uint32_t)c.width * (uint32_t)c.height;
+    const uint32_t nq = b->nq[s];
+    if (npix == 0) return cudaSuccess;
+    bool vol_on, surf_on;
+    query_flags(b, s, &vol_on, &surf_on);
+    cudaError_t e;
+#define Q_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    Q_TRY(cache_count_queries(d.sc, d.R, vol_on, surf_on, q.cnt, q.scnt, st));
+    Q_TRY(exclusive_scan_u32_large(q.cnt, q.off, npix, q.off + npix, q.scan_tmp, st));
+    Q_TRY(exclusive_scan_u32_large(q.scnt, q.soff, npix, q.soff + npix, q.scan_tmp, st));
+    Q_TRY(cache_write_queries(d.sc, d.R, vol_on, surf_on, q.off, q.soff, q.qa, q.qd, q.slist, st));
+    query_gathers_kernel<<<1, 32, 0, st>>>(q.off + npix, q.soff + npix, b->gathers + 2 * s);
+    note_launch();
+    Q_TRY(cudaGetLastError());
+    if (nq > 0) {
+        CacheGrid box;
+        box.levels = 0;
+        box.log2_t = 0;
+        const pm_scene &sc = b->scenes[s];
+        for (int a = 0; a < 3; ++a) {
+            const float ext = sc.box_max[a] - sc.box_min[a];
+            const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
+            box.lo[a] = sc.box_min[a] - m;
+            const float size = ext + 2.0f * m;
+            box.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
+        }
+        Q_TRY(cache_sample_keys(box, q.qa, nullptr, nq, q.key, q.ord, st));
+        uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
+        Q_TRY(radix_sort_pairs_u32(q.key, q.ord, q.key_tmp, q.ord_tmp, q.off + npix, nq, 0, 31, q.hist, st,
+                                   &ok_keys, &ok_vals));
+        const TileBuffers buf{q.anchor_d, ok_vals == q.ord ? q.ord_tmp : q.ord, q.defer_n, nullptr};
+        Q_TRY(knn_values_tiles(d.sc, d.surf, d.vol, q.qa, q.qd, ok_vals, nq, q.off + npix, 4, c.k, c.radius,
+                               true, q.val, buf, b->sm_count, st));
+    }
+    Q_TRY(render_composite(d.sc, q.off, q.qa, q.qd, q.val, npix, c.exposure, d.rad, d.rgba, st));
+#undef Q_TRY
+    return cudaSuccess;
+}
+
+// Counts every scene's queries (they depend on its geometry and camera
+// only) and sizes the query buffers for the largest scene.
+cudaError_t size_query_buffers(pm_batch *b) {
+    auto &q = b->q;
+    size_t max_pix = 1;
+    for (int s = 0; s < b->n; ++s) max_pix = std::max(max_pix, (size_t)b->cfgs[s].width * b->cfgs[s].height);
+    cudaError_t e;
+#define Z_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    Z_TRY(dalloc(&q.cnt, max_pix));
+    Z_TRY(dalloc(&q.off, max_pix + 1));
+    Z_TRY(dalloc(&q.scnt, max_pix));
+    Z_TRY(dalloc(&q.soff, max_pix + 1));
+    Z_TRY(dalloc(&q.slist, max_pix));
+    Z_TRY(dalloc(&q.scan_tmp, scan_tile_count((uint32_t)max_pix) + 1));
+    q.pix_cap = max_pix;
+    b->nq.assign(b->n, 0u);
+    size_t max_q = 1;
+    for (int s = 0; s < b->n; ++s) {
+        const BatchRenderScene d = render_desc(b, s);
+        const uint32_t npix = (uint32_t)b->cfgs[s].width * (uint32_t)b->cfgs[s].height;
+        if (npix == 0) continue;
+        bool vol_on, surf_on;
+        query_flags(b, s, &vol_on, &surf_on);
+        Z_TRY(cache_count_queries(d.sc, d.R, vol_on, surf_on, q.cnt, q.scnt, 0));
+        Z_TRY(exclusive_scan_u32_large(q.cnt, q.off, npix, q.off + npix, q.scan_tmp, 0));
+        Z_TRY(cudaMemcpy(&b->nq[s], q.off + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        max_q = std::max(max_q, (size_t)b->nq[s]);
+    }
+    Z_TRY(dalloc(&q.qa, max_q));
+    Z_TRY(dalloc(&q.qd, max_q));
+    Z_TRY(dalloc(&q.val, max_q));
+    Z_TRY(dalloc(&q.key, max_q));
+    Z_TRY(dalloc(&q.ord, max_q));
+    Z_TRY(dalloc(&q.key_tmp, max_q));
+    Z_TRY(dalloc(&q.ord_tmp, max_q));
+    Z_TRY(dalloc(&q.hist, radix_sort_hist_words((uint32_t)max_q)));
+    Z_TRY(dalloc(&q.anchor_d, tile_chunks((uint32_t)max_q, 4)));
+    Z_TRY(dalloc(&q.defer_n, 1));
+    q.q_cap = max_q;
+#undef Z_TRY
+    return cudaSuccess;
+}
+
 // Pads and builds the two trees of scene s on `st` with sort scratch `so`.
 cudaError_t build_scene(pm_batch *b, int s, cudaStream_t st, const pm_batch::Sort &so) {
     for (int m = 0; m < 2; ++m) {
@@ -265,7 +412,9 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
         B_TRY(cudaEventRecord(b->join[k], b->side[k]));
         B_TRY(cudaStreamWaitEvent(st, b->join[k], 0));
     }
-    B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n, b->work, b->sm_count, st));
+    if (b->n_pixel > 0) B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n_pixel, b->work, b->sm_count, st));
+    for (int s = 0; s < b->n; ++s)
+        if (b->tune[s].query_list) B_TRY(enqueue_query_scene(b, s, st));
 #undef B_TRY
     return cudaSuccess;
 }
@@ -308,7 +457,7 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     uint32_t max_cap = 0, max_map = 1;
     for (int s = 0; s < n; ++s) {
         const pm_config &c = cfgs[s];
-        b->tune[s] = pm_batch_tune{c.leaf_size, 1, 128, 16};
+        b->tune[s] = pm_batch_tune{c.leaf_size, 1, 128, 16, 1};
         const uint32_t tmax = std::max(c.surface_photons, c.volume_photons);
         uint64_t cap = c.max_paths ? c.max_paths : (uint64_t)tmax * kPathCapFactor;
         cap = std::max<uint64_t>(cap, 1024);
@@ -404,7 +553,8 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     C_TRY(cudaMemcpy(b->scenes_dev, b->dsc.data(), sizeof(PScene) * n, cudaMemcpyHostToDevice));
     C_TRY(cudaMemcpy(b->count_dev, cp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
     C_TRY(cudaMemcpy(b->write_dev, wp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
-    C_TRY(upload_render(b, all_ids(b), b->render_dev, b->prefix_dev));
+    C_TRY(upload_pixel_scenes(b));
+    C_TRY(size_query_buffers(b));
     C_TRY(cudaDeviceSynchronize());
 #undef C_TRY
     *out = b;
@@ -511,13 +661,13 @@ pm_status pm_batch_set_tune(pm_batch *b, int scene, const pm_batch_tune *t) {
     if (!b || !t || scene < 0 || scene >= b->n) return PM_ERR_INVALID;
     if ((t->leaf_size != 32 && t->leaf_size != 64 && t->leaf_size != 128) || t->tile < 1 ||
         t->tile > 64 || (t->collect_max != 32 && t->collect_max != 64 && t->collect_max != 128) ||
-        t->merge_min < 1 || t->merge_min > 33)
+        t->merge_min < 1 || t->merge_min > 33 || (t->query_list != 0 && t->query_list != 1))
         return fail(b->ctx, PM_ERR_INVALID, "invalid batch tune");
     DeviceGuard g(b->ctx->device);
     cudaDeviceSynchronize();
     b->tune[scene] = *t;
     drop_graph(b);
-    cudaError_t e = upload_render(b, all_ids(b), b->render_dev, b->prefix_dev);
+    cudaError_t e = upload_pixel_scenes(b);
     if (e != cudaSuccess) return check_cuda(b->ctx, e, "pm_batch_set_tune");
     return PM_OK;
 }
@@ -552,12 +702,15 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
     const int leaves[3] = {32, 64, 128}, tiles[4] = {1, 2, 4, 8}, collects[3] = {32, 64, 128},
               merges[3] = {8, 16, 32};
     auto time_scene = [&](int s, float *ms_out) -> cudaError_t {
-        cudaError_t ee = upload_render(b, {s}, one, one_prefix);
+        const bool ql = b->tune[s].query_list != 0;
+        cudaError_t ee = ql ? cudaSuccess : upload_render(b, {s}, one, one_prefix);
         if (ee != cudaSuccess) return ee;
         float best = 3.0e38f;
         for (int rep = 0; rep < 3; ++rep) {
             ee = cudaEventRecord(t0, stream);
-            if (ee == cudaSuccess) ee = render_batch(one, one_prefix, 1, b->work, b->sm_count, stream);
+            if (ee == cudaSuccess)
+                ee = ql ? enqueue_query_scene(b, s, stream)
+                        : render_batch(one, one_prefix, 1, b->work, b->sm_count, stream);
             if (ee == cudaSuccess) ee = cudaEventRecord(t1, stream);
             if (ee == cudaSuccess) ee = cudaEventSynchronize(t1);
             if (ee != cudaSuccess) return ee;
@@ -581,6 +734,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
         float best_ms = 3.0e38f;
         for (int li = 0; li < 3; ++li) {
             b->tune[rep].leaf_size = leaves[li];
+            b->tune[rep].query_list = 0;
             A_TRY(build_scene(b, rep, stream, b->sort[0]));
             for (int ti = 0; ti < 4; ++ti) {
                 b->tune[rep].tile = tiles[ti];
@@ -590,8 +744,8 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
                 A_TRY(time_scene(rep, &ms));
                 char buf[160];
                 snprintf(buf, sizeof(buf), "%s{\"leaf_size\": %d, \"tile\": %d, \"collect_max\": 128, "
-                         "\"merge_min\": 16, \"ms\": %.4f}", trials.empty() ? "" : ", ", leaves[li],
-                         tiles[ti], ms);
+                         "\"merge_min\": 16, \"query_list\": 0, \"ms\": %.4f}", trials.empty() ? "" : ", ",
+                         leaves[li], tiles[ti], ms);
                 trials += buf;
                 if (ms < best_ms) { best_ms = ms; best = b->tune[rep]; }
             }
@@ -606,11 +760,28 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
                 A_TRY(time_scene(rep, &ms));
                 char buf[160];
                 snprintf(buf, sizeof(buf), ", {\"leaf_size\": %d, \"tile\": %d, \"collect_max\": %d, "
-                         "\"merge_min\": %d, \"ms\": %.4f}", best.leaf_size, best.tile, collects[ci],
-                         merges[mi], ms);
+                         "\"merge_min\": %d, \"query_list\": 0, \"ms\": %.4f}", best.leaf_size, best.tile,
+                         collects[ci], merges[mi], ms);
                 trials += buf;
                 if (ms < best_ms) { best_ms = ms; best = b->tune[rep]; }
             }
+        // the query-list render at each leaf size (its other knobs do not apply)
+        const pm_batch_tune pixel_best = best;
+        for (int li = 0; li < 3; ++li) {
+            b->tune[rep] = pixel_best;
+            b->tune[rep].leaf_size = leaves[li];
+            b->tune[rep].query_list = 1;
+            A_TRY(build_scene(b, rep, stream, b->sort[0]));
+            float ms;
+            A_TRY(time_scene(rep, &ms));
+            char buf[160];
+            snprintf(buf, sizeof(buf), ", {\"leaf_size\": %d, \"tile\": %d, \"collect_max\": %d, "
+                     "\"merge_min\": %d, \"query_list\": 1, \"ms\": %.4f}", leaves[li], pixel_best.tile,
+                     pixel_best.collect_max, pixel_best.merge_min, ms);
+            trials += buf;
+            if (ms < best_ms) { best_ms = ms; best = b->tune[rep]; }
+        }
+        b->tune[rep] = best;
         int members = 0;
         for (int s = 0; s < b->n; ++s)
             if (b->cfgs[s].k == kc) { b->tune[s] = best; ++members; }
@@ -618,9 +789,9 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
         char head[400];
         snprintf(head, sizeof(head), "%s{\"k\": %d, \"scenes\": %d, \"probe_scene\": %d, \"pixels\": %llu, "
                  "\"choice\": {\"leaf_size\": %d, \"tile\": %d, \"collect_max\": %d, \"merge_min\": %d, "
-                 "\"ms\": %.4f}, \"trials\": [", first_class ? "" : ", ", kc, members, rep,
-                 (unsigned long long)most, best.leaf_size, best.tile, best.collect_max, best.merge_min,
-                 best_ms);
+                 "\"query_list\": %d, \"ms\": %.4f}, \"trials\": [", first_class ? "" : ", ", kc, members,
+                 rep, (unsigned long long)most, best.leaf_size, best.tile, best.collect_max, best.merge_min,
+                 best.query_list, best_ms);
         js += head + trials + "]}";
         first_class = false;
     }
@@ -629,7 +800,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
     cudaEventDestroy(t1);
     cudaFree(one);
     cudaFree(one_prefix);
-    A_TRY(upload_render(b, all_ids(b), b->render_dev, b->prefix_dev));
+    A_TRY(upload_pixel_scenes(b));
     // every scene's trees follow the new leaf sizes from the next frame on
     A_TRY(enqueue_frame(b, stream));
     A_TRY(cudaStreamSynchronize(stream));

@@ -106,7 +106,9 @@ struct TileBuffers {
 // Warps of an estimate pass over n queries, `groups` groups of 32 per warp.
 uint32_t tile_chunks(uint32_t n, int groups);
 // k-NN estimates of the queries in spatial order (order[0..n) indexes qa/qd
-// and val), one shared candidate set per group of 32 neighbours, `groups`
+// and val; with n_dev, the first min(n, *n_dev): n is then a capacity and
+// the launch sizes do not depend on the count), one shared candidate set
+// per group of 32 neighbours, `groups`
 // (1-4) consecutive groups per warp of which the later ones are bounded by
 // the earlier (tile_gather.cu; use 1 when the groups are not neighbours): diffuse queries e / (pi r^2) / pi from the surface map,
 // volume queries e / (4/3 pi r^3) with the phase function toward wo from
@@ -114,8 +116,8 @@ uint32_t tile_chunks(uint32_t n, int groups);
 // was found) instead.
 cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView &vol,
                              const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
-                             int groups, int k, float radius, bool raw, float4 *val,
-                             const TileBuffers &buf, int sm_count, cudaStream_t s);
+                             const uint32_t *n_dev, int groups, int k, float radius, bool raw,
+                             float4 *val, const TileBuffers &buf, int sm_count, cudaStream_t s);
 
 // The render parameters pm_render passes for the installed configuration.
 inline RenderParams render_params(const PhysicalState *st) {

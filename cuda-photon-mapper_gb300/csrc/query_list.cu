@@ -144,7 +144,8 @@ cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s) {
     // the sort's other index array is free again: the deferred-query list
     const TileBuffers buf{ql.anchor_d, ql.order == ql.ord ? ql.ord_tmp : ql.ord, ql.defer_n, ql.gather_stats};
     QL_TRY(knn_values_tiles(st->dscene, view_of(st->map[0]), view_of(st->map[1]), ql.qa, ql.qd, ql.order,
-                            ql.nq, 4, st->cfg.k, st->cfg.radius, true, ql.val, buf, st->sm_count, s));
+                            ql.nq, nullptr, 4, st->cfg.k, st->cfg.radius, true, ql.val, buf, st->sm_count,
+                            s));
 #undef QL_TRY
     return cudaSuccess;
 }

@@ -497,10 +497,11 @@ __device__ __forceinline__ void tighten(const Query &q, unsigned mask, float d_l
 template <int S>
 __global__ void __launch_bounds__(kTileWarps * 32, 5)
     query_knn_tile_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
-                          const uint32_t *order, uint32_t n, int groups, const float *anchor_d, int k,
-                          float r2cap, bool raw, float4 *out, uint32_t *defer_list, uint32_t *defer_n,
-                          unsigned long long *stats) {
+                          const uint32_t *order, uint32_t n, const uint32_t *n_dev, int groups,
+                          const float *anchor_d, int k, float r2cap, bool raw, float4 *out,
+                          uint32_t *defer_list, uint32_t *defer_n, unsigned long long *stats) {
     const int lane = threadIdx.x & 31;
+    if (n_dev) n = min(n, *n_dev);
     if (threadIdx.x == 0) {
         targs().map[0] = surf;
         targs().map[1] = vol;
@@ -611,8 +612,9 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
 template <int S>
 __global__ void __launch_bounds__(128)
     anchor_kernel(MapView surf, MapView vol, const float4 *qa, const uint32_t *order, uint32_t n,
-                  int groups, int k, float r2cap, float *anchor_d) {
+                  const uint32_t *n_dev, int groups, int k, float r2cap, float *anchor_d) {
     __shared__ WarpScratch ws[4];
+    if (n_dev) n = min(n, *n_dev);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t chunk = blockIdx.x * 4 + wib;
     const uint32_t wfirst = chunk * (uint32_t)(32 * groups);
@@ -656,8 +658,8 @@ __global__ void __launch_bounds__(128)
 
 cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView &vol,
                              const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
-                             int groups, int k, float radius, bool raw, float4 *val,
-                             const TileBuffers &buf, int sm_count, cudaStream_t s) {
+                             const uint32_t *n_dev, int groups, int k, float radius, bool raw,
+                             float4 *val, const TileBuffers &buf, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if (groups < 1 || groups > 4) return cudaErrorInvalidValue;
     const float r2 = radius * radius;
@@ -668,10 +670,10 @@ cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView
     cudaError_t e = cudaMemsetAsync(buf.defer_n, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
 #define PM_TILE_LAUNCH(SL)                                                                              \
-    anchor_kernel<SL><<<grid, block, 0, s>>>(surf, vol, qa, order, n, groups, k, r2, buf.anchor_d);      \
+    anchor_kernel<SL><<<grid, block, 0, s>>>(surf, vol, qa, order, n, n_dev, groups, k, r2, buf.anchor_d); \
     e = cudaFuncSetAttribute(query_knn_tile_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
     if (e != cudaSuccess) return e;                                                                     \
-    query_knn_tile_kernel<SL><<<grid, block, smem, s>>>(S, surf, vol, qa, qd, order, n, groups, buf.anchor_d, k, \
+    query_knn_tile_kernel<SL><<<grid, block, smem, s>>>(S, surf, vol, qa, qd, order, n, n_dev, groups, buf.anchor_d, k, \
                                                         r2, raw, val, buf.defer, buf.defer_n, buf.stats); \
     deferred_kernel<SL><<<dgrid, 128, 0, s>>>(S, surf, vol, qa, qd, buf.defer, buf.defer_n, k, r2, raw, val)
     switch ((k + 31) / 32) {

@@ -94,7 +94,7 @@ class CacheStats(_c.Structure):
 
 class BatchTune(_c.Structure):
     _fields_ = [("leaf_size", _c.c_int), ("tile", _c.c_int), ("collect_max", _c.c_int),
-                ("merge_min", _c.c_int)]
+                ("merge_min", _c.c_int), ("query_list", _c.c_int)]
 
 
 CACHE_WEIGHTS = 4 * 64 * 64 + 64 * 16
@@ -537,8 +537,8 @@ class Batch:
         self.ctx._check(self.lib.pm_batch_stats(self.h, i, _c.byref(st)), "pm_batch_stats")
         return st
 
-    def set_tune(self, i, leaf_size=32, tile=1, collect_max=128, merge_min=16):
-        t = BatchTune(leaf_size, tile, collect_max, merge_min)
+    def set_tune(self, i, leaf_size=32, tile=1, collect_max=128, merge_min=16, query_list=1):
+        t = BatchTune(leaf_size, tile, collect_max, merge_min, query_list)
         self.ctx._check(self.lib.pm_batch_set_tune(self.h, i, _c.byref(t)), "pm_batch_set_tune")
 
     def get_tune(self, i):

@@ -413,19 +413,24 @@ PM_API pm_status pm_cache_load(pm_ctx *ctx, const char *path);
  * runs a frame of all of them as: one persistent trace launch over every
  * scene's photon paths (counting pass), per-scene record extents without a
  * host round trip, one persistent trace launch (writing pass), per-scene
- * kd-tree builds on side streams, and one persistent render launch that
- * hands out pixel chunks of all scenes dynamically. Because no step reads a
- * count back to the host, the whole frame can be captured as a CUDA graph
- * (pm_batch_capture) and replayed (pm_batch_launch). Every scene's image is
- * bit-identical to a single-scene pm_emit + pm_build + pm_render with the
- * same scene, config and path cap. */
+ * kd-tree builds on side streams, then the render: scenes in query-list
+ * mode one after another through pm_render's pipeline (query list, spatial
+ * sort, shared candidate sets, composite; buffers sized at creation for the
+ * largest scene, counts kept on the device), the others in one persistent
+ * launch that hands out pixel chunks of all of them dynamically. Because no
+ * step reads a count back to the host, the whole frame can be captured as a
+ * CUDA graph (pm_batch_capture) and replayed (pm_batch_launch). Every
+ * scene's image is bit-identical to a single-scene pm_emit + pm_build +
+ * pm_render with the same scene, config and path cap. */
 typedef struct pm_batch pm_batch;
 /* Search knobs of one scene that change speed, never results: records per
- * kd leaf (32, 64, 128), pixels per warp per work chunk (1..64), records
- * collected before the first k-list sort (32, 64, 128), and the leaf
- * candidates at or above which insertion is one bulk merge (1..33). */
+ * kd leaf (32, 64, 128); query_list 1: render through the query list with
+ * shared candidate sets (the default), 0: in the persistent per-pixel
+ * launch, where the rest apply -- pixels per warp per work chunk (1..64),
+ * records collected before the first k-list sort (32, 64, 128), and the
+ * leaf candidates at or above which insertion is one bulk merge (1..33). */
 typedef struct pm_batch_tune {
-    int leaf_size, tile, collect_max, merge_min;
+    int leaf_size, tile, collect_max, merge_min, query_list;
 } pm_batch_tune;
 /* Scene `index` of the batched benchmark workload: 2..32 seeded spheres,
  * sigma_s in [0, 0.2], photons log-uniform in [1e5, 4e6] (half per map),

@@ -94,14 +94,16 @@ def test_search_knobs_do_not_change_images(ctx):
     b = photonmap.Batch(ctx, scenes, cfgs)
     b.frame()
     ref = batch_images(b, cfgs)
-    for leaf, tile, collect, merge in [(64, 4, 32, 8), (128, 2, 64, 33), (32, 8, 128, 1)]:
+    for leaf, tile, collect, merge, ql in [(64, 4, 32, 8, 0), (128, 2, 64, 33, 0), (32, 8, 128, 1, 0),
+                                           (64, 1, 128, 16, 1), (128, 1, 128, 16, 1)]:
         for i in range(len(cfgs)):
-            b.set_tune(i, leaf, tile, collect, merge)
+            # mixed: odd scenes in the other render mode
+            b.set_tune(i, leaf, tile, collect, merge, ql if i % 2 == 0 else 1 - ql)
         b.frame()
         got = batch_images(b, cfgs)
         for i, (a, r) in enumerate(zip(got, ref)):
             np.testing.assert_array_equal(bits(a), bits(r), err_msg="scene %d %s" % (
-                i, (leaf, tile, collect, merge)))
+                i, (leaf, tile, collect, merge, ql)))
     b.close()
 
 
@@ -116,14 +118,15 @@ def test_autotune_writes_its_trials(ctx, tmp_path):
     ks = sorted({cf.k for cf in cfgs})
     assert [c["k"] for c in doc["classes"]] == ks
     for c in doc["classes"]:
-        assert len(c["trials"]) == 12 + 9
+        assert len(c["trials"]) == 12 + 9 + 3
+        assert sorted({t["query_list"] for t in c["trials"]}) == [0, 1]
         assert c["choice"]["ms"] == min(t["ms"] for t in c["trials"])
         for i, cf in enumerate(cfgs):
             if cf.k == c["k"]:
                 t = b.get_tune(i)
-                assert (t.leaf_size, t.tile, t.collect_max, t.merge_min) == (
+                assert (t.leaf_size, t.tile, t.collect_max, t.merge_min, t.query_list) == (
                     c["choice"]["leaf_size"], c["choice"]["tile"], c["choice"]["collect_max"],
-                    c["choice"]["merge_min"])
+                    c["choice"]["merge_min"], c["choice"]["query_list"])
     got = batch_images(b, cfgs)
     for a, r in zip(got, ref):
         np.testing.assert_array_equal(bits(a), bits(r))
