@@ -352,7 +352,8 @@ def batch_frames(ctx, lib, args, device):
         "records_per_frame": records, "pixels_per_frame": pixels,
         "gathers_per_s": gathers / frame_s, "photon_paths_per_s": paths / frame_s,
         "graph_kernels_per_frame": launches // max(1, args.batch_steps),
-        "knobs": "defaults (leaf 32, tile 1, collect 128, merge 16); pm_batch_autotune picks per k",
+        "knobs": "defaults (leaf 32, query-list render; per-pixel knobs tile 1, collect 128, "
+                 "merge 16); pm_batch_autotune picks per k",
         "clocks": clk,
     }
 
