@@ -631,12 +631,16 @@ __global__ void half_copy_kernel(const float *p, __half2 *ph, uint32_t npairs) {
 }
 
 struct CountSink {
+    static constexpr bool kCountOnly = true;
     uint32_t n = 0, ns = 0;
+    __device__ void volume_steps(int steps) { n += (uint32_t)steps; }
     __device__ void volume(v3, v3, float) { ++n; }
     __device__ void surface(v3, int, v3, float) { ++n; ++ns; }
 };
 
 struct WriteSink {
+    static constexpr bool kCountOnly = false;
+    __device__ void volume_steps(int) {}
     float4 *qa, *qd;
     uint32_t *slist;
     uint32_t at, sat;

@@ -140,13 +140,13 @@ void pm_cache_default_config(pm_cache_config *cfg) {
     cfg->base_res = 16;
     cfg->max_res = 2048;
     cfg->train_samples = 1u << 20;
-    cfg->batch = 1u << 17;  // 8 steps per frame, each filling every SM
-    cfg->lr = 3e-2f;
+    cfg->batch = 1u << 18;  // 4 steps per frame, each filling every SM
+    cfg->lr = 5e-2f;
     cfg->beta1 = 0.9f;
     cfg->beta2 = 0.99f;
     cfg->eps = 1e-15f;
     cfg->lr_min = 1e-3f;
-    cfg->lr_half_life = 400.0f;
+    cfg->lr_half_life = 300.0f;
     cfg->loss_eps = 1.0f;
     cfg->surface_fraction = 0.5f;
     cfg->seed = 0x5EED0004ull;

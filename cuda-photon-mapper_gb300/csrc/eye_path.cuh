@@ -22,6 +22,10 @@ constexpr int kMaxMarchSteps = 1 << 16;  // per segment
 // Sink interface:
 //   void volume(v3 x, v3 wo, float w)         in-scattering query, w = T(mid) * dt
 //   void surface(v3 x, int obj, v3 wo, float w) diffuse query,   w = T(hit)
+//   static constexpr bool kCountOnly          true: volume_steps(n) replaces the
+//   void volume_steps(int n)                  n volume() calls of a march segment
+// (the path itself never depends on the transmittance, so a counting sink
+// needs no march step).
 template <class Sink>
 __device__ __forceinline__ void walk_eye(const PScene &Sc, const RenderParams &R, uint32_t pix,
                                          bool vol_on, bool surf_on, Sink &sink) {
@@ -42,7 +46,9 @@ __device__ __forceinline__ void walk_eye(const PScene &Sc, const RenderParams &R
             if (t0 < t1) {
                 const int nst = (int)fminf(ceilf((t1 - t0) / R.step), (float)kMaxMarchSteps);
                 const v3 wo = d * -1.0f;
-                for (int j = 0; j < nst; ++j) {
+                if constexpr (Sink::kCountOnly) {
+                    if (vol_on) sink.volume_steps(nst);
+                } else for (int j = 0; j < nst; ++j) {
                     const float ta = t0 + (float)j * R.step;
                     const float tb = fminf(t0 + (float)(j + 1) * R.step, t1);
                     const float dt = tb - ta;

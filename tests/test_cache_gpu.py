@@ -169,7 +169,7 @@ def test_cache_file_round_trip(ctx, tmp_path):
 def test_cached_render_against_float64_at_bench_scale(ctx):
     """The A/B of the benchmark scene (preset 2: 1M + 1M photons, 1024^2,
     k = 100): the cached render after 384 online training frames (2^20
-    samples and 8 Adam steps each) and the
+    samples and 4 Adam steps each) and the
     k-NN render, both against the FP64 oracle render on 8192 random pixels.
     The target: the cached render within 1e-2 relative RMSE of the FP64
     render (the k-NN render's own error is ~0.3 %). Training adds gradients
