@@ -186,6 +186,38 @@ def test_query_list_render_equals_single_kernel(ctx, preset, size, k, radius, ph
     assert st.surface_gathers > 0
 
 
+def test_render_with_massive_distance_ties(ctx):
+    """Maps whose records sit on a lattice, every point 40 times: the k-th
+    distance of most queries is shared by dozens of records, so the
+    shared-candidate selection has to rank more than 32 records at one
+    distance by photon index. The image equals the single-kernel render's."""
+    sc, cf = small(1, 1000, 1000, (40, 32), k=64, radius=0.1)
+    ctx.set_scene(sc, cf)
+    g = np.stack(np.meshgrid(np.arange(-0.5, 0.51, 0.1), np.arange(0.0, 1.01, 0.1),
+                             np.arange(-0.5, 0.51, 0.1), indexing="ij"), -1).reshape(-1, 3)
+    g = np.repeat(g, 40, axis=0).astype(np.float32)
+    rs = np.random.RandomState(11)
+    for mid in (0, 1):
+        perm = rs.permutation(len(g))
+        pos = np.zeros((len(g), 4), np.float32)
+        pos[:, :3] = g[perm]
+        pos[:, 3] = np.arange(len(g), dtype=np.uint32).view(np.float32)
+        pw = np.zeros((len(g), 4), np.float32)
+        pw[:, :3] = rs.uniform(1e-4, 1e-3, (len(g), 3))
+        pw[:, 3] = rs.randint(0, 2**32, len(g), dtype=np.uint64).astype(np.uint32).view(np.float32)
+        ctx.set_photons(mid, pos, pw)
+    ctx.build()
+    n = cf.width * cf.height
+    rad = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    rad1 = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    ctx.render(rad.data_ptr(), None)
+    ctx.render_single_kernel(rad1.data_ptr(), None)
+    torch.cuda.synchronize()
+    a, b = rad.cpu().numpy(), rad1.cpu().numpy()
+    np.testing.assert_array_equal(bits(a), bits(b))
+    assert a[:, :3].max() > 0.0
+
+
 def test_gather_stats_of_the_shared_candidate_sets(ctx):
     """The k-NN estimates of a frame mostly come from shared candidate
     sets, and no result contradicts its distance bound."""
