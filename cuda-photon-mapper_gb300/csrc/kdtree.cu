@@ -91,6 +91,132 @@ __global__ void split_cell_kernel(const float4 *__restrict__ pos, const uint32_t
     cell_hi[2 * g + 1] = rhi;
 }
 
+// The levels below a node of at most kSubtreeMax records are finished by
+// one CTA in shared memory: per level, a bitonic sort of the composite keys
+// (node within the subtree, the same 16-bit quantised coordinate as
+// split_key_kernel, position before the level) -- exactly the order of the
+// global stable sort by (node, coordinate) -- then the children's cells cut
+// at the coordinate of each node's right half's first record, as
+// split_cell_kernel does. The tree comes out identical; the deep levels,
+// whose global sorts carry the most node bits, cost one pass over the
+// records instead of several per level.
+constexpr int kSubtreeMax = 2048;
+constexpr int kSubtreeThreads = 512;
+constexpr int kSubtreeNodes = kSubtreeMax / 32;  // nodes of a subtree level (leaves of >= 32)
+
+struct SubtreeScratch {
+    uint64_t key[kSubtreeMax];
+    float4 p[kSubtreeMax];
+    uint32_t idx[kSubtreeMax];
+    float4 clo[2][2 * kSubtreeNodes], chi[2][2 * kSubtreeNodes];
+};
+
+__global__ void __launch_bounds__(kSubtreeThreads)
+    subtree_finish_kernel(const float4 *__restrict__ pos, uint32_t *order, uint32_t n, int l0, int D,
+                          uint32_t span0, const float4 *__restrict__ cell_lo,
+                          const float4 *__restrict__ cell_hi) {
+    extern __shared__ __align__(16) unsigned char subtree_smem[];
+    SubtreeScratch &ss = *reinterpret_cast<SubtreeScratch *>(subtree_smem);
+    const uint32_t j = blockIdx.x;
+    const uint32_t start = j * span0;
+    if (start >= n) return;
+    const int cnt = (int)min(span0, n - start);
+    const int tid = threadIdx.x;
+    for (int t = tid; t < cnt; t += blockDim.x) {
+        const uint32_t r = order[start + t];
+        ss.idx[t] = r;
+        ss.p[t] = pos[r];
+    }
+    if (tid == 0) {
+        ss.clo[0][0] = cell_lo[(1u << l0) + j];
+        ss.chi[0][0] = cell_hi[(1u << l0) + j];
+    }
+    int P = 2;
+    while (P < cnt) P <<= 1;
+    int cur = 0;
+    __syncthreads();
+    for (int l = l0; l < D; ++l) {
+        const int nspan = (int)(span0 >> (l - l0));  // records per node at this level
+        // keys
+        for (int t = tid; t < P; t += blockDim.x) {
+            uint64_t key = ~0ull;
+            if (t < cnt) {
+                const int node = t / nspan;
+                const float4 lo = ss.clo[cur][node], hi = ss.chi[cur][node];
+                const int ax = longest_axis(lo, hi);
+                const float4 q = ss.p[t];
+                const float c = ax == 0 ? q.x : (ax == 1 ? q.y : q.z);
+                const float c0 = ax == 0 ? lo.x : (ax == 1 ? lo.y : lo.z);
+                const float c1 = ax == 0 ? hi.x : (ax == 1 ? hi.y : hi.z);
+                const float f = (c - c0) / (c1 - c0) * 65536.0f;
+                const uint32_t qc = !(f > 0.0f) ? 0u : (f >= 65535.0f ? 65535u : (uint32_t)f);
+                key = ((uint64_t)node << 48) | ((uint64_t)qc << 32) | (uint32_t)t;
+            }
+            ss.key[t] = key;
+        }
+        __syncthreads();
+        for (int size = 2; size <= P; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int t = tid; t < (P >> 1); t += blockDim.x) {
+                    const int i = ((t & ~(stride - 1)) << 1) | (t & (stride - 1));
+                    const int k = i + stride;
+                    const bool up = (i & size) == 0;
+                    const uint64_t a = ss.key[i], b = ss.key[k];
+                    if ((a > b) == up) {
+                        ss.key[i] = b;
+                        ss.key[k] = a;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // the records in the new order
+        float4 np[kSubtreeMax / kSubtreeThreads];
+        uint32_t ni[kSubtreeMax / kSubtreeThreads];
+#pragma unroll
+        for (int u = 0; u < kSubtreeMax / kSubtreeThreads; ++u) {
+            const int t = tid + u * kSubtreeThreads;
+            if (t < cnt) {
+                const uint32_t old = (uint32_t)ss.key[t];
+                np[u] = ss.p[old];
+                ni[u] = ss.idx[old];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < kSubtreeMax / kSubtreeThreads; ++u) {
+            const int t = tid + u * kSubtreeThreads;
+            if (t < cnt) {
+                ss.p[t] = np[u];
+                ss.idx[t] = ni[u];
+            }
+        }
+        __syncthreads();
+        // the children's cells
+        const int nodes = (cnt + nspan - 1) / nspan, half = nspan >> 1;
+        for (int node = tid; node < nodes; node += blockDim.x) {
+            const float4 lo = ss.clo[cur][node], hi = ss.chi[cur][node];
+            float4 llo = lo, lhi = hi, rlo = lo, rhi = hi;
+            const int ncnt = min(nspan, cnt - node * nspan);
+            if (ncnt > half) {
+                const int ax = longest_axis(lo, hi);
+                const float4 q = ss.p[node * nspan + half];
+                const float m = ax == 0 ? q.x : (ax == 1 ? q.y : q.z);
+                if (ax == 0) { lhi.x = m; rlo.x = m; }
+                else if (ax == 1) { lhi.y = m; rlo.y = m; }
+                else { lhi.z = m; rlo.z = m; }
+            }
+            ss.clo[cur ^ 1][2 * node] = llo;
+            ss.chi[cur ^ 1][2 * node] = lhi;
+            ss.clo[cur ^ 1][2 * node + 1] = rlo;
+            ss.chi[cur ^ 1][2 * node + 1] = rhi;
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (int t = tid; t < cnt; t += blockDim.x) order[start + t] = ss.idx[t];
+}
+
 __global__ void iota_kernel(uint32_t *v, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) v[i] = i;
@@ -197,7 +323,15 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     } else {
         root_cell_kernel<<<1, 1, 0, s>>>(a.lo, a.hi, a.box_dev, a.node_lo, a.node_hi); note_launch();
     }
-    for (int l = 0; l < D; ++l) {
+    // levels [lf, D) are finished per subtree in shared memory
+    const uint32_t leaf = 32u << a.leaf_shift;
+    int lf = D;
+    while (lf > 0 && ((uint64_t)leaf << (D - (lf - 1))) <= (uint64_t)kSubtreeMax) --lf;
+    if (lf == 0 && D > 0) {
+        iota_kernel<<<blocks, 256, 0, s>>>(va, n);
+        note_launch();
+    }
+    for (int l = 0; l < lf; ++l) {
         const uint32_t span = (32u << a.leaf_shift) << (D - l);
         const uint32_t nodes = (n + span - 1) / span;
         split_key_kernel<<<blocks, 256, 0, s>>>(a.pos_in, l == 0 ? nullptr : va, n, l, span,
@@ -214,6 +348,16 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         }
         split_cell_kernel<<<(nodes + 255) / 256, 256, 0, s>>>(a.pos_in, va, n, l, span, nodes,
                                                                a.node_lo, a.node_hi); note_launch();
+    }
+    if (lf < D) {
+        const uint32_t span = leaf << (D - lf);
+        const uint32_t nodes = (n + span - 1) / span;
+        const int smem = (int)sizeof(SubtreeScratch);
+        e = cudaFuncSetAttribute(subtree_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        subtree_finish_kernel<<<nodes, kSubtreeThreads, smem, s>>>(a.pos_in, va, n, lf, D, span, a.node_lo,
+                                                                   a.node_hi);
+        note_launch();
     }
     permute_kernel<<<blocks, 256, 0, s>>>(va, n, a.pos_in, a.pow_in, a.pos_out, a.pow_out, a.dir_out);
     note_launch();
