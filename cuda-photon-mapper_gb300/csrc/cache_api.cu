@@ -139,14 +139,17 @@ void pm_cache_default_config(pm_cache_config *cfg) {
     cfg->log2_table = 19;
     cfg->base_res = 16;
     cfg->max_res = 2048;
-    cfg->train_samples = 1u << 20;
-    cfg->batch = 1u << 18;  // 4 steps per frame, each filling every SM
+    // 12 Adam steps of 2^15 per frame: the image error falls with the steps
+    // per frame far more than with the fresh samples, and the k-NN targets
+    // are the frame's dearest part
+    cfg->train_samples = 3u << 17;
+    cfg->batch = 1u << 15;
     cfg->lr = 5e-2f;
     cfg->beta1 = 0.9f;
     cfg->beta2 = 0.99f;
     cfg->eps = 1e-15f;
     cfg->lr_min = 1e-3f;
-    cfg->lr_half_life = 300.0f;
+    cfg->lr_half_life = 450.0f;
     cfg->loss_eps = 1.0f;
     cfg->surface_fraction = 0.5f;
     cfg->seed = 0x5EED0004ull;

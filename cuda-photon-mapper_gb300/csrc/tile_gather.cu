@@ -40,6 +40,8 @@ using namespace wknn;
 constexpr int kTileWarps = 4;
 constexpr int kAnchorAt = 15;                // the anchor: query 15 of a warp's chunk
 constexpr int kTileCap = 384;                // candidate records per warp (slots fit 16 bits)
+constexpr int kScanSlots = 2;   // candidates per lane per step of the selection scan
+constexpr int kPickSlots = 1;   // band entries per lane per step of the final selection
 constexpr float kRel = 2e-4f;                // relative and absolute margins of the distance bounds
 constexpr float kAbs = 1e-6f;
 
@@ -317,30 +319,48 @@ __device__ __forceinline__ Pick pick_k(int n, v3 q, float lo2, float hi2) {
     const uint64_t cap = targs().cap;
     const unsigned lt = (1u << lane) - 1u;
     int n_in = 0, B = 0;
-    for (int base = 0; base < n; base += 32) {
-        const int c = base + lane;
-        bool in = false, band = false;
-        float d2 = 0.0f;
-        if (c < n) {
-            const float4 p = ts.cpos[c];
-            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-            d2 = dx * dx + dy * dy + dz * dz;
-            in = d2 < lo2;
-            band = !in && d2 <= hi2 && make_key(d2, __float_as_uint(p.w)) < cap;
+    // kScanSlots slots per lane and step: their loads and distances are
+    // independent; the ballots and stores keep slot order
+    for (int base = 0; base < n; base += 32 * kScanSlots) {
+        bool in[kScanSlots], band[kScanSlots];
+        float d2[kScanSlots];
+        unsigned mi[kScanSlots], mb[kScanSlots];
+#pragma unroll
+        for (int u = 0; u < kScanSlots; ++u) {
+            const int c = base + 32 * u + lane;
+            in[u] = band[u] = false;
+            d2[u] = 0.0f;
+            if (c < n) {
+                const float4 p = ts.cpos[c];
+                const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                d2[u] = dx * dx + dy * dy + dz * dz;
+                in[u] = d2[u] < lo2;
+                band[u] = !in[u] && d2[u] <= hi2 && make_key(d2[u], __float_as_uint(p.w)) < cap;
+            }
         }
-        const unsigned mi = __ballot_sync(kFull, in), mb = __ballot_sync(kFull, band);
-        if (n_in + __popc(mi) >= k) {  // the lower bound was too high
+        int tin = 0;
+#pragma unroll
+        for (int u = 0; u < kScanSlots; ++u) {
+            mi[u] = __ballot_sync(kFull, in[u]);
+            mb[u] = __ballot_sync(kFull, band[u]);
+            tin += __popc(mi[u]);
+        }
+        if (n_in + tin >= k) {  // the lower bound was too high
             __syncwarp();
             return Pick{0, false, 0};
         }
-        if (in) ts.b.sel[n_in + __popc(mi & lt)] = (uint16_t)c;
-        if (band) {
-            const int at = B + __popc(mb & lt);
-            ts.b.bd2[at] = d2;
-            ts.b.bslot[at] = (uint16_t)c;
+#pragma unroll
+        for (int u = 0; u < kScanSlots; ++u) {
+            const int c = base + 32 * u + lane;
+            if (in[u]) ts.b.sel[n_in + __popc(mi[u] & lt)] = (uint16_t)c;
+            if (band[u]) {
+                const int at = B + __popc(mb[u] & lt);
+                ts.b.bd2[at] = d2[u];
+                ts.b.bslot[at] = (uint16_t)c;
+            }
+            n_in += __popc(mi[u]);
+            B += __popc(mb[u]);
         }
-        n_in += __popc(mi);
-        B += __popc(mb);
     }
     __syncwarp();
     const int need = k - n_in;
@@ -352,17 +372,25 @@ __device__ __forceinline__ Pick pick_k(int n, v3 q, float lo2, float hi2) {
     }
     const uint64_t kth = band_select(B, need, lo2, hi2);
     int sel = n_in;
-    for (int base = 0; base < B; base += 32) {
-        const int e = base + lane;
-        bool s = false;
-        uint16_t slot = 0;
-        if (e < B) {
-            slot = ts.b.bslot[e];
-            s = make_key(ts.b.bd2[e], __float_as_uint(ts.cpos[slot].w)) <= kth;
+    for (int base = 0; base < B; base += 32 * kPickSlots) {
+        bool sl[kPickSlots];
+        uint16_t slot[kPickSlots];
+#pragma unroll
+        for (int u = 0; u < kPickSlots; ++u) {
+            const int e = base + 32 * u + lane;
+            sl[u] = false;
+            slot[u] = 0;
+            if (e < B) {
+                slot[u] = ts.b.bslot[e];
+                sl[u] = make_key(ts.b.bd2[e], __float_as_uint(ts.cpos[slot[u]].w)) <= kth;
+            }
         }
-        const unsigned ms = __ballot_sync(kFull, s);
-        if (s) ts.b.sel[sel + __popc(ms & lt)] = slot;
-        sel += __popc(ms);
+#pragma unroll
+        for (int u = 0; u < kPickSlots; ++u) {
+            const unsigned ms = __ballot_sync(kFull, sl[u]);
+            if (sl[u]) ts.b.sel[sel + __popc(ms & lt)] = slot[u];
+            sel += __popc(ms);
+        }
     }
     __syncwarp();
     return Pick{sel, true, kth};
