@@ -226,7 +226,7 @@ CACHE_TRAIN_FLOPS = 2 * CACHE_INFER_FLOPS + 2 * (2 * 128 * 128 + 128 * 16)
 def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak):
     """The learned radiance cache on the same scene and photon maps: after
     `cache_warm_frames` online training frames, each timed step is one online
-    frame (the default 393,216 k-NN training samples + their 12 Adam steps, then the cached
+    frame (2^20 k-NN training samples + their Adam steps, then the cached
     render of every query). Error is the relative RMSE of the cached image
     against the k-NN render of the same frame (the cache's judge)."""
     import numpy as np

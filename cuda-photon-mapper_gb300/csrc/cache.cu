@@ -499,7 +499,7 @@ constexpr uint32_t kInferSmem = kOffAct + 16384u * kInferPipes;
 
 __global__ void __launch_bounds__(kThreads * kInferPipes)
     infer_kernel(CacheGrid g, CacheParams p, PScene Sc, const float4 *qa, const float4 *qd,
-                 uint32_t n, float out_scale, float4 *val) {
+                 const uint32_t *order, uint32_t n, float out_scale, float4 *val) {
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ __align__(8) uint64_t mbar[kInferPipes], wbar;
     __shared__ uint32_t taddr_s;
@@ -525,10 +525,12 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
     bool ok = abort_s[pipe] == 0;
     for (uint32_t tile = blockIdx.x * kInferPipes + pipe; tile < ntiles && ok;
          tile += gridDim.x * kInferPipes) {
-        const uint32_t i = tile * kThreads + s;
-        const bool valid = i < n;
+        const uint32_t j = tile * kThreads + s;
+        const bool valid = j < n;
+        uint32_t i = j;
         float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
         if (valid) {
+            if (order) i = order[j];
             a = qa[i];
             d = qd[i];
         }
@@ -674,6 +676,31 @@ __global__ void write_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_o
     if (pix >= (uint32_t)R.width * (uint32_t)R.height) return;
     WriteSink w{qa, qd, slist, off[pix], soff[pix]};
     walk_eye(Sc, R, pix, vol_on, surf_on, w);
+}
+
+// The queries of each block of 32 consecutive pixels (one contiguous range
+// of the list) in sample-major order: sample 0 of every pixel of the block,
+// then sample 1, ... -- neighbouring rays at similar depths, whose hash-grid
+// corners coincide on the middle levels, instead of one ray's march.
+__global__ void pixel_block_order_kernel(const uint32_t *off, uint32_t npix, uint32_t *order) {
+    const uint32_t first = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u;
+    if (first >= npix) return;  // whole warps
+    const int lane = threadIdx.x & 31;
+    const uint32_t px = first + (uint32_t)lane;
+    uint32_t o = 0, c = 0;
+    if (px < npix) {
+        o = off[px];
+        c = off[px + 1] - o;
+    }
+    uint32_t base = __shfl_sync(0xffffffffu, o, 0);
+    const uint32_t cmax = __reduce_max_sync(0xffffffffu, c);
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t s = 0; s < cmax; ++s) {
+        const bool act = s < c;
+        const unsigned m = __ballot_sync(0xffffffffu, act);
+        if (act) order[base + __popc(m & lt)] = o + s;
+        base += __popc(m);
+    }
 }
 
 __global__ void composite_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
@@ -919,9 +946,18 @@ cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t cache_pixel_block_order(const uint32_t *off, uint32_t npix, uint32_t *order,
+                                    cudaStream_t s) {
+    if (npix == 0) return cudaSuccess;
+    const uint32_t warps = (npix + 31) / 32;
+    pixel_block_order_kernel<<<(warps + 7) / 8, 256, 0, s>>>(off, npix, order);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &S,
-                        const float4 *qa, const float4 *qd, uint32_t n, float out_scale,
-                        float4 *val, int sm_count, cudaStream_t s) {
+                        const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
+                        float out_scale, float4 *val, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     cudaError_t ea = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)kInferSmem);
@@ -934,7 +970,8 @@ cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &
     per_sm = std::max(per_sm, 1);
     const uint32_t ctas = (ntiles + kInferPipes - 1) / kInferPipes;
     const uint32_t grid = std::min<uint32_t>(ctas, (uint32_t)sm_count * (uint32_t)per_sm);
-    infer_kernel<<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, n, out_scale, val);
+    infer_kernel<<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, order, n, out_scale,
+                                                                   val);
     note_launch();
     return cudaGetLastError();
 }

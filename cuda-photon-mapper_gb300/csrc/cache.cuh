@@ -116,9 +116,15 @@ cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s);
 // steps and refresh p.w_img.
 cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float beta1,
                        float beta2, float eps, int step, cudaStream_t s);
-// val[i] = max(network(query i), 0) * out_scale for the first n queries.
+// val[i] = max(network(query i), 0) * out_scale for the first n queries,
+// taken in the order order[0..n) (nullable: index order).
 cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &S,
-                        const float4 *qa, const float4 *qd, uint32_t n, float out_scale,
-                        float4 *val, int sm_count, cudaStream_t s);
+                        const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
+                        float out_scale, float4 *val, int sm_count, cudaStream_t s);
+// order: every query index once, the queries of each block of 32
+// consecutive pixels (off: the per-pixel exclusive scan, npix + 1 entries)
+// kept in the block's range, sample-major within it.
+cudaError_t cache_pixel_block_order(const uint32_t *off, uint32_t npix, uint32_t *order,
+                                    cudaStream_t s);
 
 }  // namespace pm

@@ -27,6 +27,9 @@ struct CacheState {
     // targets, and their positions in the random order training reads
     uint32_t *skey = nullptr, *sval = nullptr, *skey_tmp = nullptr, *sval_tmp = nullptr;
     uint32_t *shist = nullptr, *sn = nullptr;
+    // the order inference takes the render's queries in
+    uint32_t *iorder = nullptr;
+    uint32_t iorder_cap = 0;
     float *scale_sum = nullptr;
     float target_scale = 0.0f;  // 0: set from the first training frame
     unsigned long long steps = 0, frames = 0;
@@ -76,7 +79,7 @@ void free_cache(CacheState *c) {
     cudaFree(c->p.w_part);
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
     cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status); cudaFree(c->p.w_img);
-    cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum);
+    cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum); cudaFree(c->iorder);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
     cudaFree(c->shist); cudaFree(c->sn);
     for (auto &e : c->ev)
@@ -139,17 +142,14 @@ void pm_cache_default_config(pm_cache_config *cfg) {
     cfg->log2_table = 19;
     cfg->base_res = 16;
     cfg->max_res = 2048;
-    // 12 Adam steps of 2^15 per frame: the image error falls with the steps
-    // per frame far more than with the fresh samples, and the k-NN targets
-    // are the frame's dearest part
-    cfg->train_samples = 3u << 17;
-    cfg->batch = 1u << 15;
+    cfg->train_samples = 1u << 20;
+    cfg->batch = 1u << 18;  // 4 steps per frame, each filling every SM
     cfg->lr = 5e-2f;
     cfg->beta1 = 0.9f;
     cfg->beta2 = 0.99f;
     cfg->eps = 1e-15f;
     cfg->lr_min = 1e-3f;
-    cfg->lr_half_life = 450.0f;
+    cfg->lr_half_life = 300.0f;
     cfg->loss_eps = 1.0f;
     cfg->surface_fraction = 0.5f;
     cfg->seed = 0x5EED0004ull;
@@ -300,7 +300,15 @@ pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int sour
     PM_TRY(cudaEventRecord(c->ev[2], stream));
     if (source == 0) {
         const float scale = c->target_scale > 0.0f ? c->target_scale : 1.0f;
-        PM_TRY(cache_infer(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, st->ql.nq, scale,
+        if (st->ql.nq > c->iorder_cap) {
+            cudaFree(c->iorder);
+            c->iorder = nullptr;
+            c->iorder_cap = 0;
+            PM_TRY(dalloc(&c->iorder, st->ql.qcap));
+            c->iorder_cap = st->ql.qcap;
+        }
+        PM_TRY(cache_pixel_block_order(st->ql.off, npix, c->iorder, stream));
+        PM_TRY(cache_infer(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, c->iorder, st->ql.nq, scale,
                            st->ql.val, c->sm_count, stream));
         PM_TRY(cudaEventRecord(c->ev[3], stream));
         PM_TRY(cache_composite(st->dscene, st->ql.off, st->ql.qa, st->ql.qd, st->ql.val, npix,

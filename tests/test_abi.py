@@ -83,7 +83,7 @@ def test_struct_layouts_match_the_library():
 def test_cache_default_config():
     cfg = photonmap.cache_default_config()
     assert (cfg.levels, cfg.log2_table, cfg.base_res, cfg.max_res) == (16, 19, 16, 2048)
-    assert cfg.train_samples == 3 << 17 and cfg.batch == 1 << 15
+    assert cfg.train_samples == 1 << 20 and cfg.batch % 128 == 0
 
 
 def test_batch_scene_generator_ranges():
