@@ -144,6 +144,35 @@ def test_training_learns_the_knn_estimate(ctx):
     assert trained < 0.1, trained
 
 
+def test_cached_values_are_the_network_of_each_query(ctx):
+    """pm_render_cached takes the queries pixel block by pixel block (32
+    consecutive pixels, sample-major within a block); every query's value
+    must still land in its own slot: it equals the network output for that
+    query from the training kernel's forward pass (same weights and table),
+    and not the output of its neighbour in the list. 40 x 40 pixels: blocks
+    that straddle image rows and a short last block."""
+    sc, cf = small(2, size=(40, 40))
+    frame(ctx, sc, cf)
+    ctx.cache_enable(log2_table=12, train_samples=1 << 14, batch=1 << 12)
+    ctx.cache_train(8)
+    render(ctx, cf, cached=0)
+    vals = ctx.cache_values()[:, :3]
+    qa, qd = ctx.cache_queries()
+    scale = np.float32(ctx.cache_stats().target_scale)
+    out = ctx.cache_debug_step(qa, qd, np.zeros((len(qa), 4), np.float32))
+    assert ctx.cache_stats().tc_status == 0
+    ref = np.maximum(out["y"][:, :3], 0.0) * scale
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    err = rel(vals, ref)
+    shifted = rel(vals, np.roll(ref, 1, axis=0))
+    print("cached values vs forward pass %.3g (neighbour's: %.3g)" % (err, shifted))
+    assert err < 1e-3, err
+    assert shifted > 20 * err + 1e-3, (err, shifted)
+
+
 def test_cache_file_round_trip(ctx, tmp_path):
     sc, cf = small(1, size=(32, 32))
     frame(ctx, sc, cf)
