@@ -101,16 +101,25 @@ static_assert(kWBytes == kCacheWImageBytes, "weight image size");
 // The CTA's copy of the weight image: one bulk copy (TMA) issued by thread
 // 0 on `mbar` (phase 0), which every thread then waits for. False when the
 // bounded wait ran out.
-__device__ bool load_weight_image(unsigned char *sw, const uint4 *img, uint64_t *mbar) {
+__device__ bool load_weight_image(unsigned char *sw, const uint4 *img, uint64_t *mbar,
+                                  uint32_t polls) {
     if (threadIdx.x == 0) {
         mbar_init(mbar);
         bulk_load(sw, img, kWBytes, mbar);
     }
     __syncthreads();
-    return mbar_wait(mbar, 0);
+    return mbar_wait_drain(mbar, 0, polls);
 }
 
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// One table-gradient term as a fixed-point integer: the exact product with
+// 2^kTableGradShift (a power of two), rounded once to the nearest integer.
+__device__ __forceinline__ long long to_grad_fixed(float x) {
+    return __float2ll_rn(x * 0x1p44f);
+}
+static_assert(kTableGradShift == 44, "to_grad_fixed and from_grad_fixed use 2^44");
+__device__ __forceinline__ float from_grad_fixed(long long q) { return __ll2float_rn(q) * 0x1p-44f; }
 
 // Table slots and trilinear weights of the 8 corners around p (in [0,1]^3)
 // on level l: vertices 0..res per axis, dense indexing while (res+1)^3 fits
@@ -235,9 +244,10 @@ __device__ void encode_row(unsigned char *act, uint32_t sbo, int row, const Cach
 
 // Runs `issue` on thread 0 after the CTA's shared-memory writes are visible
 // to the tensor core, commits, and waits for completion. false when the
-// bounded wait ran out.
+// wait's first bound (polls) ran out; the MMAs have completed either way
+// (mbar_wait_drain), so the caller may stop at the end of its tile.
 template <class F>
-__device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, F issue) {
+__device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, uint32_t polls, F issue) {
     publish_smem();
     __syncthreads();
     after_sync();
@@ -245,7 +255,7 @@ __device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, F issu
         issue();
         mma_commit(mbar);
     }
-    const bool ok = mbar_wait(mbar, phase);
+    const bool ok = mbar_wait_drain(mbar, phase, polls);
     phase ^= 1u;
     after_sync();
     return ok;
@@ -255,7 +265,7 @@ __device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, F issu
 // instead of the CTA barrier; `issuer` is the pipeline's first thread.
 template <class F>
 __device__ __forceinline__ bool tc_round_group(uint64_t *mbar, uint32_t &phase, uint32_t bar,
-                                               bool issuer, F issue) {
+                                               bool issuer, uint32_t polls, F issue) {
     publish_smem();
     named_sync(bar, kThreads);
     after_sync();
@@ -263,7 +273,7 @@ __device__ __forceinline__ bool tc_round_group(uint64_t *mbar, uint32_t &phase, 
         issue();
         mma_commit(mbar);
     }
-    const bool ok = mbar_wait(mbar, phase);
+    const bool ok = mbar_wait_drain(mbar, phase, polls);
     phase ^= 1u;
     after_sync();
     return ok;
@@ -321,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int s = threadIdx.x, warp = s >> 5;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
 
-    bool ok = load_weight_image(sm, p.w_img, &wbar);
+    bool ok = load_weight_image(sm, p.w_img, &wbar, p.wait_polls);
     for (uint32_t i = s; i < kPair / 16; i += kThreads)  // the unused half of P2 stays finite
         reinterpret_cast<uint4 *>(sm + kOffP2)[i] = make_uint4(0, 0, 0, 0);
     if (s == 0) {
@@ -343,7 +353,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (!ok) abort_s = 1;
     __syncthreads();
     if (abort_s) ok = false;
-    const size_t T = (size_t)1 << g.log2_t;
 
     for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const uint32_t i = tile * kThreads + s;
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // forward, hidden layers: H_{l+1} = relu(H_l W_l)
         for (int l = 0; l < 4; ++l) {
             const uint32_t src = aP[l >> 1] + (uint32_t)(l & 1) * 1024u;
-            ok &= tc_round(&mbar, phase, [&] {
+            ok &= tc_round(&mbar, phase, p.wait_polls, [&] {
                 mma_chain(taddr, src, 256, 128, kPairSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
                           idesc_bf16(128, 64), false);
             });
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                      kPairSbo, s);
         }
         // output layer: y = H4 W4
-        ok &= tc_round(&mbar, phase, [&] {
+        ok &= tc_round(&mbar, phase, p.wait_polls, [&] {
             mma_chain(taddr, aP[2], 256, 128, kPairSbo, aW + 32768u, 256, 128, 1024, 4,
                       idesc_bf16(128, 16), false);
         });
@@ -396,7 +405,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             st8(sm + kOffGY, go + 128u, gy + 8);
         }
         // dH4 = GY W4^T (B = the output layer read MN-major)
-        ok &= tc_round(&mbar, phase, [&] {
+        ok &= tc_round(&mbar, phase, p.wait_polls, [&] {
             mma_chain(taddr, aGY, 0, 128, 256, aW + 32768u, 0, 1024, 128, 1,
                       idesc_bf16(128, 64, 0, 1), false);
         });
@@ -404,7 +413,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // dH_l = dZ_{l+1} W_l^T for l = 3, 2, 1
         for (int l = 3; l >= 1; --l) {
             const uint32_t dz = aQ[l >> 1] + (uint32_t)(l & 1) * 1024u;  // dZ_{l+1}
-            ok &= tc_round(&mbar, phase, [&] {
+            ok &= tc_round(&mbar, phase, p.wait_polls, [&] {
                 mma_chain(taddr, dz, 256, 128, kPairSbo, aW + (uint32_t)l * 8192u, 2048, 1024, 128, 4,
                           idesc_bf16(128, 64, 0, 1), false);
             });
@@ -414,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         // dX = dZ1 W0^T, and the weight gradients of the tile
         const bool acc = !first;
-        ok &= tc_round(&mbar, phase, [&] {
+        ok &= tc_round(&mbar, phase, p.wait_polls, [&] {
             mma_chain(taddr, aQ[0], 256, 128, kPairSbo, aW, 2048, 1024, 128, 4,
                       idesc_bf16(128, 64, 0, 1), false);
             mma_chain(taddr + kColDW01, aP[0], 4096, kPairSbo, 128, aQ[0], 4096, kPairSbo, 128, 8,
@@ -428,17 +437,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         float dx[32];
         tmem_ld16(taddr, 0, dx);
         tmem_ld16(taddr, 16, dx + 16);
+        // the gradient of the 32 hash-grid features; table_scatter_kernel
+        // spreads it over the table entries after this kernel
         if (valid && ok) {
-            const QueryPos q = unit_pos(g, a);
-            for (int l = 0; l < g.levels; ++l) {
-                uint32_t idx[8];
-                float w[8];
-                level_corners(g, l, q.px, q.py, q.pz, idx, w);
-                float2 *lv = p.table_grad + (size_t)l * T;
-                const float g0 = dx[2 * l], g1 = dx[2 * l + 1];
+            float4 *row = p.dx + (size_t)i * 8;
 #pragma unroll
-                for (int k = 0; k < 8; ++k) atomicAdd(lv + idx[k], make_float2(w[k] * g0, w[k] * g1));
-            }
+            for (int j = 0; j < 8; ++j)
+                row[j] = make_float4(dx[4 * j], dx[4 * j + 1], dx[4 * j + 2], dx[4 * j + 3]);
         }
         if (!ok) abort_s = 1;
         __syncthreads();
@@ -486,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if ((s & 31) == 0) red[warp] = lsum;
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (s == 0) atomicAdd(p.loss, (red[0] + red[1] + red[2] + red[3]) * loss_norm);
+    if (s == 0) p.loss_part[blockIdx.x] = (red[0] + red[1] + red[2] + red[3]) * loss_norm;
     if (warp == 0) tmem_free(taddr, kTrainCols);
 }
 
@@ -509,7 +514,7 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
     const uint32_t bar = 1u + (uint32_t)pipe;
     const bool issuer = s == 0;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
-    const bool wok = load_weight_image(sm, p.w_img, &wbar);
+    const bool wok = load_weight_image(sm, p.w_img, &wbar, p.wait_polls);
     if (issuer) {
         mbar_init(&mbar[pipe]);
         abort_s[pipe] = wok ? 0 : 1;
@@ -536,13 +541,13 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
         }
         encode_row(act, kActSbo, s, g, p.table_h, Sc, a, d, valid, nullptr);
         for (int l = 0; l < 4; ++l) {
-            ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, [&] {
+            ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, p.wait_polls, [&] {
                 mma_chain(taddr, aA, 256, 128, kActSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
                           idesc_bf16(128, 64), false);
             });
             relu_out(taddr, act, kActSbo, s);
         }
-        ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, [&] {
+        ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, p.wait_polls, [&] {
             mma_chain(taddr, aA, 256, 128, kActSbo, aW + 32768u, 256, 128, 1024, 4,
                       idesc_bf16(128, 16), false);
         });
@@ -593,9 +598,81 @@ __global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph
     }
 }
 
-// w_grad[i] += sum over the CTAs' partial rows (fixed order: deterministic).
-__global__ void wgrad_reduce_kernel(const float *part, int parts, float *w_grad) {
+// The table gradient of n samples from their feature gradients (p.dx):
+// one thread per (sample, level) adds the 8 corners' terms w * dL/dfeature
+// as fixed-point integers. Does nothing once a tensor-core wait of the
+// training kernel has given up (its rows are then incomplete).
+__global__ void __launch_bounds__(256) table_scatter_kernel(CacheGrid g, CacheParams p,
+                                                            const float4 *qa, const uint32_t *sel,
+                                                            uint32_t n) {
+    if (*(volatile int *)p.status) return;
+    const size_t T = (size_t)1 << g.log2_t;
+    const size_t total = (size_t)n * kCacheMaxLevels;
+    const float2 *dxf = reinterpret_cast<const float2 *>(p.dx);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(t / kCacheMaxLevels);
+        const int l = (int)(t % kCacheMaxLevels);
+        if (l >= g.levels) continue;
+        const float2 gr = dxf[t];
+        if (gr.x == 0.0f && gr.y == 0.0f) continue;
+        const QueryPos q = unit_pos(g, qa[sel ? sel[i] : i]);
+        uint32_t idx[8];
+        float w[8];
+        level_corners(g, l, q.px, q.py, q.pz, idx, w);
+        unsigned long long *lv = reinterpret_cast<unsigned long long *>(p.table_grad) + 2 * (size_t)l * T;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long q0 = to_grad_fixed(w[k] * gr.x), q1 = to_grad_fixed(w[k] * gr.y);
+            if (q0) atomicAdd(lv + 2 * idx[k], (unsigned long long)q0);
+            if (q1) atomicAdd(lv + 2 * idx[k] + 1, (unsigned long long)q1);
+        }
+    }
+}
+
+// The table's lazy Adam step from the fixed-point gradient: entries whose
+// two sums are zero keep their value and moments; the others are updated
+// and their sums cleared.
+__global__ void adam_table_kernel(float *p, longlong2 *gr, float *m, float *v, __half2 *ph,
+                                  uint32_t npairs, float lr, float b1, float b2, float eps, float c1,
+                                  float c2) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
+        const longlong2 q = gr[i];
+        if (q.x == 0 && q.y == 0) continue;
+        const float2 gg = make_float2(from_grad_fixed(q.x), from_grad_fixed(q.y));
+        float2 pp = reinterpret_cast<float2 *>(p)[i];
+        float2 mm = reinterpret_cast<float2 *>(m)[i];
+        float2 vv = reinterpret_cast<float2 *>(v)[i];
+        mm.x = b1 * mm.x + (1.0f - b1) * gg.x;
+        mm.y = b1 * mm.y + (1.0f - b1) * gg.y;
+        vv.x = b2 * vv.x + (1.0f - b2) * gg.x * gg.x;
+        vv.y = b2 * vv.y + (1.0f - b2) * gg.y * gg.y;
+        pp.x -= lr * (mm.x * c1) / (sqrtf(vv.x * c2) + eps);
+        pp.y -= lr * (mm.y * c1) / (sqrtf(vv.y * c2) + eps);
+        reinterpret_cast<float2 *>(p)[i] = pp;
+        reinterpret_cast<float2 *>(m)[i] = mm;
+        reinterpret_cast<float2 *>(v)[i] = vv;
+        gr[i] = make_longlong2(0, 0);
+        ph[i] = __floats2half2_rn(pp.x, pp.y);
+    }
+}
+
+// The fixed-point table gradient as floats (debug copies).
+__global__ void table_grad_float_kernel(const long long *gr, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = from_grad_fixed(gr[i]);
+}
+
+// w_grad[i] += sum over the CTAs' partial rows, and *loss += the CTAs'
+// losses, both in CTA order (deterministic).
+__global__ void wgrad_reduce_kernel(const float *part, const float *loss_part, int parts,
+                                    float *w_grad, float *loss) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        float l = 0.0f;
+        for (int b = 0; b < parts; ++b) l += loss_part[b];
+        *loss += l;
+    }
     if (i >= kCacheWeights) return;
     float acc = 0.0f;
     for (int b = 0; b < parts; ++b) acc += part[(size_t)b * kCacheWeights + i];
@@ -618,7 +695,7 @@ __global__ void init_kernel(float *p, float *gr, float *m, float *v, __half2 *ph
         const float x0 = (2.0f * pm_u01(r.v[0]) - 1.0f) * a;
         const float x1 = (2.0f * pm_u01(r.v[1]) - 1.0f) * a;
         reinterpret_cast<float2 *>(p)[i] = make_float2(x0, x1);
-        reinterpret_cast<float2 *>(gr)[i] = make_float2(0.0f, 0.0f);
+        if (gr) reinterpret_cast<float2 *>(gr)[i] = make_float2(0.0f, 0.0f);
         reinterpret_cast<float2 *>(m)[i] = make_float2(0.0f, 0.0f);
         reinterpret_cast<float2 *>(v)[i] = make_float2(0.0f, 0.0f);
         if (ph) ph[i] = __floats2half2_rn(x0, x1);
@@ -801,15 +878,24 @@ __global__ void iota_kernel(uint32_t *v, uint32_t n) {
     if (i < n) v[i] = i;
 }
 
-__global__ void value_sum_kernel(const float4 *val, uint32_t n, float *sum) {
+// One CTA of kSumThreads: thread t sums entries t, t + kSumThreads, ... in
+// index order, then a fixed reduction tree; the result does not depend on
+// scheduling.
+constexpr int kSumThreads = 1024;
+__global__ void __launch_bounds__(kSumThreads) value_sum_kernel(const float4 *val, uint32_t n, float *sum) {
+    __shared__ float red[kSumThreads];
     float acc = 0.0f;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = threadIdx.x; i < n; i += kSumThreads) {
         const float4 v = val[i];
         acc += (v.x + v.y + v.z) * (1.0f / 3.0f);
     }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = kSumThreads / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *sum = red[0];
 }
 
 }  // namespace
@@ -878,17 +964,18 @@ cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s) {
 
 cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 1024);
-    value_sum_kernel<<<blocks, 256, 0, s>>>(val, n, sum);
+    value_sum_kernel<<<1, kSumThreads, 0, s>>>(val, n, sum);
     note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t cache_init(const CacheGrid &g, const CacheParams &p, uint64_t seed, cudaStream_t s) {
     const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));  // 2 floats per entry
-    init_kernel<<<1024, 256, 0, s>>>(p.table, reinterpret_cast<float *>(p.table_grad), p.table_m,
-                                     p.table_v, p.table_h, tpairs, seed, 0x7AB1Eu, -1, 1e-4f, 1e-4f);
+    init_kernel<<<1024, 256, 0, s>>>(p.table, nullptr, p.table_m, p.table_v, p.table_h, tpairs, seed,
+                                     0x7AB1Eu, -1, 1e-4f, 1e-4f);
     note_launch();
+    cudaError_t e = cudaMemsetAsync(p.table_grad, 0, sizeof(longlong2) * tpairs, s);
+    if (e != cudaSuccess) return e;
     const float a = sqrtf(6.0f / 64.0f);
     init_kernel<<<(kCacheWeights / 2 + 255) / 256, 256, 0, s>>>(p.w, p.w_grad, p.w_m, p.w_v, nullptr,
                                                                 kCacheWeights / 2, seed, 0x3E16u,
@@ -909,6 +996,7 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
                            const float4 *val, uint32_t n, float inv_scale, float loss_norm,
                            float rel_eps, float *x_out, float *y_out, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    if (n > p.dx_cap) return cudaErrorInvalidValue;
     // the opt-in is per device: set it on every call (a host-side attribute write)
     cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kTrainSmem);
@@ -919,7 +1007,12 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
     train_kernel<<<grid, kThreads, kTrainSmem, s>>>(g, p, S, qa, qd, sel, val, n, inv_scale, loss_norm,
                                                     rel_eps, x_out, y_out);
     note_launch();
-    wgrad_reduce_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w_part, (int)grid, p.w_grad);
+    wgrad_reduce_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w_part, p.loss_part, (int)grid,
+                                                                  p.w_grad, p.loss);
+    note_launch();
+    const size_t threads = (size_t)n * kCacheMaxLevels;
+    const uint32_t sgrid = (uint32_t)std::min<size_t>((threads + 255) / 256, (size_t)sm_count * 8);
+    table_scatter_kernel<<<sgrid, 256, 0, s>>>(g, p, qa, sel, n);
     note_launch();
     return cudaGetLastError();
 }
@@ -929,13 +1022,21 @@ cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float
     const float c1 = 1.0f / (1.0f - powf(beta1, (float)step));
     const float c2 = 1.0f / (1.0f - powf(beta2, (float)step));
     const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));
-    adam_kernel<<<2048, 256, 0, s>>>(p.table, reinterpret_cast<float *>(p.table_grad), p.table_m,
-                                     p.table_v, p.table_h, tpairs, lr, beta1, beta2, eps, c1, c2, true,
-                                     nullptr);
+    adam_table_kernel<<<2048, 256, 0, s>>>(p.table, reinterpret_cast<longlong2 *>(p.table_grad),
+                                           p.table_m, p.table_v, p.table_h, tpairs, lr, beta1, beta2, eps,
+                                           c1, c2);
     note_launch();
     adam_kernel<<<(kCacheWeights / 2 + 255) / 256, 256, 0, s>>>(p.w, p.w_grad, p.w_m, p.w_v, nullptr,
                                                                 kCacheWeights / 2, lr, beta1, beta2,
                                                                 eps, c1, c2, false, p.w_img);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_table_grad_float(const CacheGrid &g, const CacheParams &p, float *out,
+                                   cudaStream_t s) {
+    const size_t n = (size_t)g.levels << (g.log2_t + 1);
+    table_grad_float_kernel<<<1024, 256, 0, s>>>(p.table_grad, out, n);
     note_launch();
     return cudaGetLastError();
 }

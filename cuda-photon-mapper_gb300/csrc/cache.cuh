@@ -28,6 +28,10 @@ constexpr int kCacheTile = 128;     // samples per tensor-core tile (one per TME
 // layers, then 64 x 16.
 constexpr int kCacheWeights = kCacheLayers * kCacheIn * kCacheHidden + kCacheHidden * kCacheOut;
 constexpr uint32_t kCacheWImageBytes = 4 * 8192 + 2048;
+// Scale of the fixed-point table gradient: resolution 2^-44 (5.7e-14), range
+// +-2^19 per entry -- a step's per-sample gradients are at most ~1e-1 and an
+// entry receives at most batch x 8 corner terms.
+constexpr int kTableGradShift = 44;
 
 struct CacheGrid {
     int levels;              // <= kCacheMaxLevels
@@ -42,12 +46,20 @@ struct CacheParams {
     float *w_part;         // per-CTA weight-gradient rows of one backward pass (parts_cap rows)
     int parts_cap;
     float *table;          // fp32 master table, levels * 2^log2_t * 2
-    float2 *table_grad;
+    // Table gradient as exact fixed-point sums: two signed 64-bit integers
+    // per entry, each term rounded once to a multiple of 2^-kTableGradShift
+    // and added with integer atomics, so the sum (and every training step)
+    // does not depend on the order the samples' atomics land in.
+    long long *table_grad;
     float *table_m, *table_v;
     __half2 *table_h;      // fp16 copy read by the forward passes
     uint4 *w_img;          // bf16 weights in the kernels' shared-memory layout (kCacheWImageBytes)
     float *loss;           // device scalar, summed over a step
+    float *loss_part;      // per-CTA loss of one backward pass (parts_cap), added to *loss in CTA order
+    float4 *dx;            // per-sample gradient of the 32 hash-grid features (8 float4 per sample)
+    uint32_t dx_cap;       // samples dx holds
     int *status;           // set when a bounded tensor-core wait runs out
+    uint32_t wait_polls;   // first bound of every mbarrier wait (kMbarSpin unless lowered for a test)
 };
 
 // Per-pixel query counts and diffuse-query counts (0 or 1) (count pass);
@@ -93,14 +105,14 @@ cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s);
 cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
                          uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel,
                          cudaStream_t s);
-// *sum += mean over rgb of val[0..n).
+// *sum = mean over rgb of val[0..n), summed in a fixed order.
 cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s);
 
 cudaError_t cache_init(const CacheGrid &g, const CacheParams &p, uint64_t seed, cudaStream_t s);
 // Refreshes the fp16 table from the fp32 master copy.
 cudaError_t cache_sync_half(const CacheGrid &g, const CacheParams &p, cudaStream_t s);
 // Forward + backward of the relative L2 loss (denominator y^2 + rel_eps)
-// over n samples (query sel[i], target val[i] * inv_scale); gradients and loss are added to p.w_grad,
+// over n <= p.dx_cap samples (query sel[i], target val[i] * inv_scale); gradients and loss are added to p.w_grad,
 // p.table_grad, p.loss with the factor loss_norm (1 / (3 * batch)). x_out
 // (n x 64 encoded features) and y_out (n x 4 outputs) are debug copies,
 // nullable.
@@ -108,6 +120,9 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
                            const float4 *qa, const float4 *qd, const uint32_t *sel,
                            const float4 *val, uint32_t n, float inv_scale, float loss_norm,
                            float rel_eps, float *x_out, float *y_out, int sm_count, cudaStream_t s);
+// out[0 .. levels * 2^log2_t * 2) = the table gradient as floats.
+cudaError_t cache_table_grad_float(const CacheGrid &g, const CacheParams &p, float *out,
+                                   cudaStream_t s);
 // Writes p.w_img from the fp32 weights.
 cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s);
 // One Adam step over all parameters; gradients are zeroed after use. The

@@ -5,6 +5,7 @@
 #include "phys_state.cuh"
 #include "pm_ctx.cuh"
 #include "radix_sort.cuh"
+#include "tc.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -78,7 +79,8 @@ void free_cache(CacheState *c) {
     cudaFree(c->p.w); cudaFree(c->p.w_grad); cudaFree(c->p.w_m); cudaFree(c->p.w_v);
     cudaFree(c->p.w_part);
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
-    cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.status); cudaFree(c->p.w_img);
+    cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.loss_part); cudaFree(c->p.status);
+    cudaFree(c->p.w_img); cudaFree(c->p.dx);
     cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum); cudaFree(c->iorder);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
     cudaFree(c->shist); cudaFree(c->sn);
@@ -194,14 +196,18 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     PM_TRY_FREE(dalloc(&p.w_m, kCacheWeights));
     PM_TRY_FREE(dalloc(&p.w_v, kCacheWeights));
     PM_TRY_FREE(dalloc(&p.table, c->table_floats));
-    PM_TRY_FREE(dalloc(&p.table_grad, c->table_floats / 2));
+    PM_TRY_FREE(dalloc(&p.table_grad, c->table_floats));
     PM_TRY_FREE(dalloc(&p.table_m, c->table_floats));
     PM_TRY_FREE(dalloc(&p.table_v, c->table_floats));
     PM_TRY_FREE(dalloc(&p.table_h, c->table_floats / 2));
     PM_TRY_FREE(dalloc(&p.w_img, kCacheWImageBytes / 16));
     PM_TRY_FREE(dalloc(&p.loss, 1));
+    PM_TRY_FREE(dalloc(&p.loss_part, p.parts_cap));
+    p.dx_cap = cfg.batch;
+    PM_TRY_FREE(dalloc(&p.dx, (size_t)cfg.batch * 8));
     PM_TRY_FREE(dalloc(&p.status, 1));
     PM_TRY_FREE(cudaMemset(p.status, 0, sizeof(int)));
+    p.wait_polls = kMbarSpin;
     PM_TRY_FREE(dalloc(&c->sel, cfg.train_samples));
     PM_TRY_FREE(dalloc(&c->tgt, cfg.train_samples));
     PM_TRY_FREE(dalloc(&c->skey, cfg.train_samples));
@@ -353,6 +359,25 @@ pm_status pm_cache_get_stats(pm_ctx *ctx, pm_cache_stats *out) {
     return PM_OK;
 }
 
+pm_status pm_cache_set_wait_limit(pm_ctx *ctx, int polls) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    ctx->cache->p.wait_polls = polls < 0 ? kMbarSpin : (uint32_t)polls;
+    return PM_OK;
+}
+
+pm_status pm_cache_clear_status(pm_ctx *ctx) {
+    if (!ctx) return PM_ERR_INVALID;
+    pm_status s = need_cache(ctx, false);
+    if (s != PM_OK) return s;
+    DeviceGuard g(ctx->device);
+    cudaError_t e;
+    PM_TRY(cudaDeviceSynchronize());
+    PM_TRY(cudaMemset(ctx->cache->p.status, 0, sizeof(int)));
+    return PM_OK;
+}
+
 pm_status pm_cache_get_params(pm_ctx *ctx, float *weights, float *table, int *res) {
     if (!ctx) return PM_ERR_INVALID;
     pm_status s = need_cache(ctx, false);
@@ -406,7 +431,9 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
     set_grid_box(c->grid, st->scene);
     cudaError_t e;
     float4 *dqa = nullptr, *dqd = nullptr, *dt = nullptr;
-    float *dx = nullptr, *dy = nullptr;
+    float *dx = nullptr, *dy = nullptr, *tg = nullptr;
+    float4 *ddx = nullptr;
+    CacheParams dp = c->p;
     std::string where;
 #define PM_DBG(x) do { e = (x); if (e != cudaSuccess) { where = #x; goto done; } } while (0)
     PM_DBG(cudaDeviceSynchronize());
@@ -421,9 +448,13 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
         PM_DBG(cudaMemcpy(dt, target, sizeof(float4) * n, cudaMemcpyHostToDevice));
     }
     PM_DBG(cudaMemset(c->p.w_grad, 0, sizeof(float) * kCacheWeights));
-    PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(float) * c->table_floats));
+    PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(long long) * c->table_floats));
     PM_DBG(cudaMemset(c->p.loss, 0, sizeof(float)));
-    PM_DBG(cache_backward(c->grid, c->p, st->dscene, dqa, dqd, nullptr, dt, n, 1.0f / target_scale,
+    // the feature-gradient rows of n samples (n may exceed the batch)
+    PM_DBG(dalloc(&ddx, (size_t)n * 8));
+    dp.dx = ddx;
+    dp.dx_cap = n;
+    PM_DBG(cache_backward(c->grid, dp, st->dscene, dqa, dqd, nullptr, dt, n, 1.0f / target_scale,
                           n ? 1.0f / (3.0f * (float)n) : 0.0f, c->cfg.loss_eps, dx, dy, c->sm_count,
                           0));
     PM_DBG(cudaDeviceSynchronize());
@@ -431,13 +462,17 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
     if (y && n) PM_DBG(cudaMemcpy(y, dy, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost));
     if (loss) PM_DBG(cudaMemcpy(loss, c->p.loss, sizeof(float), cudaMemcpyDeviceToHost));
     if (w_grad) PM_DBG(cudaMemcpy(w_grad, c->p.w_grad, sizeof(float) * kCacheWeights, cudaMemcpyDeviceToHost));
-    if (table_grad)
-        PM_DBG(cudaMemcpy(table_grad, c->p.table_grad, sizeof(float) * c->table_floats, cudaMemcpyDeviceToHost));
+    if (table_grad) {
+        // the fixed-point sums converted to floats in a scratch buffer
+        PM_DBG(dalloc(&tg, c->table_floats));
+        PM_DBG(cache_table_grad_float(c->grid, c->p, tg, 0));
+        PM_DBG(cudaMemcpy(table_grad, tg, sizeof(float) * c->table_floats, cudaMemcpyDeviceToHost));
+    }
     PM_DBG(cudaMemset(c->p.w_grad, 0, sizeof(float) * kCacheWeights));
-    PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(float) * c->table_floats));
+    PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(long long) * c->table_floats));
 done:
 #undef PM_DBG
-    cudaFree(dqa); cudaFree(dqd); cudaFree(dt); cudaFree(dx); cudaFree(dy);
+    cudaFree(dqa); cudaFree(dqd); cudaFree(dt); cudaFree(dx); cudaFree(dy); cudaFree(tg); cudaFree(ddx);
     if (e != cudaSuccess) return check_cuda(ctx, e, where.c_str());
     return PM_OK;
 }
@@ -581,7 +616,7 @@ pm_status pm_cache_load(pm_ctx *ctx, const char *path) {
         at += len;
     }
     PM_TRY(cudaMemset(c->p.w_grad, 0, sizeof(float) * nw));
-    PM_TRY(cudaMemset(c->p.table_grad, 0, sizeof(float) * nt));
+    PM_TRY(cudaMemset(c->p.table_grad, 0, sizeof(long long) * nt));
     PM_TRY(cache_sync_half(c->grid, c->p, 0));
     PM_TRY(cache_weight_image(c->p, 0));
     PM_TRY(cudaDeviceSynchronize());

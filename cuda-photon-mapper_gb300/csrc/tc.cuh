@@ -50,16 +50,26 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar) {
     asm volatile("fence.mbarrier_init.release.cluster;");
 }
 
-// Waits for the given phase; false when the bound runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase) {
+// Waits for the given phase, polling at most `polls` times; false when the
+// bound runs out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase, uint32_t polls = kMbarSpin) {
     uint32_t done = 0;
-    for (uint32_t it = 0; it < kMbarSpin && !done; ++it) {
+    for (uint32_t it = 0; it < polls && !done; ++it) {
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
             : "r"(smem_addr(mbar)), "r"(phase));
     }
     return done != 0;
+}
+
+// A wait whose first bound is `polls`: when that runs out the caller is
+// told (false), and the wait goes on under the default bound so that the
+// copy or MMA it waits for is no longer in flight when the caller stops.
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t *mbar, uint32_t phase, uint32_t polls) {
+    if (mbar_wait(mbar, phase, polls)) return true;
+    mbar_wait(mbar, phase, kMbarSpin);
+    return false;
 }
 
 // Warp-collective: allocates `cols` TMEM columns and writes their address

@@ -177,6 +177,8 @@ PROTOTYPES = {
     "pm_batch_set_tune": (_i, [_vp, _i, _c.POINTER(BatchTune)]),
     "pm_batch_get_tune": (_i, [_vp, _i, _c.POINTER(BatchTune)]),
     "pm_batch_autotune": (_i, [_vp, _c.c_char_p, _vp]),
+    "pm_cache_set_wait_limit": (_i, [_vp, _i]),
+    "pm_cache_clear_status": (_i, [_vp]),
     "pm_cache_save": (_i, [_vp, _c.c_char_p]),
     "pm_cache_load": (_i, [_vp, _c.c_char_p]),
 }
@@ -369,6 +371,12 @@ class Context:
         st = CacheStats()
         self._check(self.lib.pm_cache_get_stats(self.h, _c.byref(st)), "pm_cache_get_stats")
         return st
+
+    def cache_set_wait_limit(self, polls):
+        self._check(self.lib.pm_cache_set_wait_limit(self.h, polls), "pm_cache_set_wait_limit")
+
+    def cache_clear_status(self):
+        self._check(self.lib.pm_cache_clear_status(self.h), "pm_cache_clear_status")
 
     def cache_params(self):
         """(weights [PM_CACHE_WEIGHTS], table [levels, 2^log2, 2], res [levels])."""

@@ -376,6 +376,16 @@ PM_API pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream);
 PM_API pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int source,
                                   cudaStream_t stream);
 PM_API pm_status pm_cache_get_stats(pm_ctx *ctx, pm_cache_stats *out);
+/* Diagnostics of the tensor-core kernels' bounded waits. Every mbarrier
+ * wait of the training and inference kernels (the weight copy, each MMA
+ * round) polls at most `polls` times before it gives up (polls < 0: the
+ * default, 2^24); a wait that gives up sets tc_status, keeps waiting under
+ * the default bound so that no copy or MMA is left in flight, and its CTA
+ * stops after the current tile of 128 samples. A low bound makes that path
+ * run without a hang (0: give up without polling). pm_cache_clear_status
+ * zeroes tc_status (synchronises the device). */
+PM_API pm_status pm_cache_set_wait_limit(pm_ctx *ctx, int polls);
+PM_API pm_status pm_cache_clear_status(pm_ctx *ctx);
 /* Host copies of the fp32 weights (PM_CACHE_WEIGHTS: four [64 in][64 out]
  * layers, then [64][16]), the fp32 table (levels * 2^log2_table * 2,
  * nullable) and the grid resolutions (levels ints, nullable). */

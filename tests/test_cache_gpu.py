@@ -144,6 +144,52 @@ def test_training_learns_the_knn_estimate(ctx):
     assert trained < 0.1, trained
 
 
+def test_training_is_deterministic(ctx):
+    """Training adds its table gradients as exact fixed-point integers and
+    reduces the weight gradients, the loss and the target scale in a fixed
+    order, so the same frames give the same network bit for bit, however
+    the atomics of the many CTAs interleave."""
+    sc, cf = small(2, 30000, 30000, size=(64, 48))
+    frame(ctx, sc, cf)
+    runs = []
+    for _ in range(2):
+        ctx.cache_enable(train_samples=1 << 16, batch=1 << 13)
+        ctx.cache_train(6)
+        w, t, _ = ctx.cache_params()
+        runs.append((w, t, ctx.cache_stats().loss, render(ctx, cf, cached=0)))
+    (w0, t0, l0, i0), (w1, t1, l1, i1) = runs
+    np.testing.assert_array_equal(w0.view(np.uint32), w1.view(np.uint32))
+    np.testing.assert_array_equal(t0.view(np.uint32), t1.view(np.uint32))
+    assert np.float32(l0).view(np.uint32) == np.float32(l1).view(np.uint32)
+    np.testing.assert_array_equal(i0.view(np.uint32), i1.view(np.uint32))
+
+
+def test_bounded_wait_gives_up_reports_and_recovers(ctx):
+    """Every tensor-core and copy wait of the cache kernels is bounded. With
+    the first bound set to zero polls each wait gives up at once: the kernel
+    records tc_status, waits out the MMA or copy it issued under the default
+    bound (nothing stays in flight) and stops after its tile. The context
+    stays usable: with the default bound back, training and inference run
+    clean again."""
+    sc, cf = small(1, 20000, 20000, size=(48, 40))
+    frame(ctx, sc, cf)
+    ctx.cache_enable(log2_table=12, train_samples=1 << 13, batch=1 << 12)
+    ctx.cache_train(1)
+    assert ctx.cache_stats().tc_status == 0
+    ctx.cache_set_wait_limit(0)
+    ctx.cache_train(1)
+    assert ctx.cache_stats().tc_status == 1
+    ctx.cache_clear_status()
+    render(ctx, cf, cached=0)
+    assert ctx.cache_stats().tc_status == 1
+    ctx.cache_set_wait_limit(-1)
+    ctx.cache_clear_status()
+    ctx.cache_train(2)
+    img = render(ctx, cf, cached=0)
+    assert ctx.cache_stats().tc_status == 0
+    assert np.isfinite(img).all()
+
+
 def test_cached_values_are_the_network_of_each_query(ctx):
     """pm_render_cached takes the queries pixel block by pixel block (32
     consecutive pixels, sample-major within a block); every query's value
