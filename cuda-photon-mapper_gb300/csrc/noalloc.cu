@@ -16,6 +16,8 @@
 // reads, so nothing has to start at zero. Calls that overlap on the GPU
 // (different streams, or different host threads on the same device) race
 // on the array and must be serialised by the caller.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "gather.cuh"
@@ -48,40 +50,71 @@ constexpr size_t kOffHi = kOffLo + align256(16 * kNodes);
 constexpr size_t kOffMisc = kOffHi + align256(16 * kNodes);  // count + box
 constexpr size_t kScratchBytes = kOffMisc + 256;
 static_assert(kScratchBytes == PM_KNN_NOALLOC_SCRATCH_BYTES, "scratch size in pm.h is stale");
+static_assert(6 * 128 * sizeof(float) <= kOffKeysTmp - kOffKeys, "prepare partials fit the key area");
 
 __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
+// The scratch array's device address per device, valid for the CUDA
+// context it was looked up in.
+struct ScratchAddr {
+    CUcontext ctx;
+    unsigned char *addr;
+};
 std::mutex g_mu;
-unsigned char *g_addr[kMaxDevices] = {};
+ScratchAddr g_addr[kMaxDevices] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
 
-// Device address of g_scratch on the current device, looked up once per
-// device. In host code `g_scratch` names a host-side stand-in, not device
-// memory, so kernels get this address instead.
+// Device address of g_scratch on the current device. In host code
+// `g_scratch` names a host-side stand-in, not device memory, so kernels get
+// this address instead. It is looked up (cudaGetSymbolAddress, with the
+// device current) on the first call on each device, and again whenever the
+// current context differs from the one it was looked up in (after a
+// cudaDeviceReset, or under a context the caller made current through the
+// driver API): an address from another context is not this one's memory.
 cudaError_t scratch_address(unsigned char **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    if (!g_ctx_get_current) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
+        g_ctx_get_current = (CtxGetCurrentFn)fn;
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    ScratchAddr &slot = g_addr[dev];
+    if (!ctx || !slot.addr || slot.ctx != ctx) {
+        // also makes the device's primary context current when no context is
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_scratch);
         if (e != cudaSuccess) return e;
-        g_addr[dev] = (unsigned char *)p;
+        if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+        slot.addr = (unsigned char *)p;
+        slot.ctx = ctx;
     }
-    *out = g_addr[dev];
+    *out = slot.addr;
     return cudaSuccess;
 }
 
-// Copies the points with their index in .w (the tie-break key), writes the
-// count for the sort and the points' bounding box (the tree's root cell).
-__global__ void __launch_bounds__(1024) prepare_kernel(const float4 *__restrict__ pts, uint32_t n,
-                                                       float4 *ipos, uint32_t *count, float *box) {
-    __shared__ float red[6][32];
+constexpr int kPrepBlocks = 128;
+constexpr int kPrepThreads = 256;
+
+// Copies the points with their index in .w (the tie-break key), grid-stride
+// over kPrepBlocks CTAs, and writes each CTA's bounding box of its points to
+// part[6 * block ..] (lo xyz, hi xyz).
+__global__ void __launch_bounds__(kPrepThreads) prepare_kernel(const float4 *__restrict__ pts,
+                                                               uint32_t n, float4 *ipos, float *part) {
+    __shared__ float red[6][kPrepThreads / 32];
     const float inf = __int_as_float(0x7f800000);
     float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        float4 p = pts[i];
+    for (uint32_t i = blockIdx.x * kPrepThreads + threadIdx.x; i < n; i += kPrepBlocks * kPrepThreads) {
+        const float4 p = pts[i];
         ipos[i] = make_float4(p.x, p.y, p.z, __uint_as_float(i));
         lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
         hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
@@ -95,16 +128,26 @@ __global__ void __launch_bounds__(1024) prepare_kernel(const float4 *__restrict_
     if (lane == 0)
         for (int a = 0; a < 3; ++a) { red[a][warp] = lo[a]; red[3 + a][warp] = hi[a]; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        const int nw = blockDim.x >> 5;
-        for (int w = 1; w < nw; ++w)
-            for (int a = 0; a < 3; ++a) {
-                red[a][0] = fminf(red[a][0], red[a][w]);
-                red[3 + a][0] = fmaxf(red[3 + a][0], red[3 + a][w]);
-            }
-        for (int a = 0; a < 6; ++a) box[a] = red[a][0];
-        *count = n;
+    if (threadIdx.x < 6) {
+        const int a = threadIdx.x;
+        float v = red[a][0];
+        for (int w = 1; w < kPrepThreads / 32; ++w) v = a < 3 ? fminf(v, red[a][w]) : fmaxf(v, red[a][w]);
+        part[6 * blockIdx.x + a] = v;
     }
+}
+
+// The points' bounding box (the tree's root cell) from the CTAs' boxes, and
+// the count the sort reads. Minima and maxima do not depend on the order they
+// are taken in, so the box is exactly the one a single pass finds.
+__global__ void box_kernel(const float *part, uint32_t n, uint32_t *count, float *box) {
+    const int a = threadIdx.x;
+    if (a < 6) {
+        float v = part[a];
+        for (int b = 1; b < kPrepBlocks; ++b)
+            v = a < 3 ? fminf(v, part[6 * b + a]) : fmaxf(v, part[6 * b + a]);
+        box[a] = v;
+    }
+    if (a == 0) *count = n;
 }
 
 }  // namespace
@@ -129,7 +172,7 @@ extern "C" pm_status pm_knn_noalloc(const float4 *points, uint32_t n, const floa
     float4 *hi = (float4 *)(base + kOffHi);
     uint32_t *count = (uint32_t *)(base + kOffMisc);
     float *box = (float *)(base + kOffMisc + 16);
-    MapView m;
+    MapView m{};
     m.pos = tpos;
     m.pow = nullptr;
     m.lo = lo;
@@ -137,7 +180,12 @@ extern "C" pm_status pm_knn_noalloc(const float4 *points, uint32_t n, const floa
     m.n = n;
     m.depth = tree_depth(n);
     if (n > 0) {
-        prepare_kernel<<<1, 1024, 0, stream>>>(points, n, ipos, count, box);
+        // the CTAs' boxes go to the start of the sort-key area, which the
+        // build overwrites only after box_kernel has read them (stream order)
+        float *part = (float *)(base + kOffKeys);
+        prepare_kernel<<<kPrepBlocks, kPrepThreads, 0, stream>>>(points, n, ipos, part);
+        note_launch();
+        box_kernel<<<1, 32, 0, stream>>>(part, n, count, box);
         note_launch();
         KdBuildArgs a;
         a.n = n;

@@ -70,6 +70,38 @@ def test_noalloc_matches_allocating_path_on_consecutive_calls():
         np.testing.assert_array_equal(bd.view(np.uint32), ad.view(np.uint32))
 
 
+def test_noalloc_allocates_no_device_memory():
+    """The device's free memory (cudaMemGetInfo) is the same before and
+    after calls: the scratch is the library's static array, not an
+    allocation. The first call may load the library's kernels and its
+    static array on this device (a one-time module load, not an allocation
+    by the entry point), so the check covers the calls after it."""
+    torch.cuda.set_device(0)
+    rs = np.random.RandomState(5)
+    for n, k in [(4096, 16), (MAX_POINTS, 64), (1000, 128)]:
+        pos = points(rs, n)
+        q = np.zeros((4096, 4), np.float32)
+        q[:, :3] = rs.uniform([-0.5, 0.0, -0.5], [0.5, 1.0, 0.5], size=(4096, 3))
+        pd = torch.from_numpy(pos).cuda()
+        qd = torch.from_numpy(q).cuda()
+        idx = torch.zeros((len(q), k), dtype=torch.int32, device="cuda")
+        d2 = torch.zeros((len(q), k), dtype=torch.float32, device="cuda")
+        lib = photonmap.load()
+
+        def call():
+            s = lib.pm_knn_noalloc(pd.data_ptr(), n, qd.data_ptr(), len(q), k, 0.1,
+                                   idx.data_ptr(), d2.data_ptr(), None)
+            torch.cuda.synchronize()
+            assert s == 0, s
+
+        call()
+        free_before, _ = torch.cuda.mem_get_info()
+        for _ in range(3):
+            call()
+        free_after, _ = torch.cuda.mem_get_info()
+        assert free_after == free_before, (n, free_before, free_after)
+
+
 def test_noalloc_rejects_more_points_than_its_scratch_holds():
     lib = photonmap.load()
     dummy = torch.zeros(4, dtype=torch.float32, device="cuda")
