@@ -16,11 +16,14 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libphotonmap.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle.so")
-REF_DIR = "/root/reference"
+# The reference checkout, when present: $PM_REFERENCE_DIR, else a directory
+# named `reference` beside the repository.
+REF_DIR = os.environ.get("PM_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off",
            "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 

@@ -3,8 +3,10 @@
 # oracle/ref_shim.h. Test infrastructure: only tests/golden/make_golden.py
 # loads it. Needs the reference checkout; outputs go to oracle/_ref/ only.
 #
-#   make -f oracle/ref.mk REF=/root/reference
-REF ?= /root/reference
+#   make -f oracle/ref.mk REF=<reference checkout>
+ifndef REF
+$(error REF=<path of the reference checkout> is required)
+endif
 OUT := oracle/_ref
 CXX ?= g++
 

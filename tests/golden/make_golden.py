@@ -51,7 +51,9 @@ def load_ref(ref_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PM_REFERENCE_DIR")
+                    or os.path.join(os.path.dirname(ROOT), "reference"),
+                    help="reference checkout (default: $PM_REFERENCE_DIR, else ../reference)")
     args = ap.parse_args()
     lib = load_ref(args.ref)
     out = {}
