@@ -82,10 +82,14 @@ void seeded_spheres(pm_scene &s, int count, float rmin, float rmax, SplitMix &rn
         }
         s.spheres[i] = make_float4(cx, cy, cz, r);
         float pick = rng.uniform();
-        if (pick < 0.5f)
-            set_mat(s.sphere_mat[i], PM_MAT_DIFFUSE, rng.range(0.2f, 0.9f), rng.range(0.2f, 0.9f),
-                    rng.range(0.2f, 0.9f), 1.0f);
-        else if (pick < 0.75f)
+        if (pick < 0.5f) {
+            // red, green, blue drawn in that order (separate statements: the
+            // order of a call's argument evaluations is unspecified)
+            const float ar = rng.range(0.2f, 0.9f);
+            const float ag = rng.range(0.2f, 0.9f);
+            const float ab = rng.range(0.2f, 0.9f);
+            set_mat(s.sphere_mat[i], PM_MAT_DIFFUSE, ar, ag, ab, 1.0f);
+        } else if (pick < 0.75f)
             set_mat(s.sphere_mat[i], PM_MAT_MIRROR, 1.0f, 1.0f, 1.0f, 1.0f);
         else
             set_mat(s.sphere_mat[i], PM_MAT_DIELECTRIC, 1.0f, 1.0f, 1.0f, 1.5f);

@@ -117,6 +117,12 @@ def _phys_protos(lib):
     lib.pmo64_emit.restype = i
     lib.pmo64_render.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32, vp, u32, vp]
     lib.pmo64_render.restype = None
+    lib.pmo_preset.argtypes = [i, ctypes.c_uint64, vp, vp]
+    lib.pmo_preset.restype = i
+    lib.pmo_knn_kd.argtypes = [vp, u32, vp, u32, i, f, vp, vp]
+    lib.pmo_knn_kd.restype = None
+    lib.pmo_set_gather_index.argtypes = [i]
+    lib.pmo_set_gather_index.restype = None
     lib.pmo_trace_path.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]
     lib.pmo_trace_path.restype = None
     lib.pmo64_radius_gather.argtypes = [vp, vp, vp, u32, vp, vp, u32, f, f, vp]
@@ -138,6 +144,60 @@ def phys_lib():
 
 
 NOISE_SEED_SALT = 0x6E6F697365
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("albedo", ctypes.c_float * 3), ("ior", ctypes.c_float)]
+
+
+class Scene(ctypes.Structure):
+    """pmo_scene: the memory layout of the product's pm_scene (float4
+    members 16-byte aligned, float2 8-byte), declared here so that CPU-only
+    callers need not load the product library."""
+    _fields_ = [
+        ("num_spheres", ctypes.c_int), ("_pad0", ctypes.c_byte * 12),
+        ("spheres", (ctypes.c_float * 4) * 64),
+        ("sphere_mat", Material * 64),
+        ("num_planes", ctypes.c_int), ("_pad1", ctypes.c_byte * 4),
+        ("planes", (ctypes.c_float * 2) * 8),
+        ("plane_mat", Material * 8),
+        ("box_min", ctypes.c_float * 3), ("box_max", ctypes.c_float * 3),
+        ("light", ctypes.c_float * 3), ("light_power", ctypes.c_float),
+        ("sigma_s", ctypes.c_float), ("sigma_a", ctypes.c_float), ("hg_g", ctypes.c_float),
+        ("het_res", ctypes.c_int), ("het_min", ctypes.c_float), ("het_max", ctypes.c_float),
+        ("cam_pos", ctypes.c_float * 3), ("focal", ctypes.c_float),
+        ("_pad2", ctypes.c_byte * 8),
+    ]
+
+
+class Config(ctypes.Structure):
+    """pmo_config: the memory layout of the product's pm_config."""
+    _fields_ = [
+        ("seed", ctypes.c_uint64), ("scene_id", ctypes.c_uint32),
+        ("surface_photons", ctypes.c_uint32), ("volume_photons", ctypes.c_uint32),
+        ("max_paths", ctypes.c_uint32), ("max_bounces", ctypes.c_int),
+        ("rr_survival", ctypes.c_float), ("width", ctypes.c_int), ("height", ctypes.c_int),
+        ("k", ctypes.c_int), ("radius", ctypes.c_float), ("march_step", ctypes.c_float),
+        ("leaf_size", ctypes.c_int), ("exposure", ctypes.c_float), ("_pad", ctypes.c_byte * 4),
+    ]
+
+
+def preset(which, seed):
+    """Benchmark preset `which` (1, 2, 3) from the oracle's restatement of
+    the product's scene generator: (Scene, Config), byte-equal to
+    pm_preset's."""
+    lib = phys_lib()
+    assert ctypes.sizeof(Scene) == lib.pmo_sizeof_scene()
+    assert ctypes.sizeof(Config) == lib.pmo_sizeof_config()
+    sc, cf = Scene(), Config()
+    if lib.pmo_preset(which, seed & (2 ** 64 - 1), ctypes.byref(sc), ctypes.byref(cf)) != 0:
+        raise ValueError("no preset %r" % (which,))
+    return sc, cf
+
+
+def set_gather_index(which):
+    """'kdtree' (default) or 'grid': the neighbour index of render()."""
+    phys_lib().pmo_set_gather_index({"grid": 0, "kdtree": 1}[which])
 
 
 def noise_grid(scene, cfg):
@@ -196,9 +256,20 @@ def knn(pos, queries, k, radius):
     return idx, d2
 
 
+def knn_kd(pos, queries, k, radius):
+    """knn() through the CPU kd-tree (the same sets)."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    idx = np.zeros((len(q), k), np.uint32)
+    d2 = np.zeros((len(q), k), np.float32)
+    phys_lib().pmo_knn_kd(pos.ctypes.data, len(pos), q.ctypes.data, len(q), k, radius,
+                          idx.ctypes.data, d2.ctypes.data)
+    return idx, d2
+
+
 def render_timed(scene, cfg, het, maps, pixels):
     """float32 render of `pixels`; returns (radiance, gathers[2], seconds[2]
-    = neighbour-grid build, shading)."""
+    = neighbour-index build, shading)."""
     pixels = np.ascontiguousarray(pixels, np.uint32)
     out = np.zeros((len(pixels), 4), np.float32)
     gathers = np.zeros(2, np.uint64)

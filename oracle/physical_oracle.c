@@ -357,16 +357,25 @@ void pmo_trace_path(const pmo_scene *scene, const pmo_config *cfg, const float *
 /* Traces paths 0, 1, 2, ... until each map holds its target (or max_paths
  * paths are spent) and fills the maps exactly as the GPU's compaction does:
  * records in path order, truncated at the target, index in pos[3], power
- * scaled by light_power / (paths the map drew from). */
+ * scaled by light_power / (paths the map drew from). Paths are traced in
+ * parallel rounds of PMO_EMIT_ROUND (each into its own slots) and merged in
+ * path order, so the maps equal a serial run's. */
+#define PMO_EMIT_ROUND 32768u
 int pmo_emit(const pmo_scene *scene, const pmo_config *cfg, const float *het, float (*spos)[4],
              float (*spow)[4], float (*vpos)[4], float (*vpow)[4], uint32_t *sizes,
              uint32_t *paths) {
-    const int mb = cfg->max_bounces;
-    float(*a)[4] = malloc(sizeof(float) * 4 * mb);
-    float(*b)[4] = malloc(sizeof(float) * 4 * mb);
-    float(*c)[4] = malloc(sizeof(float) * 4 * mb);
-    float(*e)[4] = malloc(sizeof(float) * 4 * mb);
-    if (!a || !b || !c || !e) { free(a); free(b); free(c); free(e); return -1; }
+    const int mb = cfg->max_bounces > 0 ? cfg->max_bounces : 1;
+    const size_t slots = (size_t)PMO_EMIT_ROUND * (size_t)mb;
+    float(*a)[4] = malloc(sizeof(float) * 4 * slots);
+    float(*b)[4] = malloc(sizeof(float) * 4 * slots);
+    float(*c)[4] = malloc(sizeof(float) * 4 * slots);
+    float(*e)[4] = malloc(sizeof(float) * 4 * slots);
+    uint32_t *ncs = malloc(sizeof(uint32_t) * PMO_EMIT_ROUND);
+    uint32_t *ncv = malloc(sizeof(uint32_t) * PMO_EMIT_ROUND);
+    if (!a || !b || !c || !e || !ncs || !ncv) {
+        free(a); free(b); free(c); free(e); free(ncs); free(ncv);
+        return -1;
+    }
     uint32_t targets[2] = {cfg->surface_photons, cfg->volume_photons};
     uint32_t n[2] = {0, 0}, np[2] = {0, 0};
     int done[2] = {targets[0] == 0, targets[1] == 0};
@@ -374,38 +383,44 @@ int pmo_emit(const pmo_scene *scene, const pmo_config *cfg, const float *het, fl
     uint64_t cap64 = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 16u;
     if (cap64 < 1024) cap64 = 1024;
     uint32_t cap = (uint32_t)cap64;
-    for (uint32_t id = 0; id < cap && !(done[0] && done[1]); ++id) {
-        uint32_t cs, cv;
-        pmo_trace_path(scene, cfg, het, id, a, b, &cs, c, e, &cv);
-        uint32_t cnt[2] = {cs, cv};
-        float(*src_pos[2])[4] = {a, c};
-        float(*src_pow[2])[4] = {b, e};
-        float(*dst_pos[2])[4] = {spos, vpos};
-        float(*dst_pow[2])[4] = {spow, vpow};
-        for (int m = 0; m < 2; ++m) {
-            if (done[m]) continue;
-            np[m] = id + 1;
-            for (uint32_t k = 0; k < cnt[m] && n[m] < targets[m]; ++k) {
-                memcpy(dst_pos[m][n[m]], src_pos[m][k], sizeof(float) * 4);
-                memcpy(dst_pow[m][n[m]], src_pow[m][k], sizeof(float) * 4);
-                dst_pos[m][n[m]][3] = u2f(n[m]);
-                n[m]++;
+    for (uint32_t base = 0; base < cap && !(done[0] && done[1]); base += PMO_EMIT_ROUND) {
+        const uint32_t m = cap - base < PMO_EMIT_ROUND ? cap - base : PMO_EMIT_ROUND;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long j = 0; j < (long)m; ++j)
+            pmo_trace_path(scene, cfg, het, base + (uint32_t)j, a + (size_t)j * mb, b + (size_t)j * mb,
+                           &ncs[j], c + (size_t)j * mb, e + (size_t)j * mb, &ncv[j]);
+        for (uint32_t j = 0; j < m && !(done[0] && done[1]); ++j) {
+            const uint32_t id = base + j;
+            uint32_t cnt[2] = {ncs[j], ncv[j]};
+            float(*src_pos[2])[4] = {a + (size_t)j * mb, c + (size_t)j * mb};
+            float(*src_pow[2])[4] = {b + (size_t)j * mb, e + (size_t)j * mb};
+            float(*dst_pos[2])[4] = {spos, vpos};
+            float(*dst_pow[2])[4] = {spow, vpow};
+            for (int mm = 0; mm < 2; ++mm) {
+                if (done[mm]) continue;
+                np[mm] = id + 1;
+                for (uint32_t k = 0; k < cnt[mm] && n[mm] < targets[mm]; ++k) {
+                    memcpy(dst_pos[mm][n[mm]], src_pos[mm][k], sizeof(float) * 4);
+                    memcpy(dst_pow[mm][n[mm]], src_pow[mm][k], sizeof(float) * 4);
+                    dst_pos[mm][n[mm]][3] = u2f(n[mm]);
+                    n[mm]++;
+                }
+                if (n[mm] >= targets[mm]) done[mm] = 1;
             }
-            if (n[m] >= targets[m]) done[m] = 1;
         }
     }
-    for (int m = 0; m < 2; ++m) {
-        float(*pw)[4] = m == 0 ? spow : vpow;
-        float scale = scene->light_power / (float)np[m];
-        for (uint32_t i = 0; i < n[m]; ++i) {
+    for (int mm = 0; mm < 2; ++mm) {
+        float(*pw)[4] = mm == 0 ? spow : vpow;
+        float scale = scene->light_power / (float)np[mm];
+        for (uint32_t i = 0; i < n[mm]; ++i) {
             pw[i][0] = pw[i][0] * scale;
             pw[i][1] = pw[i][1] * scale;
             pw[i][2] = pw[i][2] * scale;
         }
-        sizes[m] = n[m];
-        paths[m] = np[m];
+        sizes[mm] = n[mm];
+        paths[mm] = np[mm];
     }
-    free(a); free(b); free(c); free(e);
+    free(a); free(b); free(c); free(e); free(ncs); free(ncv);
     return 0;
 }
 
@@ -587,8 +602,18 @@ typedef struct {
     scn S;
     const float (*spos)[4], (*spow)[4], (*vpos)[4], (*vpow)[4];
     uint32_t ns, nv;
-    pmo_grid *gs, *gv;
+    pmo_grid *gs, *gv;  /* neighbour grids, or */
+    pmo_kd *ks, *kv;    /* kd-trees (pmo_set_gather_index) */
 } render_ctx;
+
+static int g_gather_index = PMO_GATHER_KDTREE;
+
+void pmo_set_gather_index(int which) { g_gather_index = which; }
+
+static int render_knn(const render_ctx *R, int vol, const float q[3], int k, float r2, uint64_t *keys) {
+    if (vol) return R->kv ? pmo_kd_knn(R->kv, q, k, r2, keys) : pmo_grid_knn(R->gv, q, k, r2, keys);
+    return R->ks ? pmo_kd_knn(R->ks, q, k, r2, keys) : pmo_grid_knn(R->gs, q, k, r2, keys);
+}
 
 static v3 shade(const render_ctx *R, uint32_t pix, uint64_t *counts) {
     const pmo_scene *s = R->s;
@@ -625,7 +650,7 @@ static v3 shade(const render_ctx *R, uint32_t pix, uint64_t *counts) {
                     float tau_mid = tau + st * (0.5f * dt);
                     if (R->nv > 0) {
                         float q[3] = {x.x, x.y, x.z};
-                        int cnt = pmo_grid_knn(R->gv, q, c->k, r2cap, keys);
+                        int cnt = render_knn(R, 1, q, c->k, r2cap, keys);
                         int found;
                         float r2;
                         v3 e = flux_sum(keys, cnt, c->k, R->vpow, 1, wo, s->hg_g, r2cap, &found, &r2);
@@ -648,7 +673,7 @@ static v3 shade(const render_ctx *R, uint32_t pix, uint64_t *counts) {
         if (m->kind == PMO_MAT_DIFFUSE) {
             if (R->ns > 0) {
                 float q[3] = {hp.x, hp.y, hp.z};
-                int cnt = pmo_grid_knn(R->gs, q, c->k, r2cap, keys);
+                int cnt = render_knn(R, 0, q, c->k, r2cap, keys);
                 int found;
                 float r2;
                 v3 e = flux_sum(keys, cnt, c->k, R->spow, 0, nf, 0.0f, r2cap, &found, &r2);
@@ -705,8 +730,15 @@ void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float
     R.S = make_scn(scene, het);
     R.spos = spos; R.spow = spow; R.vpos = vpos; R.vpow = vpow;
     R.ns = ns; R.nv = nv;
-    R.gs = pmo_grid_build(spos, ns, cfg->radius);
-    R.gv = pmo_grid_build(vpos, nv, cfg->radius);
+    R.gs = R.gv = NULL;
+    R.ks = R.kv = NULL;
+    if (g_gather_index == PMO_GATHER_KDTREE) {
+        R.ks = pmo_kd_build(spos, ns);
+        R.kv = pmo_kd_build(vpos, nv);
+    } else {
+        R.gs = pmo_grid_build(spos, ns, cfg->radius);
+        R.gv = pmo_grid_build(vpos, nv, cfg->radius);
+    }
     double t1 = omp_get_wtime();
     uint64_t total[2] = {0, 0};
 #pragma omp parallel
@@ -724,6 +756,8 @@ void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float
     if (seconds) { seconds[0] = t1 - t0; seconds[1] = omp_get_wtime() - t1; }
     pmo_grid_free(R.gs);
     pmo_grid_free(R.gv);
+    pmo_kd_free(R.ks);
+    pmo_kd_free(R.kv);
 }
 
 /* Value-noise grid of the heterogeneous medium (GPU: scene.cu). */

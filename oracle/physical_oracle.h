@@ -56,6 +56,21 @@ typedef struct pmo_config {
 } pmo_config;
 
 typedef struct pmo_grid pmo_grid;
+typedef struct pmo_kd pmo_kd;
+
+/* The benchmark presets 1-3 (preset_oracle.c; the bytes pm_preset writes). */
+int pmo_preset(int which, uint64_t seed, pmo_scene *scene, pmo_config *cfg);
+
+/* kd-tree k nearest neighbours (kdtree_oracle.c), pmo_grid_knn's contract. */
+pmo_kd *pmo_kd_build(const float (*pos)[4], uint32_t n);
+void pmo_kd_free(pmo_kd *t);
+int pmo_kd_knn(const pmo_kd *t, const float q[3], int k, float r2, uint64_t *keys);
+void pmo_knn_kd(const float (*pos)[4], uint32_t n, const float (*queries)[4], uint32_t nq, int k,
+                float radius, uint32_t *idx_out, float *d2_out);
+/* The neighbour index pmo_render's gathers use: a kd-tree per map (the
+ * default) or a uniform grid of cell = radius. The k-NN sets are the same. */
+enum { PMO_GATHER_GRID = 0, PMO_GATHER_KDTREE = 1 };
+void pmo_set_gather_index(int which);
 
 /* single precision, bit-exact with the GPU (physical_oracle.c) */
 void pmo_trace_path(const pmo_scene *scene, const pmo_config *cfg, const float *het, uint32_t id,
@@ -74,8 +89,8 @@ void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,
                 const float (*spos)[4], const float (*spow)[4], uint32_t ns,
                 const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
                 const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers);
-/* pmo_render with seconds[0] = neighbour-grid build time, seconds[1] =
- * shading time (all threads). */
+/* pmo_render with seconds[0] = neighbour-index build time (kd-trees or
+ * grids of both maps), seconds[1] = shading time (all threads). */
 void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float *het,
                       const float (*spos)[4], const float (*spow)[4], uint32_t ns,
                       const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,

@@ -287,6 +287,45 @@ def test_oracle_knn_matches_brute_force(ties):
         bi, bd = brute_knn(pos, q, k, r)
         np.testing.assert_array_equal(oi, bi)
         np.testing.assert_array_equal(od.view(np.uint32), bd.view(np.uint32))
+        # the CPU kd-tree (the benchmark's CPU gather) finds the same sets
+        ki, kd = oracle.knn_kd(pos, q, k, r)
+        np.testing.assert_array_equal(ki, bi)
+        np.testing.assert_array_equal(kd.view(np.uint32), bd.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [0, 1, 16, 17, 1000, 60000])
+def test_kdtree_knn_equals_grid_knn(n):
+    """Leaf-sized, just-above-leaf and large maps, a fifth of the points on a
+    lattice (exact distance ties), queries inside and outside the box."""
+    rs = np.random.RandomState(n + 3)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rs.uniform(0.0, 1.0, (n, 3))
+    pos[: n // 5, :3] = np.round(pos[: n // 5, :3] * 10) / 10
+    pos[:, 3] = np.arange(n, dtype=np.uint32).view(np.float32)
+    q = np.zeros((2000, 4), np.float32)
+    q[:, :3] = rs.uniform(-0.1, 1.1, (2000, 3))
+    q[:200, :3] = np.round(q[:200, :3] * 10) / 10
+    for k, r in [(1, 0.05), (64, 0.1), (128, 0.2)]:
+        gi, gd = oracle.knn(pos, q, k, r)
+        ki, kd = oracle.knn_kd(pos, q, k, r)
+        np.testing.assert_array_equal(ki, gi)
+        np.testing.assert_array_equal(kd.view(np.uint32), gd.view(np.uint32))
+
+
+def test_render_is_the_same_with_either_neighbour_index():
+    """pmo_render through kd-trees (the default) and through grids: the
+    same k-NN sets, so the same bits."""
+    sc, cf = oracle.preset(2, 0x5EED0002)
+    cf.surface_photons = cf.volume_photons = 20000
+    cf.width, cf.height = 40, 30
+    maps = oracle.emit(sc, cf, None)
+    try:
+        oracle.set_gather_index("grid")
+        a = oracle.render(sc, cf, None, maps)
+    finally:
+        oracle.set_gather_index("kdtree")
+    b = oracle.render(sc, cf, None, maps)
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
 # ---- presets (host only) -------------------------------------------------------
@@ -307,6 +346,17 @@ def test_presets(which, ns):
         assert kinds.count(photonmap.MAT_DIFFUSE) >= 1
     again = photonmap.preset(which, 0x5EED0000 + which)[0]
     assert bytes(again) == bytes(sc)
+
+
+@pytest.mark.parametrize("which", [1, 2, 3])
+def test_oracle_presets_equal_the_library_presets(which):
+    """The oracle's restatement of the scene generator (used where the
+    product library must not be loaded) writes the same bytes as pm_preset."""
+    for seed in (0x5EED0000 + which, 0, 2 ** 64 - 1):
+        a, b = oracle.preset(which, seed)
+        c, d = photonmap.preset(which, seed)
+        assert bytes(a) == bytes(c)
+        assert bytes(b) == bytes(d)
 
 
 def test_fixed_sum_is_order_independent_and_close_to_exact():
