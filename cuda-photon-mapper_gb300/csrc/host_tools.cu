@@ -1,9 +1,10 @@
 // host_tools.cu -- host-side utilities around the photon mapper: photon-map
-// files, PPM image output and a headless frame driver with the reference's
+// files, PPM and PNG image output and a headless frame driver with the reference's
 // display()/keyboard() semantics.
 #include "pm.h"
 #include "pm_ctx.cuh"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -78,6 +79,103 @@ pm_status pm_write_ppm(const char *path, const uchar4 *rgba, unsigned width, uns
         }
         ok = fwrite(row.data(), 1, row.size(), f) == row.size();
     }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? PM_OK : PM_ERR_INVALID;
+}
+
+// ---- PNG (ISO/IEC 15948): RGB 8-bit, the zlib stream in stored deflate blocks ----
+// (RFC 1950 / 1951), so no compression library is needed: the file is the
+// image's bytes plus framing, readable by any PNG decoder.
+
+namespace {
+
+uint32_t crc32_update(uint32_t crc, const unsigned char *p, size_t n) {
+    static uint32_t table[256];
+    static bool ready = false;
+    if (!ready) {  // the reflected CRC-32 polynomial 0xEDB88320 (ISO 3309)
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            table[i] = c;
+        }
+        ready = true;
+    }
+    for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
+    return crc;
+}
+
+void put_be32(std::vector<unsigned char> &v, uint32_t x) {
+    v.push_back((unsigned char)(x >> 24));
+    v.push_back((unsigned char)(x >> 16));
+    v.push_back((unsigned char)(x >> 8));
+    v.push_back((unsigned char)x);
+}
+
+bool write_chunk(FILE *f, const char *type, const std::vector<unsigned char> &data) {
+    std::vector<unsigned char> head;
+    put_be32(head, (uint32_t)data.size());
+    head.insert(head.end(), type, type + 4);
+    uint32_t crc = crc32_update(0xffffffffu, head.data() + 4, 4);
+    crc = crc32_update(crc, data.data(), data.size()) ^ 0xffffffffu;
+    std::vector<unsigned char> tail;
+    put_be32(tail, crc);
+    return fwrite(head.data(), 1, head.size(), f) == head.size() &&
+           (data.empty() || fwrite(data.data(), 1, data.size(), f) == data.size()) &&
+           fwrite(tail.data(), 1, 4, f) == 4;
+}
+
+}  // namespace
+
+pm_status pm_write_png(const char *path, const uchar4 *rgba, unsigned width, unsigned height) {
+    if (!path || !width || !height || !rgba) return PM_ERR_INVALID;
+    const size_t row = 1 + 3 * (size_t)width;  // filter byte 0, then RGB
+    const size_t raw = row * height;
+    if (row > 0x7fffffffu || raw > ((size_t)1 << 31)) return PM_ERR_LIMIT;
+    // the scanlines (filter type 0)
+    std::vector<unsigned char> img(raw);
+    for (unsigned y = 0; y < height; ++y) {
+        unsigned char *r = img.data() + y * row;
+        r[0] = 0;
+        for (unsigned x = 0; x < width; ++x) {
+            const uchar4 &p = rgba[(size_t)y * width + x];
+            r[1 + 3 * x] = p.x;
+            r[2 + 3 * x] = p.y;
+            r[3 + 3 * x] = p.z;
+        }
+    }
+    // zlib stream: header 0x78 0x01, stored blocks of <= 65535 bytes, Adler-32
+    std::vector<unsigned char> z;
+    z.reserve(raw + raw / 65535 * 5 + 16);
+    z.push_back(0x78);
+    z.push_back(0x01);
+    for (size_t at = 0; at < raw || raw == 0;) {
+        const size_t len = std::min<size_t>(65535, raw - at);
+        const bool last = at + len == raw;
+        z.push_back(last ? 1 : 0);
+        z.push_back((unsigned char)(len & 0xff));
+        z.push_back((unsigned char)(len >> 8));
+        z.push_back((unsigned char)(~len & 0xff));
+        z.push_back((unsigned char)((~len >> 8) & 0xff));
+        z.insert(z.end(), img.begin() + at, img.begin() + at + len);
+        at += len;
+        if (last) break;
+    }
+    uint32_t a = 1, b = 0;
+    for (size_t i = 0; i < raw; ++i) {
+        a = (a + img[i]) % 65521u;
+        b = (b + a) % 65521u;
+    }
+    put_be32(z, (b << 16) | a);
+    std::vector<unsigned char> ihdr;
+    put_be32(ihdr, width);
+    put_be32(ihdr, height);
+    const unsigned char rest[5] = {8, 2, 0, 0, 0};  // 8-bit, truecolour, deflate, filter 0, no interlace
+    ihdr.insert(ihdr.end(), rest, rest + 5);
+    FILE *f = fopen(path, "wb");
+    if (!f) return PM_ERR_INVALID;
+    static const unsigned char sig[8] = {0x89, 'P', 'N', 'G', 0x0d, 0x0a, 0x1a, 0x0a};
+    bool ok = fwrite(sig, 1, 8, f) == 8 && write_chunk(f, "IHDR", ihdr) && write_chunk(f, "IDAT", z) &&
+              write_chunk(f, "IEND", {});
     ok = (fclose(f) == 0) && ok;
     return ok ? PM_OK : PM_ERR_INVALID;
 }

@@ -148,6 +148,7 @@ PROTOTYPES = {
     "pm_save_map": (_i, [_vp, _i, _c.c_char_p]),
     "pm_load_map": (_i, [_vp, _i, _c.c_char_p]),
     "pm_write_ppm": (_i, [_c.c_char_p, _vp, _u, _u]),
+    "pm_write_png": (_i, [_c.c_char_p, _vp, _u, _u]),
     "pm_viewer_create": (_i, [_c.POINTER(_vp), _u, _u]),
     "pm_viewer_destroy": (None, [_vp]),
     "pm_viewer_key": (None, [_vp, _c.c_ubyte]),
@@ -571,6 +572,14 @@ def write_ppm(path, rgba):
     s = load().pm_write_ppm(path.encode(), a.ctypes.data, a.shape[1], a.shape[0])
     if s != PM_OK:
         raise PMError("pm_write_ppm(%s)" % path)
+
+
+def write_png(path, rgba):
+    """rgba: uint8 [h, w, 4] host array (alpha dropped)."""
+    a = np.ascontiguousarray(rgba, np.uint8)
+    s = load().pm_write_png(path.encode(), a.ctypes.data, a.shape[1], a.shape[0])
+    if s != PM_OK:
+        raise PMError("pm_write_png(%s)" % path)
 
 
 def preset(which, seed=0x5EED0000):

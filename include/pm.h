@@ -300,6 +300,10 @@ PM_API pm_status pm_load_map(pm_ctx *ctx, int map, const char *path);
  * the headless stand-in for the reference's GL blit (callbacksPBO.cpp:65-92). */
 PM_API pm_status pm_write_ppm(const char *path, const uchar4 *rgba, unsigned width,
                               unsigned height);
+/* The same pixels as an 8-bit RGB PNG (row 0 on top; the zlib stream in
+ * stored deflate blocks, so the file is about the size of a PPM). */
+PM_API pm_status pm_write_png(const char *path, const uchar4 *rgba, unsigned width,
+                              unsigned height);
 
 /* Headless frame driver with the reference's frame loop and keys
  * (callbacksPBO.cpp:19-27 state, :47-101 display, :104-143 keyboard): the
