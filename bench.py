@@ -1,27 +1,34 @@
 #!/usr/bin/env python
 """Frame benchmark of the GB300 photon mapper.
 
-One step = one frame of the physically based pipeline on benchmark preset 2
-(8 seeded spheres in the box, 1M surface + 1M volume photons, a kd-tree over
-each map, 1024x1024 eye rays with specular chains, a k=100 nearest-photon
-surface estimate and a volume march of step 0.01 with a k=100 volume
-estimate per step): pm_emit + pm_build + pm_render through the C ABI.
+One step = one frame of the physically based pipeline on benchmark preset 3,
+the 16M-photon volumetric scene (64 seeded spheres in the box, a
+heterogeneous 128^3 value-noise medium, 8M surface + 8M volume photons with
+up to 8 bounces, a kd-tree over each map, 1920x1080 eye rays with specular
+chains, a k=128 nearest-photon surface estimate and a volume march of step
+0.01 with a k=128 volume estimate per step): pm_emit + pm_build + pm_render
+through the C ABI.
 
 Prints one JSON line. `value` is k-NN gathers (surface + volume radiance
 estimates) per second of whole-frame device time; photon throughput and the
-per-phase times are reported beside it. Two more workloads ride on the same
-line: `cache` (the learned radiance cache on the same scene: online frame
-and cached render against the k-NN render, with the cached image's error
-against the k-NN image) and `batch` (64 independent scenes per frame in
-persistent multi-scene launches, captured as a CUDA graph).
+per-phase times are reported beside it, with the relative RMSE of sampled
+pixels against the FP64 oracle render (`fp64`) and their bit-equality with
+the FP32 oracle (`parity_sample`). More workloads ride on the same line:
+`preset2` (the 2M-photon scene, same metric), `cache` (the learned radiance
+cache on the preset-2 scene: online frame and cached render against the k-NN
+render, errors against the k-NN and FP64 renders), `batch` (64 independent
+scenes per frame captured as a CUDA graph) and `legacy` (the reference's own
+voxel frame).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Under torchrun each rank renders its own replica of the scene on its GPU
 (replicas only: the path has no exchange step); value = all ranks' gathers
 over the slowest rank's time. --impl reference times the CPU restatement of
-the same path (the reference has no physically based tracer of its own) on
-this host's cores, on a bounded sample of the same frame.
+the same path in oracle/ (the reference has no physically based tracer of
+its own) on this host's cores, without loading the product library: all
+threads, emission of a sample of the frame's photon paths and the gathers of
+a sample of its pixels through a kd-tree per map, per step.
 """
 import argparse
 import json
@@ -53,8 +60,13 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--preset", type=int, default=2)
-    ap.add_argument("--seed", type=lambda s: int(s, 0), default=0x5EED0002)
+    ap.add_argument("--preset", type=int, default=3)
+    ap.add_argument("--seed", type=lambda s: int(s, 0), default=None,
+                    help="scene seed (default 0x5EED0000 + preset)")
+    ap.add_argument("--secondary-preset", type=int, default=2,
+                    help="second scene timed on the same line (0: none)")
+    ap.add_argument("--fp64-pixels", type=int, default=8192,
+                    help="pixels sampled for the FP64 and FP32 oracle checks (0: none)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache A/B")
@@ -68,14 +80,36 @@ def parse_args():
     return ap.parse_args()
 
 
-def preset_config(args):
-    """The preset's scene and configuration, with --resolution applied."""
-    import photonmap
-    scene, cfg = photonmap.preset(args.preset, args.seed)
+def preset_config(args, preset=None, seed=None, product=True):
+    """The preset's scene and configuration, with --resolution applied: from
+    the product library (pm_preset) or, for the CPU-only reference arm, from
+    the oracle's byte-equal restatement."""
+    preset = args.preset if preset is None else preset
+    if seed is None:
+        seed = args.seed if (args.seed is not None and preset == args.preset) else 0x5EED0000 + preset
+    if product:
+        import photonmap
+        scene, cfg = photonmap.preset(preset, seed)
+    else:
+        import oracle
+        scene, cfg = oracle.preset(preset, seed)
     if args.resolution:
         w, h = (int(v) for v in args.resolution.lower().split("x"))
         cfg.width, cfg.height = w, h
     return scene, cfg
+
+
+def workload_config(args, preset, cfg, world=1):
+    """The `config` object both arms print for the same workload."""
+    return {
+        "workload": "preset %d: %s" % (preset, PRESET_DESC[preset]),
+        "preset": preset, "seed": int(cfg.seed), "resolution": [cfg.width, cfg.height],
+        "photons": [int(cfg.surface_photons), int(cfg.volume_photons)], "k": int(cfg.k),
+        "radius": float(cfg.radius), "march_step": float(cfg.march_step),
+        "max_bounces": int(cfg.max_bounces),
+        "l2": "flushed between timed GPU frames (256 MiB write, outside the timed events)",
+        "parallelism": "replicas x%d" % world,
+    }
 
 
 def dist_info():
@@ -170,34 +204,98 @@ def reduce_ranks(times, counts, device):
     return t.tolist(), c.tolist()
 
 
-def cpu_frame_sample(scene, cfg, pixels, seed=1234):
-    """The CPU restatement on a bounded sample of one frame: full photon
-    emission, neighbour grids over both maps, `pixels` random pixels shaded
-    with all host threads. Returns frame-equivalent numbers."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+class CpuFrame:
+    """The CPU restatement of one frame (oracle/, all host threads), timed on
+    bounded samples: a step traces 1/path_div of the frame's photon paths and
+    shades `pixels` random pixels through a kd-tree per map (built once);
+    the frame time is extrapolated from them plus the measured tree build.
+    maps: the frame's photon maps (None: the full CPU emission, timed)."""
+
+    def __init__(self, scene, cfg, het, maps=None, paths_total=None, pixels=CPU_SAMPLE_PIXELS,
+                 path_div=64):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        self.oracle = oracle
+        self.scene, self.cfg, self.het = scene, cfg, het
+        self.emit_full_s = None
+        if maps is None:
+            t0 = time.perf_counter()
+            maps = oracle.emit(scene, cfg, het)
+            self.emit_full_s = time.perf_counter() - t0
+            paths_total = int(max(maps.paths))
+        self.maps = maps
+        self.paths_total = int(paths_total)
+        self.renderer = oracle.Renderer(scene, cfg, het, maps)
+        self.build_s = self.renderer.build_s
+        self.npix = cfg.width * cfg.height
+        self.pixels = min(pixels, self.npix)
+        self.path_count = max(1, -(-self.paths_total // path_div))
+        self.threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+    def step(self, i):
+        import numpy as np
+        first = (i * self.path_count) % max(1, self.paths_total - self.path_count + 1)
+        t0 = time.perf_counter()
+        self.oracle.trace_sample(self.scene, self.cfg, self.het, first, self.path_count)
+        t1 = time.perf_counter()
+        rs = np.random.RandomState(1234 + i)
+        pix = np.sort(rs.choice(self.npix, size=self.pixels, replace=False)).astype(np.uint32)
+        _, gathers = self.renderer.pixels(pix)
+        t2 = time.perf_counter()
+        scale = self.npix / float(self.pixels)
+        frame_s = ((t1 - t0) * self.paths_total / self.path_count + self.build_s
+                   + (t2 - t1) * scale)
+        return {"wall_s": t2 - t0, "frame_s": frame_s,
+                "gathers_frame": float(gathers.sum()) * scale}
+
+    def sample_text(self):
+        src = ("maps from the full CPU emission (%.1f s, done once)" % self.emit_full_s
+               if self.emit_full_s is not None else "the GPU frame's maps (bit-equal to the CPU "
+               "emission's), copied to the host")
+        return ("per step, on %d threads: %d of the frame's %d photon paths traced (1/%d) and "
+                "%d random pixels of %dx%d shaded through a kd-tree per map (built once in %.2f "
+                "s); %s; frame time extrapolated from the samples plus the tree build"
+                % (self.threads, self.path_count, self.paths_total,
+                   -(-self.paths_total // self.path_count), self.pixels, self.cfg.width,
+                   self.cfg.height, self.build_s, src))
+
+    def close(self):
+        self.renderer.close()
+
+
+def rel_rmse(a, b):
     import numpy as np
+    a = np.asarray(a, np.float64)[:, :3]
+    b = np.asarray(b, np.float64)[:, :3]
+    return float(np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-300))
+
+
+def oracle_checks(scene, cfg, rad, npixels, fp32_maps=None, seed=77):
+    """Sampled-pixel checks of a GPU frame's radiance `rad` (host [npix, 4]):
+    relative RMSE against the FP64 oracle render (own FP64 emission) and,
+    when the frame's maps are given, bit-equality with the FP32 oracle render
+    over them. Returns (dict, pixels, fp64 radiance of those pixels)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     het = oracle.noise_grid(scene, cfg)
-    t0 = time.perf_counter()
-    maps = oracle.emit(scene, cfg, het)
-    t_emit = time.perf_counter() - t0
     npix = cfg.width * cfg.height
     rs = np.random.RandomState(seed)
-    pix = np.sort(rs.choice(npix, size=min(pixels, npix), replace=False)).astype(np.uint32)
-    _, gathers, secs = oracle.render_timed(scene, cfg, het, maps, pix)
-    scale = npix / float(len(pix))
-    g_frame = float(gathers.sum()) * scale
-    t_frame = t_emit + secs[0] + secs[1] * scale
-    return {
-        "gathers_per_s": g_frame / t_frame,
-        "frame_s": t_frame,
-        "emit_s": t_emit,
-        "grid_s": float(secs[0]),
-        "shade_sample_s": float(secs[1]),
-        "sample_pixels": int(len(pix)),
-        "paths": int(max(maps.paths)),
-        "cores": os.cpu_count(),
-    }
+    pix = np.sort(rs.choice(npix, size=min(npixels, npix), replace=False)).astype(np.uint32)
+    t0 = time.perf_counter()
+    m64 = oracle.emit(scene, cfg, het, double=True)
+    r64 = oracle.render(scene, cfg, het, m64, pixels=pix, double=True)
+    out = {"pixels": int(len(pix)), "rel_rmse": rel_rmse(rad[pix], r64),
+           "seconds": time.perf_counter() - t0,
+           "what": "GPU FP32 frame vs the FP64 oracle (own FP64 emission and render) on random "
+                   "pixels"}
+    parity = None
+    if fp32_maps is not None:
+        r32 = oracle.render(scene, cfg, het, fp32_maps, pixels=pix)
+        same = np.all(r32.view(np.uint32) == rad[pix].view(np.uint32), axis=1)
+        parity = {"pixels": int(len(pix)), "bit_equal_fraction": float(same.mean()),
+                  "what": "GPU radiance vs the FP32 oracle render over the GPU's maps"}
+    return out, parity, pix, r64
 
 
 def peaks_bf16():
@@ -223,7 +321,7 @@ CACHE_INFER_FLOPS = 2 * (4 * 64 * 64 + 64 * 16)
 CACHE_TRAIN_FLOPS = 2 * CACHE_INFER_FLOPS + 2 * (2 * 128 * 128 + 128 * 16)
 
 
-def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak):
+def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak, fp64=None):
     """The learned radiance cache on the same scene and photon maps: after
     `cache_warm_frames` online training frames, each timed step is one online
     frame (2^20 k-NN training samples + their Adam steps, then the cached
@@ -263,6 +361,11 @@ def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak):
             values_ms.append(cs.ms_values)
         cached = rad[:, :3].double().cpu().numpy()
     err = float(np.sqrt(np.mean((cached - knn_img) ** 2)) / np.sqrt(np.mean(knn_img ** 2)))
+    fp64_err = None
+    if fp64 is not None:
+        pix, r64 = fp64
+        fp64_err = {"cached": rel_rmse(cached[pix], r64), "knn": rel_rmse(knn_img[pix], r64),
+                    "pixels": int(len(pix))}
     nq = cs.queries
     values_s = statistics.mean(values_ms) / 1e3
     infer_tflops = nq * CACHE_INFER_FLOPS / values_s / 1e12
@@ -283,6 +386,7 @@ def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak):
         "speedup_online_frame": knn_render_ms / statistics.mean(frame_ms),
         "speedup_render": knn_render_ms / statistics.mean(render_ms),
         "rel_rmse_vs_knn": err,
+        "rel_rmse_vs_fp64": fp64_err,
         "queries_per_frame": int(nq), "queries_per_s": nq / values_s,
         "loss": float(cs.loss),
         "tensor": {"infer_tflops": infer_tflops, "train_tflops": train_tflops,
@@ -434,39 +538,137 @@ def legacy_frames(ctx, args, with_cpu):
 
 
 def run_reference(args):
+    """The CPU restatement of the path (oracle/, all host threads) on the
+    same workload and config; never loads the product library."""
     world, rank, _ = dist_info()
     if rank != 0:
         return 0
-    import photonmap
-    scene, cfg = preset_config(args)
-    threads = os.cpu_count()
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    for _ in range(args.warmup):
-        cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
-    vals, frames = [], []
-    for i in range(args.steps):
-        r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS, seed=1234 + i)
-        vals.append(r["gathers_per_s"])
-        frames.append(r["frame_s"])
-    value = statistics.mean(vals)
-    sample = ("per step: full CPU photon emission (%d paths, 1 thread), neighbour grids, "
-              "%d random pixels of %dx%d shaded on %d threads; frame time extrapolated to all "
-              "pixels" % (r["paths"], CPU_SAMPLE_PIXELS, cfg.width, cfg.height, threads))
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))  # before the oracle's OpenMP starts
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    scene, cfg = preset_config(args, product=False)
+    het = oracle.noise_grid(scene, cfg)
+    t0 = time.perf_counter()
+    cpu = CpuFrame(scene, cfg, het)
+    setup_s = time.perf_counter() - t0
+    for i in range(args.warmup):
+        cpu.step(i)
+    res = [cpu.step(args.warmup + i) for i in range(args.steps)]
+    frame_s = statistics.mean(r["frame_s"] for r in res)
+    gathers = statistics.mean(r["gathers_frame"] for r in res)
+    value = gathers / frame_s
+    cores = int(os.environ.get("OMP_NUM_THREADS", threads))
     line = {
         "impl": "reference",
         "metric": "gathers/s", "value": value, "unit": "gathers/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * statistics.mean(frames), "higher_is_better": True,
+        "ms_per_step": 1e3 * statistics.mean(r["wall_s"] for r in res),
+        "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "preset %d: %s" % (args.preset, PRESET_DESC[args.preset]),
-                   "preset": args.preset},
-        "cpu_baseline": {"value": value, "unit": "gathers/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+        "config": workload_config(args, args.preset, cfg, world),
+        "frame_ms_extrapolated": 1e3 * frame_s,
+        "setup_s": setup_s,
+        "cpu_baseline": {"value": value, "unit": "gathers/s", "cores": cores, "kind": "port",
+                         "sample": cpu.sample_text()},
         "e2e": {"value": value, "unit": "gathers/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    cpu.close()
     print(json.dumps(line))
     return 0
+
+
+def measure_frames(ctx, lib, scene, cfg, stream, flush, steps, warmup, barrier, device):
+    """Times `steps` frames (pm_emit + pm_build + pm_render) after `warmup`,
+    with CUDA events on the library's stream and an L2 flush before each."""
+    import torch
+    ctx.set_scene(scene, cfg)
+    sh = stream.cuda_stream
+    npix = cfg.width * cfg.height
+    rad = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
+    rgba = torch.empty((npix, 4), dtype=torch.uint8, device="cuda")
+
+    def frame():
+        ctx.emit(sh)
+        ctx.build(sh)
+        ctx.render(rad.data_ptr(), rgba.data_ptr(), sh)
+
+    r = {"frame_ms": [], "emit_ms": [], "build_ms": [], "render_ms": [], "gather_ms": [],
+         "surf": 0, "vol": 0, "paths": 0, "rad": rad, "rgba": rgba, "frame": frame}
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            flush.zero_()
+            frame()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(device)
+        clocks.start()
+        l0 = lib.pm_kernel_launches()
+        for _ in range(steps):
+            flush.zero_()  # L2 flush between frames, before the start event
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            frame()
+            ev1.record(stream)
+            ev1.synchronize()
+            st = ctx.stats()
+            r["frame_ms"].append(ev0.elapsed_time(ev1))
+            r["emit_ms"].append(st.ms_emit)
+            r["build_ms"].append(st.ms_build)
+            r["render_ms"].append(st.ms_render)
+            r["gather_ms"].append(st.ms_gather)
+            r["surf"] += st.surface_gathers
+            r["vol"] += st.volume_gathers
+            r["paths"] += st.paths_traced
+        r["launches"] = lib.pm_kernel_launches() - l0
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        r["clocks"] = clocks.stop()
+        r["map_sizes"] = list(st.map_size)
+    return r
+
+
+def phases_of(r, steps, world=1):
+    return {
+        "emit_ms": statistics.mean(r["emit_ms"]), "build_ms": statistics.mean(r["build_ms"]),
+        "render_ms": statistics.mean(r["render_ms"]), "gather_ms": statistics.mean(r["gather_ms"]),
+        "frame_ms": statistics.mean(r["frame_ms"]),
+        "paths_per_frame": r["paths"] / steps / world,
+        "photons_per_s": r["paths"] / (sum(r["emit_ms"]) / 1e3) / world,
+        "records_per_s": sum(r["map_sizes"]) * steps / (sum(r["emit_ms"]) / 1e3),
+        "map_sizes": r["map_sizes"],
+        "surface_gathers_per_frame": r["surf"] / steps,
+        "volume_gathers_per_frame": r["vol"] / steps,
+    }
+
+
+def estimate_roofline(r, steps, k, peak, peak_kind, traffic):
+    """The k-NN estimate pass against HBM: per query the k records' 32 B
+    (position + power), the 32 B query record, its 4 B index in spatial order
+    and the 16 B value written, over the pass's CUDA-event time."""
+    gather_s = statistics.mean(r["gather_ms"]) / 1e3
+    q_per_frame = (r["surf"] + r["vol"]) / steps
+    alg_bytes = q_per_frame * (32.0 * k + 52.0)
+    achieved = alg_bytes / gather_s / 1e9
+    return {"bound": "hbm", "kernel": "query_knn_tile_kernel", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+            "formula": "gathers x (32 B x k + 52 B), over the CUDA-event time of the k-NN "
+                       "estimate pass (anchor, shared-candidate and deferred launches; events "
+                       "on the render stream)"}
+
+
+def host_maps(ctx):
+    """The context's two photon maps copied to the host as oracle maps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    spos, spow = ctx.photons_soa(0)
+    vpos, vpow = ctx.photons_soa(1)
+    return oracle.maps_from_arrays(spos, spow, vpos, vpow)
 
 
 def run_ours(args):
@@ -482,12 +684,8 @@ def run_ours(args):
     scene, cfg = preset_config(args)
     cfg.scene_id = rank  # each replica traces its own photon streams
     ctx = photonmap.Context(local)
-    ctx.set_scene(scene, cfg)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
-    npix = cfg.width * cfg.height
-    rad = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
-    rgba = torch.empty((npix, 4), dtype=torch.uint8, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -495,48 +693,14 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def frame():
-        ctx.emit(sh)
-        ctx.build(sh)
-        ctx.render(rad.data_ptr(), rgba.data_ptr(), sh)
-
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            flush.zero_()
-            frame()
-        torch.cuda.synchronize()
-        barrier()
-        torch.cuda.synchronize()
-        clocks = ClockSampler(local)
-        clocks.start()
-        l0 = lib.pm_kernel_launches()
-        frame_ms, emit_ms, build_ms, render_ms, gather_ms = [], [], [], [], []
-        gathers = surf = vol = paths = 0
-        for _ in range(args.steps):
-            flush.zero_()  # L2 flush between frames, before the start event
-            ev0 = torch.cuda.Event(enable_timing=True)
-            ev1 = torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            frame()
-            ev1.record(stream)
-            ev1.synchronize()
-            st = ctx.stats()
-            frame_ms.append(ev0.elapsed_time(ev1))
-            emit_ms.append(st.ms_emit)
-            build_ms.append(st.ms_build)
-            render_ms.append(st.ms_render)
-            gather_ms.append(st.ms_gather)
-            surf += st.surface_gathers
-            vol += st.volume_gathers
-            paths += st.paths_traced
-        launches = lib.pm_kernel_launches() - l0
-        torch.cuda.synchronize()
-        barrier()
-        torch.cuda.synchronize()
-        clk = clocks.stop()
-        map_sizes = list(st.map_size)
-    gathers = surf + vol
-    t_total = sum(frame_ms) / 1e3
+    head = measure_frames(ctx, lib, scene, cfg, stream, flush, args.steps, args.warmup, barrier,
+                          local)
+    frame = head["frame"]
+    rad, rgba = head["rad"], head["rgba"]
+    npix = cfg.width * cfg.height
+    gathers = head["surf"] + head["vol"]
+    t_total = sum(head["frame_ms"]) / 1e3
+    paths, launches = head["paths"], head["launches"]
 
     # end to end through the C ABI: per step the scene goes in from host
     # memory (pm_update_scene), the frame's radiance and 8-bit image come
@@ -567,14 +731,6 @@ def run_ours(args):
         return 0
 
     peak, peak_kind = load_peaks()
-    k = cfg.k
-    gather_s = statistics.mean(gather_ms) / 1e3
-    q_per_frame = (surf + vol) / args.steps
-    # per query: k records of 32 B (position + power), the 32 B query record,
-    # its 4 B index in spatial order and the 16 B value written
-    alg_bytes = q_per_frame * (32.0 * k + 52.0)
-    achieved = alg_bytes / gather_s / 1e9
-    traffic = load_traffic(args.preset)
     line = {
         "metric": "gathers/s",
         "value": gathers / t_total,
@@ -588,56 +744,67 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {
-            "workload": "preset %d: %s" % (args.preset, PRESET_DESC[args.preset]),
-            "preset": args.preset, "seed": args.seed, "resolution": [cfg.width, cfg.height],
-            "photons": [cfg.surface_photons, cfg.volume_photons], "k": k,
-            "radius": cfg.radius, "march_step": cfg.march_step,
-            "l2": "flushed between timed frames (256 MiB write, outside the timed events)",
-            "parallelism": "replicas x%d" % world,
-        },
-        "phases": {
-            "emit_ms": statistics.mean(emit_ms), "build_ms": statistics.mean(build_ms),
-            "render_ms": statistics.mean(render_ms), "gather_ms": statistics.mean(gather_ms),
-            "frame_ms": statistics.mean(frame_ms),
-            "paths_per_frame": paths / args.steps / world,
-            "photons_per_s": paths / (sum(emit_ms) / 1e3) / world,
-            "records_per_s": sum(map_sizes) * args.steps / (sum(emit_ms) / 1e3),
-            "map_sizes": map_sizes,
-            "surface_gathers_per_frame": surf / args.steps,
-            "volume_gathers_per_frame": vol / args.steps,
-        },
+        "config": workload_config(args, args.preset, cfg, world),
+        "phases": phases_of(head, args.steps, world),
         "e2e": {"value": e2e_g / t_e2e, "unit": "gathers/s",
                 "h2d_bytes_per_step": int(photonmap.ctypes.sizeof(photonmap.Scene)),
                 "d2h_bytes_per_step": int(npix * (16 + 4)),
                 "steps": args.e2e_steps},
-        "roofline": {"bound": "hbm", "kernel": "query_knn_tile_kernel", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind,
-                     "traffic": traffic,
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "formula": "gathers x (32 B x k + 52 B), over the CUDA-event time of the "
-                                "k-NN estimate pass (anchor, shared-candidate and deferred "
-                                "launches; events on the render stream)"},
+        "roofline": estimate_roofline(head, args.steps, cfg.k, peak, peak_kind,
+                                      load_traffic(args.preset)),
         "gpu_launches": int(launches),
-        "clocks": clk,
+        "clocks": head["clocks"],
     }
-    if not args.no_cache:
-        line["cache"] = cache_ab(ctx, lib, stream, rad, flush, args, cfg,
-                                 statistics.mean(render_ms), peaks_bf16())
-    if not args.no_batch:
-        line["batch"] = batch_frames(ctx, lib, args, local)
-    if not args.no_legacy:
-        line["legacy"] = legacy_frames(ctx, args, with_cpu=(world == 1 and not args.no_cpu_baseline))
-    if world == 1 and not args.no_cpu_baseline:
-        r = cpu_frame_sample(scene, cfg, CPU_SAMPLE_PIXELS)
-        line["cpu_baseline"] = {
-            "value": r["gathers_per_s"], "unit": "gathers/s", "cores": r["cores"], "kind": "port",
-            "sample": "full CPU photon emission (%d paths, 1 thread) + neighbour grids + %d "
-                      "random pixels shaded on %d threads, frame time extrapolated to %dx%d"
-                      % (r["paths"], r["sample_pixels"], r["cores"], cfg.width, cfg.height),
-            "frame_s": r["frame_s"],
+    single = world == 1
+    if single and (args.fp64_pixels or not args.no_cpu_baseline):
+        gpu_maps = host_maps(ctx)
+        rad_host = host_rad.numpy().copy()
+        if args.fp64_pixels:
+            line["fp64"], line["parity_sample"], _, _ = oracle_checks(
+                scene, cfg, rad_host, args.fp64_pixels, gpu_maps)
+        if not args.no_cpu_baseline:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            cpu = CpuFrame(scene, cfg, oracle.noise_grid(scene, cfg), maps=gpu_maps,
+                           paths_total=head["paths"] / args.steps)
+            res = [cpu.step(i) for i in range(2)]
+            fs = statistics.mean(r["frame_s"] for r in res)
+            line["cpu_baseline"] = {
+                "value": statistics.mean(r["gathers_frame"] for r in res) / fs,
+                "unit": "gathers/s", "cores": cpu.threads, "kind": "port",
+                "sample": cpu.sample_text(), "frame_s_extrapolated": fs,
+                "wall_s_per_step": statistics.mean(r["wall_s"] for r in res)}
+            cpu.close()
+        del gpu_maps
+    if single and args.secondary_preset:
+        p2 = args.secondary_preset
+        sc2, cf2 = preset_config(args, p2)
+        steps2 = max(3, args.steps // 4)
+        sec = measure_frames(ctx, lib, sc2, cf2, stream, flush, steps2, min(args.warmup, 3),
+                             barrier, local)
+        g2 = sec["surf"] + sec["vol"]
+        line["preset%d" % p2] = {
+            "config": workload_config(args, p2, cf2),
+            "value": g2 / (sum(sec["frame_ms"]) / 1e3), "unit": "gathers/s",
+            "ms_per_step": statistics.mean(sec["frame_ms"]), "steps": steps2,
+            "phases": phases_of(sec, steps2),
+            "roofline": estimate_roofline(sec, steps2, cf2.k, peak, peak_kind, load_traffic(p2)),
+            "clocks": sec["clocks"],
         }
+        fp64_2 = None
+        if args.fp64_pixels:
+            rad2 = sec["rad"].cpu().numpy()
+            chk, par, pix2, r64_2 = oracle_checks(sc2, cf2, rad2, args.fp64_pixels, host_maps(ctx))
+            line["preset%d" % p2]["fp64"] = chk
+            line["preset%d" % p2]["parity_sample"] = par
+            fp64_2 = (pix2, r64_2)
+        if not args.no_cache:
+            line["cache"] = cache_ab(ctx, lib, stream, sec["rad"], flush, args, cf2,
+                                     statistics.mean(sec["render_ms"]), peaks_bf16(), fp64_2)
+    if single and not args.no_batch:
+        line["batch"] = batch_frames(ctx, lib, args, local)
+    if single and not args.no_legacy:
+        line["legacy"] = legacy_frames(ctx, args, with_cpu=not args.no_cpu_baseline)
     print(json.dumps(line))
     return 0
 

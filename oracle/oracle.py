@@ -123,6 +123,14 @@ def _phys_protos(lib):
     lib.pmo_knn_kd.restype = None
     lib.pmo_set_gather_index.argtypes = [i]
     lib.pmo_set_gather_index.restype = None
+    lib.pmo_render_create.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32]
+    lib.pmo_render_create.restype = vp
+    lib.pmo_render_pixels.argtypes = [vp, vp, u32, vp, vp]
+    lib.pmo_render_pixels.restype = None
+    lib.pmo_render_free.argtypes = [vp]
+    lib.pmo_render_free.restype = None
+    lib.pmo_trace_sample.argtypes = [vp, vp, vp, u32, u32]
+    lib.pmo_trace_sample.restype = ctypes.c_uint64
     lib.pmo_trace_path.argtypes = [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]
     lib.pmo_trace_path.restype = None
     lib.pmo64_radius_gather.argtypes = [vp, vp, vp, u32, vp, vp, u32, f, f, vp]
@@ -280,6 +288,54 @@ def render_timed(scene, cfg, het, maps, pixels):
                                 pixels.ctypes.data, len(pixels), out.ctypes.data,
                                 gathers.ctypes.data, secs.ctypes.data)
     return out, gathers, secs
+
+
+class Renderer:
+    """float32 renders of pixel samples over fixed maps: the neighbour
+    indexes are built once (build_s) and reused by every pixels() call."""
+
+    def __init__(self, scene, cfg, het, maps):
+        import time
+        self.lib = phys_lib()
+        self.keep = (scene, cfg, het, maps)
+        t0 = time.perf_counter()
+        self.h = self.lib.pmo_render_create(
+            ctypes.byref(scene), ctypes.byref(cfg), _ptr(het), maps.spos.ctypes.data,
+            maps.spow.ctypes.data, len(maps.spos), maps.vpos.ctypes.data, maps.vpow.ctypes.data,
+            len(maps.vpos))
+        self.build_s = time.perf_counter() - t0
+
+    def pixels(self, pixels):
+        """(radiance [n, 4], gathers [2]) of the given pixel indices."""
+        pixels = np.ascontiguousarray(pixels, np.uint32)
+        out = np.zeros((len(pixels), 4), np.float32)
+        gathers = np.zeros(2, np.uint64)
+        self.lib.pmo_render_pixels(self.h, pixels.ctypes.data, len(pixels), out.ctypes.data,
+                                   gathers.ctypes.data)
+        return out, gathers
+
+    def close(self):
+        if self.h:
+            self.lib.pmo_render_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def trace_sample(scene, cfg, het, first, count):
+    """Traces paths first .. first + count - 1 on all threads (timing sample
+    of the emission); returns the records they produced."""
+    return int(phys_lib().pmo_trace_sample(ctypes.byref(scene), ctypes.byref(cfg), _ptr(het),
+                                           first, count))
+
+
+def maps_from_arrays(spos, spow, vpos, vpow):
+    """PhysicalMaps over given float32 [n, 4] record arrays (e.g. a GPU
+    map copied to the host)."""
+    a = [np.ascontiguousarray(x, np.float32) for x in (spos, spow, vpos, vpow)]
+    sizes = np.array([len(a[0]), len(a[2])], np.uint32)
+    return PhysicalMaps(a[0], a[1], a[2], a[3], sizes, np.zeros(2, np.uint32))
 
 
 def render(scene, cfg, het, maps, pixels=None, double=False):

@@ -718,46 +718,93 @@ void pmo_render(const pmo_scene *scene, const pmo_config *cfg, const float *het,
     pmo_render_timed(scene, cfg, het, spos, spow, ns, vpos, vpow, nv, pixels, npix, out, gathers, NULL);
 }
 
-void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float *het,
-                      const float (*spos)[4], const float (*spow)[4], uint32_t ns,
-                      const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
-                      const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers,
-                      double *seconds) {
-    double t0 = omp_get_wtime();
+struct pmo_render_ctx {
     render_ctx R;
-    R.s = scene;
-    R.c = cfg;
-    R.S = make_scn(scene, het);
-    R.spos = spos; R.spow = spow; R.vpos = vpos; R.vpow = vpow;
-    R.ns = ns; R.nv = nv;
-    R.gs = R.gv = NULL;
-    R.ks = R.kv = NULL;
+    pmo_scene scene;
+    pmo_config cfg;
+};
+
+pmo_render_ctx *pmo_render_create(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                                  const float (*spos)[4], const float (*spow)[4], uint32_t ns,
+                                  const float (*vpos)[4], const float (*vpow)[4], uint32_t nv) {
+    pmo_render_ctx *x = calloc(1, sizeof(pmo_render_ctx));
+    if (!x) return NULL;
+    x->scene = *scene;
+    x->cfg = *cfg;
+    render_ctx *R = &x->R;
+    R->s = &x->scene;
+    R->c = &x->cfg;
+    R->S = make_scn(&x->scene, het);
+    R->spos = spos; R->spow = spow; R->vpos = vpos; R->vpow = vpow;
+    R->ns = ns; R->nv = nv;
     if (g_gather_index == PMO_GATHER_KDTREE) {
-        R.ks = pmo_kd_build(spos, ns);
-        R.kv = pmo_kd_build(vpos, nv);
+        R->ks = pmo_kd_build(spos, ns);
+        R->kv = pmo_kd_build(vpos, nv);
     } else {
-        R.gs = pmo_grid_build(spos, ns, cfg->radius);
-        R.gv = pmo_grid_build(vpos, nv, cfg->radius);
+        R->gs = pmo_grid_build(spos, ns, cfg->radius);
+        R->gv = pmo_grid_build(vpos, nv, cfg->radius);
     }
-    double t1 = omp_get_wtime();
+    return x;
+}
+
+void pmo_render_pixels(const pmo_render_ctx *x, const uint32_t *pixels, uint32_t npix,
+                       float (*out)[4], uint64_t *gathers) {
     uint64_t total[2] = {0, 0};
 #pragma omp parallel
     {
         uint64_t local[2] = {0, 0};
 #pragma omp for schedule(dynamic, 16)
         for (long i = 0; i < (long)npix; ++i) {
-            v3 L = shade(&R, pixels[i], local);
+            v3 L = shade(&x->R, pixels[i], local);
             out[i][0] = L.x; out[i][1] = L.y; out[i][2] = L.z; out[i][3] = 1.0f;
         }
 #pragma omp critical
         { total[0] += local[0]; total[1] += local[1]; }
     }
     if (gathers) { gathers[0] = total[0]; gathers[1] = total[1]; }
+}
+
+void pmo_render_free(pmo_render_ctx *x) {
+    if (!x) return;
+    pmo_grid_free(x->R.gs);
+    pmo_grid_free(x->R.gv);
+    pmo_kd_free(x->R.ks);
+    pmo_kd_free(x->R.kv);
+    free(x);
+}
+
+void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                      const float (*spos)[4], const float (*spow)[4], uint32_t ns,
+                      const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
+                      const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers,
+                      double *seconds) {
+    double t0 = omp_get_wtime();
+    pmo_render_ctx *x = pmo_render_create(scene, cfg, het, spos, spow, ns, vpos, vpow, nv);
+    double t1 = omp_get_wtime();
+    pmo_render_pixels(x, pixels, npix, out, gathers);
     if (seconds) { seconds[0] = t1 - t0; seconds[1] = omp_get_wtime() - t1; }
-    pmo_grid_free(R.gs);
-    pmo_grid_free(R.gv);
-    pmo_kd_free(R.ks);
-    pmo_kd_free(R.kv);
+    pmo_render_free(x);
+}
+
+uint64_t pmo_trace_sample(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                          uint32_t first, uint32_t count) {
+    const int mb = cfg->max_bounces > 0 ? cfg->max_bounces : 1;
+    uint64_t records = 0;
+#pragma omp parallel reduction(+ : records)
+    {
+        float(*a)[4] = malloc(sizeof(float) * 4 * mb);
+        float(*b)[4] = malloc(sizeof(float) * 4 * mb);
+        float(*c)[4] = malloc(sizeof(float) * 4 * mb);
+        float(*e)[4] = malloc(sizeof(float) * 4 * mb);
+#pragma omp for schedule(dynamic, 256)
+        for (long j = 0; j < (long)count; ++j) {
+            uint32_t cs = 0, cv = 0;
+            if (a && b && c && e) pmo_trace_path(scene, cfg, het, first + (uint32_t)j, a, b, &cs, c, e, &cv);
+            records += cs + cv;
+        }
+        free(a); free(b); free(c); free(e);
+    }
+    return records;
 }
 
 /* Value-noise grid of the heterogeneous medium (GPU: scene.cu). */

@@ -96,6 +96,21 @@ void pmo_render_timed(const pmo_scene *scene, const pmo_config *cfg, const float
                       const float (*vpos)[4], const float (*vpow)[4], uint32_t nv,
                       const uint32_t *pixels, uint32_t npix, float (*out)[4], uint64_t *gathers,
                       double *seconds);
+/* A render context that keeps its neighbour indexes (built once) for
+ * repeated pixel samples; pmo_render_pixels runs on all threads. The maps
+ * must outlive the context. */
+typedef struct pmo_render_ctx pmo_render_ctx;
+pmo_render_ctx *pmo_render_create(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                                  const float (*spos)[4], const float (*spow)[4], uint32_t ns,
+                                  const float (*vpos)[4], const float (*vpow)[4], uint32_t nv);
+void pmo_render_pixels(const pmo_render_ctx *x, const uint32_t *pixels, uint32_t npix,
+                       float (*out)[4], uint64_t *gathers);
+void pmo_render_free(pmo_render_ctx *x);
+/* Traces paths first .. first + count - 1 on all threads without keeping
+ * their records (a timing sample of the emission); returns the records the
+ * paths produced. */
+uint64_t pmo_trace_sample(const pmo_scene *scene, const pmo_config *cfg, const float *het,
+                          uint32_t first, uint32_t count);
 void pmo_noise_grid(float *grid, int res, uint64_t seed, float lo, float hi);
 void pmo_philox(uint64_t seed, const uint32_t *ctr, uint32_t *out);
 float pmo_logf(float x);

@@ -271,42 +271,61 @@ static void trace_path(const pmo_scene *s, const pmo_config *cfg, const float *h
     *nv_out = nv < (uint32_t)mb ? nv : (uint32_t)mb;
 }
 
+/* Paths traced in parallel rounds, each into its own slots, then merged in
+ * path order: the maps equal a serial run's. */
+#define PMO64_EMIT_ROUND 32768u
 int pmo64_emit(const pmo_scene *scene, const pmo_config *cfg, const float *het, double *spos,
                double *spow, double *vpos, double *vpow, uint32_t *sizes, uint32_t *paths) {
-    const int mb = cfg->max_bounces;
-    double *a = malloc(sizeof(double) * 4 * mb), *b = malloc(sizeof(double) * 6 * mb);
-    double *c = malloc(sizeof(double) * 4 * mb), *e = malloc(sizeof(double) * 6 * mb);
+    const int mb = cfg->max_bounces > 0 ? cfg->max_bounces : 1;
+    const size_t slots = (size_t)PMO64_EMIT_ROUND * (size_t)mb;
+    double *a = malloc(sizeof(double) * 4 * slots), *b = malloc(sizeof(double) * 6 * slots);
+    double *c = malloc(sizeof(double) * 4 * slots), *e = malloc(sizeof(double) * 6 * slots);
+    uint32_t *ncs = malloc(sizeof(uint32_t) * PMO64_EMIT_ROUND);
+    uint32_t *ncv = malloc(sizeof(uint32_t) * PMO64_EMIT_ROUND);
+    if (!a || !b || !c || !e || !ncs || !ncv) {
+        free(a); free(b); free(c); free(e); free(ncs); free(ncv);
+        return -1;
+    }
     uint32_t targets[2] = {cfg->surface_photons, cfg->volume_photons};
     uint32_t n[2] = {0, 0}, np[2] = {0, 0};
     int done[2] = {targets[0] == 0, targets[1] == 0};
     uint32_t tmax = targets[0] > targets[1] ? targets[0] : targets[1];
     uint64_t cap = cfg->max_paths ? cfg->max_paths : (uint64_t)tmax * 16u;
     if (cap < 1024) cap = 1024;
-    for (uint32_t id = 0; id < cap && !(done[0] && done[1]); ++id) {
-        uint32_t cs, cv;
-        trace_path(scene, cfg, het, id, a, b, &cs, c, e, &cv);
-        uint32_t cnt[2] = {cs, cv};
-        double *sp[2] = {a, c}, *sw[2] = {b, e}, *dp[2] = {spos, vpos}, *dw[2] = {spow, vpow};
-        for (int m = 0; m < 2; ++m) {
-            if (done[m]) continue;
-            np[m] = id + 1;
-            for (uint32_t k = 0; k < cnt[m] && n[m] < targets[m]; ++k) {
-                memcpy(dp[m] + 4 * n[m], sp[m] + 4 * k, sizeof(double) * 4);
-                memcpy(dw[m] + 6 * n[m], sw[m] + 6 * k, sizeof(double) * 6);
-                dp[m][4 * n[m] + 3] = n[m];
-                n[m]++;
+    for (uint64_t base = 0; base < cap && !(done[0] && done[1]); base += PMO64_EMIT_ROUND) {
+        const uint32_t m = cap - base < PMO64_EMIT_ROUND ? (uint32_t)(cap - base) : PMO64_EMIT_ROUND;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long j = 0; j < (long)m; ++j)
+            trace_path(scene, cfg, het, (uint32_t)(base + (uint64_t)j), a + (size_t)j * mb * 4,
+                       b + (size_t)j * mb * 6, &ncs[j], c + (size_t)j * mb * 4, e + (size_t)j * mb * 6,
+                       &ncv[j]);
+        for (uint32_t j = 0; j < m && !(done[0] && done[1]); ++j) {
+            const uint32_t id = (uint32_t)(base + j);
+            uint32_t cnt[2] = {ncs[j], ncv[j]};
+            double *sp[2] = {a + (size_t)j * mb * 4, c + (size_t)j * mb * 4};
+            double *sw[2] = {b + (size_t)j * mb * 6, e + (size_t)j * mb * 6};
+            double *dp[2] = {spos, vpos}, *dw[2] = {spow, vpow};
+            for (int mm = 0; mm < 2; ++mm) {
+                if (done[mm]) continue;
+                np[mm] = id + 1;
+                for (uint32_t k = 0; k < cnt[mm] && n[mm] < targets[mm]; ++k) {
+                    memcpy(dp[mm] + 4 * n[mm], sp[mm] + 4 * k, sizeof(double) * 4);
+                    memcpy(dw[mm] + 6 * n[mm], sw[mm] + 6 * k, sizeof(double) * 6);
+                    dp[mm][4 * n[mm] + 3] = n[mm];
+                    n[mm]++;
+                }
+                if (n[mm] >= targets[mm]) done[mm] = 1;
             }
-            if (n[m] >= targets[m]) done[m] = 1;
         }
     }
-    for (int m = 0; m < 2; ++m) {
-        double *w = m == 0 ? spow : vpow;
-        double scale = (double)scene->light_power / np[m];
-        for (uint32_t i = 0; i < n[m]; ++i) { w[6 * i] *= scale; w[6 * i + 1] *= scale; w[6 * i + 2] *= scale; }
-        sizes[m] = n[m];
-        paths[m] = np[m];
+    for (int mm = 0; mm < 2; ++mm) {
+        double *w = mm == 0 ? spow : vpow;
+        double scale = (double)scene->light_power / np[mm];
+        for (uint32_t i = 0; i < n[mm]; ++i) { w[6 * i] *= scale; w[6 * i + 1] *= scale; w[6 * i + 2] *= scale; }
+        sizes[mm] = n[mm];
+        paths[mm] = np[mm];
     }
-    free(a); free(b); free(c); free(e);
+    free(a); free(b); free(c); free(e); free(ncs); free(ncv);
     return 0;
 }
 
