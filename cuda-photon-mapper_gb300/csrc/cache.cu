@@ -48,7 +48,9 @@ constexpr uint32_t kOffP2 = kOffP1 + kPair;            // H4 | unused
 constexpr uint32_t kOffQ0 = kOffP2 + kPair;            // dZ1 | dZ2
 constexpr uint32_t kOffQ1 = kOffQ0 + kPair;            // dZ3 | dZ4
 constexpr uint32_t kOffGY = kOffQ1 + kPair;            // dL/dy, 128 x 16
-constexpr uint32_t kTrainSmem = kOffGY + 4096;
+constexpr uint32_t kOffXS = kOffGY + 4096;             // next tile's encoded features (staging)
+constexpr uint32_t kXTile = 16384;                     // 128 samples x 64 features bf16
+constexpr uint32_t kTrainSmem = kOffXS + kXTile;
 constexpr uint32_t kPairSbo = 2048;                    // 8-sample groups in a pair buffer
 // Inference: weights + one 128 x 64 activation tile per pipeline.
 constexpr uint32_t kOffAct = kWBytes;
@@ -319,12 +321,33 @@ __device__ __forceinline__ void relu_grad(uint32_t taddr, const unsigned char *h
     }
 }
 
+// The encoded features of samples 0..rows-1 (query sel[i], zero rows from n
+// on) as tile images: tile t = samples 128t..128t+127 in the K-major
+// core-matrix layout with 8-sample groups 1 KB apart (16 KB per tile), the
+// layout the training kernel copies into its first activation buffer. One
+// thread per sample: the 128 hash-table reads of an encoding run at full
+// occupancy here instead of on the tensor-core kernel's critical path.
+__global__ void __launch_bounds__(256)
+    encode_kernel(CacheGrid g, const __half2 *tab, PScene Sc, const float4 *qa, const float4 *qd,
+                  const uint32_t *sel, uint32_t n, uint32_t rows, unsigned char *xt, float *x_out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        const bool valid = i < n;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
+        if (valid) {
+            const uint32_t qi = sel ? sel[i] : i;
+            a = qa[qi];
+            d = qd[qi];
+        }
+        encode_row(xt + (size_t)(i >> 7) * kXTile, kActSbo, (int)(i & 127u), g, tab, Sc, a, d, valid,
+                   (valid && x_out) ? x_out + (size_t)i * 64 : nullptr);
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
-    train_kernel(CacheGrid g, CacheParams p, PScene Sc, const float4 *qa, const float4 *qd,
-                 const uint32_t *sel, const float4 *val, uint32_t n, float inv_scale,
-                 float loss_norm, float rel_eps, float *x_out, float *y_out) {
+    train_kernel(CacheParams p, const unsigned char *xt, const float4 *val, uint32_t n,
+                 float inv_scale, float loss_norm, float rel_eps, float *y_out) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t mbar, wbar;
+    __shared__ __align__(8) uint64_t mbar, wbar, xbar;
     __shared__ uint32_t taddr_s;
     __shared__ int abort_s;
     __shared__ float red[kThreads / 32];
@@ -336,7 +359,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         reinterpret_cast<uint4 *>(sm + kOffP2)[i] = make_uint4(0, 0, 0, 0);
     if (s == 0) {
         mbar_init(&mbar);
+        mbar_init(&xbar);
         abort_s = 0;
+        // the first tile's features into the staging buffer
+        if (blockIdx.x < ntiles) bulk_load(sm + kOffXS, xt + (size_t)blockIdx.x * kXTile, kXTile, &xbar);
     }
     if (warp == 0) tmem_alloc(&taddr_s, kTrainCols);
     publish_smem();
@@ -347,7 +373,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t aP[3] = {base + kOffP0, base + kOffP1, base + kOffP2};
     const uint32_t aQ[2] = {base + kOffQ0, base + kOffQ1};
     const uint32_t aW = base, aGY = base + kOffGY;
-    uint32_t phase = 0;
+    uint32_t phase = 0, xphase = 0;
+    bool xpending = blockIdx.x < ntiles;  // a staging copy in flight
     float lsum = 0.0f;
     bool first = true;
     if (!ok) abort_s = 1;
@@ -357,21 +384,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const uint32_t i = tile * kThreads + s;
         const bool valid = i < n;
-        const uint32_t qi = valid ? (sel ? sel[i] : i) : 0u;
-        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
-        if (valid) {
-            a = qa[qi];
-            d = qd[qi];
+        // this tile's features: staging buffer -> H0 (the first half of
+        // pair P0, whose 8-sample groups are 2 KB apart)
+        ok &= mbar_wait_drain(&xbar, xphase, p.wait_polls);
+        xphase ^= 1u;
+        xpending = false;
+#pragma unroll
+        for (int j = 0; j < (int)(kXTile / 16 / kThreads); ++j) {
+            const uint32_t u = (uint32_t)(j * kThreads + s);
+            *reinterpret_cast<uint4 *>(sm + kOffP0 + (u >> 6) * 2048u + (u & 63u) * 16u) =
+                *reinterpret_cast<const uint4 *>(sm + kOffXS + u * 16u);
         }
-        encode_row(sm + kOffP0, kPairSbo, s, g, p.table_h, Sc, a, d, valid,
-                   (valid && x_out) ? x_out + (size_t)i * 64 : nullptr);
-        // forward, hidden layers: H_{l+1} = relu(H_l W_l)
+        const uint32_t next = tile + gridDim.x;
+        const bool prefetch = next < ntiles;
+        // forward, hidden layers: H_{l+1} = relu(H_l W_l); the first round
+        // also starts the copy of the next tile's features into the staging
+        // buffer, whose reads above the round's barrier have completed
         for (int l = 0; l < 4; ++l) {
             const uint32_t src = aP[l >> 1] + (uint32_t)(l & 1) * 1024u;
             ok &= tc_round(&mbar, phase, p.wait_polls, [&] {
                 mma_chain(taddr, src, 256, 128, kPairSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
                           idesc_bf16(128, 64), false);
+                if (l == 0 && prefetch) bulk_load(sm + kOffXS, xt + (size_t)next * kXTile, kXTile, &xbar);
             });
+            if (l == 0) xpending = prefetch;
             const int o = l + 1;
             relu_out(taddr, sm + kOffP0 + (uint32_t)(o >> 1) * kPair + (uint32_t)(o & 1) * 1024u,
                      kPairSbo, s);
@@ -452,6 +488,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
         }
     }
+    // a staging copy still in flight (the loop stopped early) completes
+    // before the CTA's shared memory is released
+    if (xpending) mbar_wait(&xbar, xphase, kMbarSpin);
     // weight gradients of this CTA -> its row of partial sums (every CTA
     // has at least one tile: the grid is at most the tile count)
     float *part = p.w_part + (size_t)blockIdx.x * kCacheWeights;
@@ -1002,10 +1041,15 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
                                          (int)kTrainSmem);
     if (e != cudaSuccess) return e;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
+    const uint32_t rows = ntiles * kThreads;
+    const uint32_t egrid = std::min<uint32_t>((rows + 255) / 256, (uint32_t)sm_count * 16);
+    encode_kernel<<<egrid, 256, 0, s>>>(g, p.table_h, S, qa, qd, sel, n, rows,
+                                        reinterpret_cast<unsigned char *>(p.xt), x_out);
+    note_launch();
     const uint32_t grid = std::min<uint32_t>(
         ntiles, (uint32_t)std::min(sm_count, p.parts_cap));
-    train_kernel<<<grid, kThreads, kTrainSmem, s>>>(g, p, S, qa, qd, sel, val, n, inv_scale, loss_norm,
-                                                    rel_eps, x_out, y_out);
+    train_kernel<<<grid, kThreads, kTrainSmem, s>>>(p, reinterpret_cast<const unsigned char *>(p.xt), val,
+                                                    n, inv_scale, loss_norm, rel_eps, y_out);
     note_launch();
     wgrad_reduce_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w_part, p.loss_part, (int)grid,
                                                                   p.w_grad, p.loss);
@@ -1064,13 +1108,11 @@ cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &
                                           (int)kInferSmem);
     if (ea != cudaSuccess) return ea;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel,
-                                                                  kThreads * kInferPipes, kInferSmem);
-    if (e != cudaSuccess) return e;
-    per_sm = std::max(per_sm, 1);
+    // one CTA (four pipelines, 16 warps) per SM: two CTAs per SM fit when the
+    // kernel compiles to 64 registers or fewer, but run slower (the table
+    // reads of twice the pipelines compete for the same L1)
     const uint32_t ctas = (ntiles + kInferPipes - 1) / kInferPipes;
-    const uint32_t grid = std::min<uint32_t>(ctas, (uint32_t)sm_count * (uint32_t)per_sm);
+    const uint32_t grid = std::min<uint32_t>(ctas, (uint32_t)sm_count);
     infer_kernel<<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, order, n, out_scale,
                                                                    val);
     note_launch();

@@ -57,7 +57,8 @@ struct CacheParams {
     float *loss;           // device scalar, summed over a step
     float *loss_part;      // per-CTA loss of one backward pass (parts_cap), added to *loss in CTA order
     float4 *dx;            // per-sample gradient of the 32 hash-grid features (8 float4 per sample)
-    uint32_t dx_cap;       // samples dx holds
+    uint4 *xt;             // per-sample encoded features, 128-sample tile images (128 B per sample)
+    uint32_t dx_cap;       // samples dx and xt hold (a multiple of 128)
     int *status;           // set when a bounded tensor-core wait runs out
     uint32_t wait_polls;   // first bound of every mbarrier wait (kMbarSpin unless lowered for a test)
 };

@@ -80,7 +80,7 @@ void free_cache(CacheState *c) {
     cudaFree(c->p.w_part);
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
     cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.loss_part); cudaFree(c->p.status);
-    cudaFree(c->p.w_img); cudaFree(c->p.dx);
+    cudaFree(c->p.w_img); cudaFree(c->p.dx); cudaFree(c->p.xt);
     cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum); cudaFree(c->iorder);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
     cudaFree(c->shist); cudaFree(c->sn);
@@ -145,14 +145,14 @@ void pm_cache_default_config(pm_cache_config *cfg) {
     cfg->base_res = 16;
     cfg->max_res = 2048;
     cfg->train_samples = 1u << 20;
-    cfg->batch = 1u << 18;  // 4 steps per frame, each filling every SM
+    cfg->batch = 1u << 17;  // 8 steps per frame, each filling every SM
     cfg->lr = 5e-2f;
     cfg->beta1 = 0.9f;
     cfg->beta2 = 0.99f;
     cfg->eps = 1e-15f;
-    cfg->lr_min = 1e-3f;
+    cfg->lr_min = 3e-4f;
     cfg->lr_half_life = 300.0f;
-    cfg->loss_eps = 1.0f;
+    cfg->loss_eps = 10.0f;
     cfg->surface_fraction = 0.5f;
     cfg->seed = 0x5EED0004ull;
 }
@@ -205,6 +205,7 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     PM_TRY_FREE(dalloc(&p.loss_part, p.parts_cap));
     p.dx_cap = cfg.batch;
     PM_TRY_FREE(dalloc(&p.dx, (size_t)cfg.batch * 8));
+    PM_TRY_FREE(dalloc(&p.xt, (size_t)cfg.batch * 8));
     PM_TRY_FREE(dalloc(&p.status, 1));
     PM_TRY_FREE(cudaMemset(p.status, 0, sizeof(int)));
     p.wait_polls = kMbarSpin;
@@ -433,6 +434,7 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
     float4 *dqa = nullptr, *dqd = nullptr, *dt = nullptr;
     float *dx = nullptr, *dy = nullptr, *tg = nullptr;
     float4 *ddx = nullptr;
+    uint4 *dxt = nullptr;
     CacheParams dp = c->p;
     std::string where;
 #define PM_DBG(x) do { e = (x); if (e != cudaSuccess) { where = #x; goto done; } } while (0)
@@ -451,9 +453,11 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
     PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(long long) * c->table_floats));
     PM_DBG(cudaMemset(c->p.loss, 0, sizeof(float)));
     // the feature-gradient rows of n samples (n may exceed the batch)
-    PM_DBG(dalloc(&ddx, (size_t)n * 8));
+    PM_DBG(dalloc(&ddx, (size_t)(n + 127) / 128 * 128 * 8));
+    PM_DBG(dalloc(&dxt, (size_t)(n + 127) / 128 * 128 * 8));
     dp.dx = ddx;
-    dp.dx_cap = n;
+    dp.xt = dxt;
+    dp.dx_cap = (n + 127) / 128 * 128;
     PM_DBG(cache_backward(c->grid, dp, st->dscene, dqa, dqd, nullptr, dt, n, 1.0f / target_scale,
                           n ? 1.0f / (3.0f * (float)n) : 0.0f, c->cfg.loss_eps, dx, dy, c->sm_count,
                           0));
@@ -472,7 +476,7 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
     PM_DBG(cudaMemset(c->p.table_grad, 0, sizeof(long long) * c->table_floats));
 done:
 #undef PM_DBG
-    cudaFree(dqa); cudaFree(dqd); cudaFree(dt); cudaFree(dx); cudaFree(dy); cudaFree(tg); cudaFree(ddx);
+    cudaFree(dqa); cudaFree(dqd); cudaFree(dt); cudaFree(dx); cudaFree(dy); cudaFree(tg); cudaFree(ddx); cudaFree(dxt);
     if (e != cudaSuccess) return check_cuda(ctx, e, where.c_str());
     return PM_OK;
 }
