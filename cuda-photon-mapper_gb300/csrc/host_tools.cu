@@ -5,6 +5,7 @@
 #include "pm_ctx.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -262,6 +263,99 @@ pm_status pm_viewer_display(pm_viewer *v, uchar4 *pos) {
     if (cudaDeviceSynchronize() != cudaSuccess) {
         cudaGetLastError();
         return PM_ERR_CUDA;
+    }
+    s.frames++;
+    if (s.anim_flag) s.anim_time += s.anim_inc;
+    return PM_OK;
+}
+
+// ---- physically based frame driver (the same loop over pm_emit / pm_build /
+// pm_render, with temporal reuse) -------------------------------------------
+
+struct pm_phys_viewer {
+    pm_phys_viewer_state s;
+    pm_ctx *ctx;
+    pm_scene base;       // the scene as installed; animation moves sphere 0 from here
+    pm_scene current;    // the scene of the last emission
+    bool have_maps;
+};
+
+pm_status pm_phys_viewer_create(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg,
+                                pm_phys_viewer **out) {
+    if (!ctx || !scene || !cfg || !out) return PM_ERR_INVALID;
+    pm_status st = pm_set_scene(ctx, scene, cfg);
+    if (st != PM_OK) return st;
+    pm_phys_viewer *v = new pm_phys_viewer();
+    memset(&v->s, 0, sizeof(v->s));
+    v->s.anim_flag = 0;
+    v->s.emit_flag = 0;  // an unchanged scene gives the same maps: reuse them
+    v->s.use_cache = 1;
+    v->s.cache_frames = 1;
+    v->s.anim_time = 0.0f;
+    v->s.anim_inc = 0.1f;
+    v->s.anim_radius = 0.05f;
+    v->ctx = ctx;
+    v->base = *scene;
+    v->current = *scene;
+    v->have_maps = false;
+    *out = v;
+    return PM_OK;
+}
+
+void pm_phys_viewer_destroy(pm_phys_viewer *v) { delete v; }
+
+void pm_phys_viewer_key(pm_phys_viewer *v, unsigned char key) {
+    if (!v) return;
+    pm_phys_viewer_state &s = v->s;
+    switch (key) {
+        case 27: s.quit = 1; break;
+        case 'a': case 'A': s.anim_flag = s.anim_flag ? 0 : 1; break;
+        case 'e': case 'E': s.emit_flag = s.emit_flag ? 0 : 1; break;
+        case 'c': case 'C': s.use_cache = s.use_cache ? 0 : 1; break;
+        case '-': s.anim_inc = (float)((double)s.anim_inc - 0.01); break;
+        case '+': s.anim_inc = (float)((double)s.anim_inc + 0.01); break;
+        case 'r': s.anim_inc = 0.01f; break;
+        default: break;
+    }
+}
+
+pm_status pm_phys_viewer_state_get(const pm_phys_viewer *v, pm_phys_viewer_state *out) {
+    if (!v || !out) return PM_ERR_INVALID;
+    *out = v->s;
+    return PM_OK;
+}
+
+pm_status pm_phys_viewer_display(pm_phys_viewer *v, float4 *radiance, uchar4 *rgba,
+                                 cudaStream_t stream) {
+    if (!v) return PM_ERR_INVALID;
+    pm_phys_viewer_state &s = v->s;
+    pm_status st;
+    // the frame's scene: sphere 0 displaced along x by anim_radius *
+    // sin(anim_time), kept inside the box
+    pm_scene sc = v->base;
+    if (sc.num_spheres > 0 && s.anim_time != 0.0f) {
+        float4 &p = sc.spheres[0];
+        const float lo = sc.box_min[0] + p.w, hi = sc.box_max[0] - p.w;
+        p.x = fminf(fmaxf(p.x + s.anim_radius * sinf(s.anim_time), lo), hi);
+    }
+    const bool changed = memcmp(&sc, &v->current, sizeof(sc)) != 0;
+    if (changed && (st = pm_update_scene(v->ctx, &sc)) != PM_OK) return st;
+    if (!v->have_maps || changed || s.emit_flag) {
+        if ((st = pm_emit(v->ctx, stream)) != PM_OK) return st;
+        if ((st = pm_build(v->ctx, stream)) != PM_OK) return st;
+        v->current = sc;
+        v->have_maps = true;
+        s.emissions++;
+    } else {
+        s.reuses++;
+    }
+    const bool cached = s.use_cache && v->ctx->cache != nullptr;
+    if (cached) {
+        if (s.cache_frames > 0 && (st = pm_cache_train(v->ctx, s.cache_frames, stream)) != PM_OK) return st;
+        if ((st = pm_render_cached(v->ctx, radiance, rgba, 0, stream)) != PM_OK) return st;
+        s.cached_frames++;
+    } else if ((st = pm_render(v->ctx, radiance, rgba, stream)) != PM_OK) {
+        return st;
     }
     s.frames++;
     if (s.anim_flag) s.anim_time += s.anim_inc;

@@ -76,6 +76,14 @@ class ViewerState(_c.Structure):
                 ("anim_inc", _c.c_float), ("frames", _c.c_ulonglong)]
 
 
+class PhysViewerState(_c.Structure):
+    _fields_ = [("anim_flag", _c.c_int), ("emit_flag", _c.c_int), ("use_cache", _c.c_int),
+                ("cache_frames", _c.c_int), ("anim_time", _c.c_float), ("anim_inc", _c.c_float),
+                ("anim_radius", _c.c_float), ("quit", _c.c_int), ("frames", _c.c_ulonglong),
+                ("emissions", _c.c_ulonglong), ("reuses", _c.c_ulonglong),
+                ("cached_frames", _c.c_ulonglong)]
+
+
 class CacheConfig(_c.Structure):
     _fields_ = [("levels", _c.c_int), ("log2_table", _c.c_int), ("base_res", _c.c_int),
                 ("max_res", _c.c_int), ("train_samples", _c.c_uint32), ("batch", _c.c_uint32),
@@ -154,6 +162,11 @@ PROTOTYPES = {
     "pm_viewer_key": (None, [_vp, _c.c_ubyte]),
     "pm_viewer_state_get": (_i, [_vp, _c.POINTER(ViewerState)]),
     "pm_viewer_display": (_i, [_vp, _vp]),
+    "pm_phys_viewer_create": (_i, [_vp, _c.POINTER(Scene), _c.POINTER(Config), _c.POINTER(_vp)]),
+    "pm_phys_viewer_destroy": (None, [_vp]),
+    "pm_phys_viewer_key": (None, [_vp, _c.c_ubyte]),
+    "pm_phys_viewer_state_get": (_i, [_vp, _c.POINTER(PhysViewerState)]),
+    "pm_phys_viewer_display": (_i, [_vp, _vp, _vp, _vp]),
     "pm_cache_default_config": (None, [_c.POINTER(CacheConfig)]),
     "pm_cache_enable": (_i, [_vp, _c.POINTER(CacheConfig)]),
     "pm_cache_disable": (_i, [_vp]),
@@ -481,6 +494,40 @@ class Viewer:
             self.close()
         except Exception:
             pass
+
+
+class PhysViewer:
+    """pm_phys_viewer: the frame loop over a context's physically based
+    pipeline with temporal reuse of the maps, trees and cache."""
+
+    def __init__(self, ctx, scene, cfg):
+        self.lib = load()
+        self.ctx = ctx
+        h = _c.c_void_p()
+        ctx._check(self.lib.pm_phys_viewer_create(ctx.h, _c.byref(scene), _c.byref(cfg),
+                                                  _c.byref(h)), "pm_phys_viewer_create")
+        self.h = h
+
+    def key(self, k):
+        self.lib.pm_phys_viewer_key(self.h, ord(k) if isinstance(k, str) else k)
+
+    def state(self):
+        st = PhysViewerState()
+        self.ctx._check(self.lib.pm_phys_viewer_state_get(self.h, _c.byref(st)),
+                        "pm_phys_viewer_state_get")
+        return st
+
+    def display(self, radiance=None, rgba=None, stream=0):
+        self.ctx._check(self.lib.pm_phys_viewer_display(self.h, radiance, rgba, stream),
+                        "pm_phys_viewer_display")
+
+    def close(self):
+        if self.h:
+            self.lib.pm_phys_viewer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def batch_scene(index, seed=0x5EED0005):

@@ -325,6 +325,36 @@ PM_API void pm_viewer_key(pm_viewer *v, unsigned char key);
 PM_API pm_status pm_viewer_state_get(const pm_viewer *v, pm_viewer_state *out);
 PM_API pm_status pm_viewer_display(pm_viewer *v, uchar4 *pos);
 
+/* Physically based frame driver: the reference's frame loop
+ * (callbacksPBO.cpp:47-101) over pm_emit / pm_build / pm_render, with
+ * temporal reuse. pm_phys_viewer_create installs the scene (pm_set_scene) on
+ * ctx. Each display: with anim_flag set, sphere 0 moves to x + anim_radius *
+ * sin(anim_time) (clamped inside the box; pm_update_scene); the photon maps
+ * are re-emitted and their kd-trees rebuilt only when the scene changed
+ * since the last emission, emit_flag is set, or no maps exist yet -- an
+ * unchanged scene gives the same maps, so they are reused; with use_cache
+ * set and the radiance cache enabled (pm_cache_enable) the network takes
+ * cache_frames online training frames on the current maps and renders the
+ * frame (pm_render_cached; the network carries over from frame to frame),
+ * else pm_render; anim_time then advances by anim_inc when anim_flag is set.
+ * Keys as the reference's keyboard() (callbacksPBO.cpp:104-143): 'a'
+ * animation, 'e' re-emission every frame, '+' / '-' / 'r' anim_inc, 27 quit;
+ * plus 'c' for the cache. The context must outlive the driver. */
+typedef struct pm_phys_viewer pm_phys_viewer;
+typedef struct pm_phys_viewer_state {
+    int anim_flag, emit_flag, use_cache, cache_frames;
+    float anim_time, anim_inc, anim_radius;
+    int quit;
+    unsigned long long frames, emissions, reuses, cached_frames;
+} pm_phys_viewer_state;
+PM_API pm_status pm_phys_viewer_create(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg,
+                                       pm_phys_viewer **out);
+PM_API void pm_phys_viewer_destroy(pm_phys_viewer *v);
+PM_API void pm_phys_viewer_key(pm_phys_viewer *v, unsigned char key);
+PM_API pm_status pm_phys_viewer_state_get(const pm_phys_viewer *v, pm_phys_viewer_state *out);
+PM_API pm_status pm_phys_viewer_display(pm_phys_viewer *v, float4 *radiance, uchar4 *rgba,
+                                        cudaStream_t stream);
+
 /* ---- 6. learned radiance cache ------------------------------------------------
  * No counterpart in the reference, whose render always gathers photons. A
  * frame is split into radiance queries -- every volume march sample and the
