@@ -37,6 +37,8 @@ struct PScene {
     float sigma_s, sigma_a, g;
     int het_res;
     float sigma_max;                 // majorant of sigma_t
+    float inv_sigma_max;             // 1 / sigma_max (0 without a medium)
+    float het_scale[3];              // het_res / box extent per axis (grid cells per unit length)
     const float *het;                // het_res^3 sigma_s values (device)
     float cam[3], focal;
     // Uniform grid over the box for the sphere tests (grid_res = 0: none):
@@ -56,12 +58,15 @@ constexpr int kNone = 0x7fffffff;
 PM_HD float vget(v3 v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
 // Distance to the first crossing of sphere s beyond kRayEps along (o, d),
-// or -1 when the line misses it.
+// or -1 when the line misses it. The quadratic's terms are fused
+// multiply-adds (one rounding each; the oracle writes the same fmaf calls):
+// the photon tracer spends most of its floating-point instructions in this
+// test, over every sphere at every event.
 __device__ __forceinline__ float sphere_t(float4 s, v3 o, v3 d) {
-    v3 oc = mk3(o.x - s.x, o.y - s.y, o.z - s.z);
-    float b = dot(oc, d);
-    float c = dot(oc, oc) - s.w * s.w;
-    float disc = b * b - c;
+    const float ox = o.x - s.x, oy = o.y - s.y, oz = o.z - s.z;
+    const float b = __fmaf_rn(oz, d.z, __fmaf_rn(oy, d.y, ox * d.x));
+    const float c = __fmaf_rn(oz, oz, __fmaf_rn(oy, oy, __fmaf_rn(ox, ox, -(s.w * s.w))));
+    const float disc = __fmaf_rn(b, b, -c);
     if (!(disc > 0.0f)) return -1.0f;
     float sq = sqrtf(disc);
     float t = -b - sq;
@@ -228,7 +233,7 @@ __device__ __forceinline__ float sigma_s_at(const PScene &S, v3 x) {
     int r = S.het_res;
     int i[3];
     for (int a = 0; a < 3; ++a) {
-        float f = (vget(x, a) - S.bmin[a]) / (S.bmax[a] - S.bmin[a]) * (float)r;
+        float f = (vget(x, a) - S.bmin[a]) * S.het_scale[a];
         int q = (int)f;
         i[a] = q < 0 ? 0 : (q >= r ? r - 1 : q);
     }

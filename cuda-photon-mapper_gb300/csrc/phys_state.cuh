@@ -43,7 +43,10 @@ struct PhysicalState {
     uint32_t *cnt[2] = {nullptr, nullptr};  // records per path, per map
     uint32_t *off[2] = {nullptr, nullptr};  // exclusive scans of cnt
     uint32_t *scan_tmp = nullptr;
-    uint32_t *words = nullptr;  // [0] path counter [1] stored_s [2] stored_v [3] total [4..7] extents
+    // the writing pass's work: ids of the paths holding a record of a map,
+    // in increasing order, and the per-tile counts and offsets that place them
+    uint32_t *need_list = nullptr, *need_tile = nullptr, *need_tile_off = nullptr;
+    uint32_t *words = nullptr;  // [0] path counter [1] stored_s [2] stored_v [3] total [4..7] extents [8] needed paths
     struct Map {
         float4 *pos = nullptr, *pow = nullptr, *tpos = nullptr, *tpow = nullptr;
         float4 *tdir = nullptr;  // decoded directions in tree order
@@ -96,7 +99,8 @@ void query_list_free(QueryList &ql);
 cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s);
 constexpr int kGatherStats = 7;
 // Scratch of knn_values_tiles: anchor_d[tile_chunks(n, groups)], defer[n],
-// one defer_n word; stats: kGatherStats counters added (nullable).
+// two defer_n words (deferred count, chunk counter); stats: kGatherStats
+// counters added (nullable).
 struct TileBuffers {
     float *anchor_d;
     uint32_t *defer;

@@ -33,6 +33,7 @@ void free_state(PhysicalState *st) {
     for (auto &p : st->cnt) cudaFree(p);
     for (auto &p : st->off) cudaFree(p);
     cudaFree(st->scan_tmp);
+    cudaFree(st->need_list); cudaFree(st->need_tile); cudaFree(st->need_tile_off);
     cudaFree(st->words);
     for (auto &m : st->map) {
         cudaFree(m.pos); cudaFree(m.pow); cudaFree(m.tpos); cudaFree(m.tpow); cudaFree(m.tdir);
@@ -90,6 +91,9 @@ pm_status pm_set_scene(pm_ctx *ctx, const pm_scene *scene, const pm_config *cfg)
     for (auto &p : st->cnt) PM_TRY(dalloc(&p, st->path_cap));
     for (auto &p : st->off) PM_TRY(dalloc(&p, st->path_cap));
     PM_TRY(dalloc(&st->scan_tmp, scan_tile_count(st->path_cap) + 1));
+    PM_TRY(dalloc(&st->need_list, st->path_cap));
+    PM_TRY(dalloc(&st->need_tile, needed_tiles(st->path_cap)));
+    PM_TRY(dalloc(&st->need_tile_off, needed_tiles(st->path_cap)));
     PM_TRY(dalloc(&st->words, 16));
     PM_TRY(cudaMemset(st->words, 0, 16 * sizeof(uint32_t)));
     const uint32_t targets[2] = {cfg->surface_photons, cfg->volume_photons};
@@ -184,9 +188,13 @@ pm_status pm_emit(pm_ctx *ctx, cudaStream_t stream) {
         PM_TRY(map_extent(issued, st->cnt[m], st->off[m], st->words + 3, st->scan_tmp, target,
                           st->words + 4 + 2 * m, stream));
     }
-    // writing pass over the paths the maps need
+    // writing pass over the paths the maps need, taken from their list
+    PM_TRY(needed_paths(issued, st->cnt[0], st->cnt[1], st->words + 4, st->words + 6, st->need_tile,
+                        st->need_tile_off, st->scan_tmp, st->need_list, st->words + 8, stream));
     PM_TRY(cudaMemsetAsync(st->words, 0, sizeof(uint32_t), stream));
     P.store = 1;
+    P.list = st->need_list;
+    P.list_n = st->words + 8;
     P.off_s = st->off[0];
     P.off_v = st->off[1];
     P.ext_s = st->words + 4;

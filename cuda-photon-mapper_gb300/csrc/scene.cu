@@ -249,6 +249,9 @@ PScene to_device_scene(const pm_scene &s, const float *het_dev) {
     d.het_res = s.het_res;
     d.het = het_dev;
     d.sigma_max = (s.het_res > 0 ? s.het_max : s.sigma_s) + s.sigma_a;
+    d.inv_sigma_max = d.sigma_max > 0.0f ? 1.0f / d.sigma_max : 0.0f;
+    for (int a = 0; a < 3; ++a)
+        d.het_scale[a] = s.het_res > 0 ? (float)s.het_res / (s.box_max[a] - s.box_min[a]) : 0.0f;
     d.focal = s.focal;
     // Sphere grid for scenes with many spheres, all inside the box (the
     // walk only visits the box): G = ceil(1.5 * cbrt(n)) cells per axis,

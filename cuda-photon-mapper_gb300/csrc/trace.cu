@@ -12,10 +12,12 @@
 // Two passes over the same deterministic paths: the counting pass stores
 // nothing and stops issuing paths once both maps are full; a scan of the
 // per-path counts then fixes every record's final index (records in path
-// order, cut at the map's target), and the writing pass retraces exactly
-// the paths the maps need and writes each record straight into the SoA
-// float4 map arrays, its power scaled by the number of paths the map drew
-// from. No per-path staging memory, no compaction copy.
+// order, cut at the map's target), a compaction lists the ids of the paths
+// the maps need (those with a record below a map's extent: about a tenth of
+// the issued paths when one map fills much later than the other), and the
+// writing pass retraces exactly those and writes each record straight into
+// the SoA float4 map arrays, its power scaled by the number of paths the map
+// drew from. No per-path staging memory, no compaction of records.
 #include "launch_count.cuh"
 #include "trace.cuh"
 #include "radix_sort.cuh"
@@ -90,16 +92,20 @@ __device__ bool step_path(const PScene &S, const TraceParams &P, Path &p, const 
                 }
             }
         } else {
-            // Delta tracking against the majorant (Woodcock et al. 1965).
+            // Delta tracking against the majorant (Woodcock et al. 1965):
+            // tentative collision j draws its distance and acceptance from
+            // words 2(j % 2), 2(j % 2) + 1 of Philox block 1 + j / 2.
             float t = 0.0f;
+            pm_u32x4 q;
             for (uint32_t j = 0; j < kMaxDeltaSteps; ++j) {
-                pm_u32x4 q = philox(P.seed, p.id, (uint32_t)p.ev, 1u + j, P.scene_id);
-                t += -pm_logf(1.0f - pm_u01(q.v[0])) / S.sigma_max;
+                if ((j & 1u) == 0u) q = philox(P.seed, p.id, (uint32_t)p.ev, 1u + (j >> 1), P.scene_id);
+                const uint32_t ua = (j & 1u) ? q.v[2] : q.v[0], ub = (j & 1u) ? q.v[3] : q.v[1];
+                t += -pm_logf(1.0f - pm_u01(ua)) * S.inv_sigma_max;
                 if (!(t < seg)) break;
                 v3 y = p.o + p.d * t;
                 float s = sigma_s_at(S, y);
                 float sty = s + S.sigma_a;
-                if (pm_u01(q.v[1]) * S.sigma_max < sty) {
+                if (pm_u01(ub) * S.sigma_max < sty) {
                     vol = true;
                     x = y;
                     ss = s;
@@ -182,7 +188,7 @@ __device__ __forceinline__ void trace_loop(const PScene &S, const TraceParams &P
         mv.n = P.ext_v[0]; mv.paths = P.ext_v[1];
         ms.scale = ms.paths ? P.power / (float)ms.paths : 0.0f;
         mv.scale = mv.paths ? P.power / (float)mv.paths : 0.0f;
-        cap = max(ms.paths, mv.paths);
+        cap = P.list ? *P.list_n : max(ms.paths, mv.paths);
     }
     Path p;
     bool live = false;
@@ -227,11 +233,17 @@ __device__ __forceinline__ void trace_loop(const PScene &S, const TraceParams &P
                 pool += min(need, avail);
             }
             if (!live && id < cap) {
-                // the writing pass retraces only paths with a record in a map
-                const bool needed = !P.store || (id < ms.paths && P.cnt_s[id] > 0u) ||
-                                    (id < mv.paths && P.cnt_v[id] > 0u);
+                // the writing pass retraces only paths with a record in a map:
+                // those of its list, or (without a list) the ids whose counts
+                // are nonzero
+                uint32_t pid = id;
+                bool needed = true;
+                if (P.store) {
+                    if (P.list) pid = P.list[id];
+                    else needed = (id < ms.paths && P.cnt_s[id] > 0u) || (id < mv.paths && P.cnt_v[id] > 0u);
+                }
                 if (needed) {
-                    start_path(P, id, p, S);
+                    start_path(P, pid, p, S);
                     live = true;
                 }
             }
@@ -305,7 +317,73 @@ __global__ void map_extent_kernel(const uint32_t *off, const uint32_t *cnt, uint
     extent[1] = lo + 1;
 }
 
+constexpr uint32_t kNeedTile = 1024;
+
+__device__ __forceinline__ bool path_needed(uint32_t id, const uint32_t *cnt_s, const uint32_t *cnt_v,
+                                            uint32_t ps, uint32_t pv) {
+    return (id < ps && cnt_s[id] > 0u) || (id < pv && cnt_v[id] > 0u);
+}
+
+// Needed paths per tile of kNeedTile ids.
+__global__ void __launch_bounds__(kNeedTile) need_count_kernel(uint32_t issued, const uint32_t *cnt_s,
+                                                               const uint32_t *cnt_v, const uint32_t *ext_s,
+                                                               const uint32_t *ext_v, uint32_t *tile_cnt) {
+    __shared__ uint32_t warp_n[kNeedTile / 32];
+    const uint32_t id = blockIdx.x * kNeedTile + threadIdx.x;
+    const bool need = id < issued && path_needed(id, cnt_s, cnt_v, ext_s[1], ext_v[1]);
+    const uint32_t b = __popc(__ballot_sync(0xffffffffu, need));
+    if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = b;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const uint32_t v = __reduce_add_sync(0xffffffffu, warp_n[threadIdx.x]);
+        if (threadIdx.x == 0) tile_cnt[blockIdx.x] = v;
+    }
+}
+
+// Each tile's needed ids, in order, at the tile's offset.
+__global__ void __launch_bounds__(kNeedTile) need_scatter_kernel(uint32_t issued, const uint32_t *cnt_s,
+                                                                 const uint32_t *cnt_v, const uint32_t *ext_s,
+                                                                 const uint32_t *ext_v, const uint32_t *tile_off,
+                                                                 uint32_t *list) {
+    __shared__ uint32_t warp_off[kNeedTile / 32];
+    const uint32_t id = blockIdx.x * kNeedTile + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool need = id < issued && path_needed(id, cnt_s, cnt_v, ext_s[1], ext_v[1]);
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (lane == 0) warp_off[warp] = __popc(m);
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of the 32 warp counts
+        const uint32_t v = warp_off[lane];
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        warp_off[lane] = x - v;
+    }
+    __syncthreads();
+    if (need) list[tile_off[blockIdx.x] + warp_off[warp] + __popc(m & ((1u << lane) - 1u))] = id;
+}
+
 }  // namespace
+
+uint32_t needed_tiles(uint32_t n) { return (n + kNeedTile - 1) / kNeedTile + 1; }
+
+cudaError_t needed_paths(uint32_t issued, const uint32_t *cnt_s, const uint32_t *cnt_v,
+                         const uint32_t *ext_s, const uint32_t *ext_v, uint32_t *tile_cnt,
+                         uint32_t *tile_off, uint32_t *scan_tmp, uint32_t *list, uint32_t *list_n,
+                         cudaStream_t s) {
+    if (issued == 0) return cudaMemsetAsync(list_n, 0, sizeof(uint32_t), s);
+    const uint32_t tiles = (issued + kNeedTile - 1) / kNeedTile;
+    need_count_kernel<<<tiles, kNeedTile, 0, s>>>(issued, cnt_s, cnt_v, ext_s, ext_v, tile_cnt);
+    note_launch();
+    cudaError_t e = exclusive_scan_u32_large(tile_cnt, tile_off, tiles, list_n, scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    need_scatter_kernel<<<tiles, kNeedTile, 0, s>>>(issued, cnt_s, cnt_v, ext_s, ext_v, tile_off, list);
+    note_launch();
+    return cudaGetLastError();
+}
 
 cudaError_t trace_photons(const PScene &S, const TraceParams &P, int sm_count, cudaStream_t s) {
     // 4 warps per CTA, enough CTAs to fill every SM several times over.

@@ -26,6 +26,10 @@ struct TraceParams {
     const uint32_t *ext_s, *ext_v;
     float power;
     float4 *spos, *spow, *vpos, *vpow;
+    // Writing pass with a list (nullable): the paths to trace are
+    // list[0 .. *list_n), instead of every id below the extents whose
+    // counts are nonzero.
+    const uint32_t *list, *list_n;
 };
 
 // One persistent launch over the photon paths (counting or writing pass).
@@ -41,6 +45,16 @@ cudaError_t map_extent(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint
 cudaError_t map_extent_dev(uint32_t cap, const uint32_t *issued_dev, const uint32_t *cnt,
                            uint32_t *off, uint32_t *total, uint32_t *scan_tmp, uint32_t target,
                            uint32_t *extent, cudaStream_t s);
+// The ids below `issued` of the paths that hold a record of a map (id <
+// ext_s[1] with cnt_s > 0, or id < ext_v[1] with cnt_v > 0), in increasing
+// order, into list[0 .. *list_n): per-tile counts, a scan of them, then each
+// tile's ids placed at its offset. tile_cnt / tile_off hold
+// needed_tiles(issued) words; scan_tmp as exclusive_scan_u32_large's.
+uint32_t needed_tiles(uint32_t n);
+cudaError_t needed_paths(uint32_t issued, const uint32_t *cnt_s, const uint32_t *cnt_v,
+                         const uint32_t *ext_s, const uint32_t *ext_v, uint32_t *tile_cnt,
+                         uint32_t *tile_off, uint32_t *scan_tmp, uint32_t *list, uint32_t *list_n,
+                         cudaStream_t s);
 // One persistent launch over the paths of n scenes (scenes and params are
 // device arrays; each scene's params carry its own counters and maps).
 cudaError_t trace_photons_batch(const PScene *scenes, const TraceParams *params, int n,

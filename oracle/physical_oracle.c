@@ -47,7 +47,7 @@ static void vset(v3 *v, int a, float s) { if (a == 0) v->x = s; else if (a == 1)
 typedef struct {
     const pmo_scene *s;
     const float *het;
-    float sigma_max;
+    float sigma_max, inv_sigma_max, het_scale[3];
 } scn;
 
 static scn make_scn(const pmo_scene *s, const float *het) {
@@ -55,6 +55,9 @@ static scn make_scn(const pmo_scene *s, const float *het) {
     c.s = s;
     c.het = het;
     c.sigma_max = (s->het_res > 0 ? s->het_max : s->sigma_s) + s->sigma_a;
+    c.inv_sigma_max = c.sigma_max > 0.0f ? 1.0f / c.sigma_max : 0.0f;
+    for (int a = 0; a < 3; ++a)
+        c.het_scale[a] = s->het_res > 0 ? (float)s->het_res / (s->box_max[a] - s->box_min[a]) : 0.0f;
     return c;
 }
 
@@ -68,10 +71,11 @@ static hitr intersect(const scn *S, v3 o, v3 d, float tmax) {
     h.obj = NONE;
     for (int i = 0; i < s->num_spheres; ++i) {
         const float *sp = s->spheres[i];
-        v3 oc = mk(o.x - sp[0], o.y - sp[1], o.z - sp[2]);
-        float b = dot3(oc, d);
-        float c = dot3(oc, oc) - sp[3] * sp[3];
-        float disc = b * b - c;
+        /* the GPU's sphere_t (phys_common.cuh): the same fused multiply-adds */
+        const float ox = o.x - sp[0], oy = o.y - sp[1], oz = o.z - sp[2];
+        float b = fmaf(oz, d.z, fmaf(oy, d.y, ox * d.x));
+        float c = fmaf(oz, oz, fmaf(oy, oy, fmaf(ox, ox, -(sp[3] * sp[3]))));
+        float disc = fmaf(b, b, -c);
         if (disc > 0.0f) {
             float sq = sqrtf(disc);
             float t = -b - sq;
@@ -145,7 +149,7 @@ static float sigma_s_at(const scn *S, v3 x) {
     if (s->het_res <= 0) return s->sigma_s;
     int r = s->het_res, i[3];
     for (int a = 0; a < 3; ++a) {
-        float f = (vget(x, a) - s->box_min[a]) / (s->box_max[a] - s->box_min[a]) * (float)r;
+        float f = (vget(x, a) - s->box_min[a]) * S->het_scale[a];
         int q = (int)f;
         i[a] = q < 0 ? 0 : (q >= r ? r - 1 : q);
     }
@@ -295,14 +299,17 @@ void pmo_trace_path(const pmo_scene *scene, const pmo_config *cfg, const float *
                 }
             } else {
                 float t = 0.0f;
+                pm_u32x4 q;
                 for (uint32_t j = 0; j < MAX_DELTA_STEPS; ++j) {
-                    pm_u32x4 q = philox(cfg->seed, id, (uint32_t)ev, 1u + j, cfg->scene_id);
-                    t += -pm_logf(1.0f - pm_u01(q.v[0])) / S.sigma_max;
+                    /* two tentative collisions per Philox block (GPU: trace.cu step_path) */
+                    if ((j & 1u) == 0u) q = philox(cfg->seed, id, (uint32_t)ev, 1u + (j >> 1), cfg->scene_id);
+                    const uint32_t ua = (j & 1u) ? q.v[2] : q.v[0], ub = (j & 1u) ? q.v[3] : q.v[1];
+                    t += -pm_logf(1.0f - pm_u01(ua)) * S.inv_sigma_max;
                     if (!(t < seg)) break;
                     v3 y = add(o, scl(d, t));
                     float sv = sigma_s_at(&S, y);
                     float sty = sv + s->sigma_a;
-                    if (pm_u01(q.v[1]) * S.sigma_max < sty) { vol = 1; x = y; ss = sv; st = sty; break; }
+                    if (pm_u01(ub) * S.sigma_max < sty) { vol = 1; x = y; ss = sv; st = sty; break; }
                 }
             }
         }

@@ -207,13 +207,16 @@ static void trace_path(const pmo_scene *s, const pmo_config *cfg, const float *h
                 }
             } else {
                 double t = 0.0;
+                pm_u32x4 q;
                 for (uint32_t j = 0; j < 4096u; ++j) {
-                    pm_u32x4 q = philox(cfg->seed, id, (uint32_t)ev, 1u + j, cfg->scene_id);
-                    t += -log(1.0 - u01(q.v[0])) / smax;
+                    /* two tentative collisions per Philox block, as the float32 paths */
+                    if ((j & 1u) == 0u) q = philox(cfg->seed, id, (uint32_t)ev, 1u + (j >> 1), cfg->scene_id);
+                    const uint32_t ua = (j & 1u) ? q.v[2] : q.v[0], ub = (j & 1u) ? q.v[3] : q.v[1];
+                    t += -log(1.0 - u01(ua)) / smax;
                     if (!(t < seg)) break;
                     d3 y = add(o, scl(d, t));
                     double sv = sigma_s_at(s, het, y), sty = sv + s->sigma_a;
-                    if (u01(q.v[1]) * smax < sty) { vol = 1; x = y; ss = sv; st = sty; break; }
+                    if (u01(ub) * smax < sty) { vol = 1; x = y; ss = sv; st = sty; break; }
                 }
             }
         }
