@@ -343,7 +343,7 @@ cudaError_t size_query_buffers(pm_batch *b) {
     Z_TRY(dalloc(&q.ord_tmp, max_q));
     Z_TRY(dalloc(&q.hist, radix_sort_hist_words((uint32_t)max_q)));
     Z_TRY(dalloc(&q.anchor_d, tile_chunks((uint32_t)max_q, 4)));
-    Z_TRY(dalloc(&q.defer_n, 1));
+    Z_TRY(dalloc(&q.defer_n, 2));  // deferred count, chunk counter
     q.q_cap = max_q;
 #undef Z_TRY
     return cudaSuccess;

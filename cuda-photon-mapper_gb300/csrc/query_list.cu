@@ -131,7 +131,7 @@ cudaError_t knn_values_raw(PhysicalState *st, cudaStream_t s) {
     QL_TRY(query_list_sort(st, s));
     if (!ql.gather_stats) {
         QL_TRY(dalloc(&ql.gather_stats, kGatherStats));
-        QL_TRY(dalloc(&ql.defer_n, 1));
+        QL_TRY(dalloc(&ql.defer_n, 2));  // deferred count, chunk counter
     }
     if (tile_chunks(ql.nq, 4) > ql.anchor_cap) {
         cudaFree(ql.anchor_d);

@@ -527,7 +527,8 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
     query_knn_tile_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
                           const uint32_t *order, uint32_t n, const uint32_t *n_dev, int groups,
                           const float *anchor_d, int k, float r2cap, bool raw, float4 *out,
-                          uint32_t *defer_list, uint32_t *defer_n, unsigned long long *stats) {
+                          uint32_t *defer_list, uint32_t *defer_n, uint32_t *chunk_counter,
+                          unsigned long long *stats) {
     const int lane = threadIdx.x & 31;
     if (n_dev) n = min(n, *n_dev);
     if (threadIdx.x == 0) {
@@ -546,10 +547,17 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
     TileScratch &ts = scratch();
     if (lane < kStCount) ts.st[lane] = 0;
     __syncthreads();
-    const uint32_t chunk = blockIdx.x * kTileWarps + (threadIdx.x >> 5);
-    const uint32_t wfirst = chunk * (uint32_t)(32 * groups);
-    if (wfirst >= n) return;
+    const uint32_t nchunks = (n + 32u * (uint32_t)groups - 1u) / (32u * (uint32_t)groups);
     const float rcap = sqrtf(r2cap);
+    // persistent warps: each takes the next chunk from the counter until
+    // none is left, so a block's resources are never held by finished warps
+    // waiting on a slow one
+    for (;;) {
+    uint32_t chunk = 0;
+    if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
+    chunk = __shfl_sync(kFull, chunk, 0);
+    if (chunk >= nchunks) break;
+    const uint32_t wfirst = chunk * (uint32_t)(32 * groups);
     // exact distances known so far (lane j: one point; kd < 0: none): the
     // anchor, later the previous group
     float kx = 0.f, ky = 0.f, kz = 0.f, kd = -1.0f;
@@ -632,6 +640,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
         kz = q.x.z;
         kd = ((members >> lane) & 1u) ? dnew : -1.0f;
     }
+    }  // chunks
     __syncwarp();
     if (stats && lane < kStCount && ts.st[lane]) atomicAdd(&stats[lane], ts.st[lane]);
 }
@@ -695,14 +704,20 @@ cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView
     const dim3 grid((chunks + kTileWarps - 1) / kTileWarps), block(kTileWarps * 32);
     const int smem = (int)(kTileWarps * sizeof(TileScratch));
     const dim3 dgrid(std::max(sm_count, 1) * 8);
-    cudaError_t e = cudaMemsetAsync(buf.defer_n, 0, sizeof(uint32_t), s);
+    // defer_n[0]: deferred queries, defer_n[1]: the chunk counter
+    cudaError_t e = cudaMemsetAsync(buf.defer_n, 0, 2 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
+    int per_sm = 1;
+    // persistent tile launch: as many blocks as fit on the GPU at once
 #define PM_TILE_LAUNCH(SL)                                                                              \
     anchor_kernel<SL><<<grid, block, 0, s>>>(surf, vol, qa, order, n, n_dev, groups, k, r2, buf.anchor_d); \
     e = cudaFuncSetAttribute(query_knn_tile_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
     if (e != cudaSuccess) return e;                                                                     \
-    query_knn_tile_kernel<SL><<<grid, block, smem, s>>>(S, surf, vol, qa, qd, order, n, n_dev, groups, buf.anchor_d, k, \
-                                                        r2, raw, val, buf.defer, buf.defer_n, buf.stats); \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, query_knn_tile_kernel<SL>, kTileWarps * 32, smem); \
+    if (e != cudaSuccess) return e;                                                                     \
+    query_knn_tile_kernel<SL><<<std::min<uint32_t>(grid.x, (uint32_t)std::max(sm_count, 1) * (uint32_t)std::max(per_sm, 1)), \
+                                block, smem, s>>>(S, surf, vol, qa, qd, order, n, n_dev, groups, buf.anchor_d, k, \
+                                                  r2, raw, val, buf.defer, buf.defer_n, buf.defer_n + 1, buf.stats); \
     deferred_kernel<SL><<<dgrid, 128, 0, s>>>(S, surf, vol, qa, qd, buf.defer, buf.defer_n, k, r2, raw, val)
     switch ((k + 31) / 32) {
         case 1: PM_TILE_LAUNCH(1); break;
