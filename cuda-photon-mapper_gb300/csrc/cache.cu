@@ -113,6 +113,17 @@ __device__ bool load_weight_image(unsigned char *sw, const uint4 *img, uint64_t 
     return mbar_wait_drain(mbar, 0, polls);
 }
 
+// A bounded wait of the inference kernel: under a lowered first bound
+// (kLowered) the drain of mbar_wait_drain, else the plain wait under the
+// default bound. Kept apart because the runtime bound and the drain path
+// cost the inference kernel its register allocation (61 instead of 96
+// registers, 18 % slower on preset 2).
+template <bool kLowered>
+__device__ __forceinline__ bool infer_wait(uint64_t *mbar, uint32_t phase, uint32_t polls) {
+    if (kLowered) return mbar_wait_drain(mbar, phase, polls);
+    return mbar_wait(mbar, phase);
+}
+
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 
 // One table-gradient term as a fixed-point integer: the exact product with
@@ -265,7 +276,7 @@ __device__ __forceinline__ bool tc_round(uint64_t *mbar, uint32_t &phase, uint32
 
 // The same for one 128-thread pipeline of a larger CTA: named barrier `bar`
 // instead of the CTA barrier; `issuer` is the pipeline's first thread.
-template <class F>
+template <bool kLowered, class F>
 __device__ __forceinline__ bool tc_round_group(uint64_t *mbar, uint32_t &phase, uint32_t bar,
                                                bool issuer, uint32_t polls, F issue) {
     publish_smem();
@@ -275,7 +286,7 @@ __device__ __forceinline__ bool tc_round_group(uint64_t *mbar, uint32_t &phase, 
         issue();
         mma_commit(mbar);
     }
-    const bool ok = mbar_wait_drain(mbar, phase, polls);
+    const bool ok = infer_wait<kLowered>(mbar, phase, polls);
     phase ^= 1u;
     after_sync();
     return ok;
@@ -541,6 +552,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 constexpr int kInferPipes = 4;
 constexpr uint32_t kInferSmem = kOffAct + 16384u * kInferPipes;
 
+template <bool kLowered>
 __global__ void __launch_bounds__(kThreads * kInferPipes)
     infer_kernel(CacheGrid g, CacheParams p, PScene Sc, const float4 *qa, const float4 *qd,
                  const uint32_t *order, uint32_t n, float out_scale, float4 *val) {
@@ -553,7 +565,12 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
     const uint32_t bar = 1u + (uint32_t)pipe;
     const bool issuer = s == 0;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
-    const bool wok = load_weight_image(sm, p.w_img, &wbar, p.wait_polls);
+    if (threadIdx.x == 0) {
+        mbar_init(&wbar);
+        bulk_load(sm, p.w_img, kWBytes, &wbar);
+    }
+    __syncthreads();
+    const bool wok = infer_wait<kLowered>(&wbar, 0, p.wait_polls);
     if (issuer) {
         mbar_init(&mbar[pipe]);
         abort_s[pipe] = wok ? 0 : 1;
@@ -580,13 +597,13 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
         }
         encode_row(act, kActSbo, s, g, p.table_h, Sc, a, d, valid, nullptr);
         for (int l = 0; l < 4; ++l) {
-            ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, p.wait_polls, [&] {
+            ok &= tc_round_group<kLowered>(&mbar[pipe], phase, bar, issuer, p.wait_polls, [&] {
                 mma_chain(taddr, aA, 256, 128, kActSbo, aW + (uint32_t)l * 8192u, 256, 128, 1024, 4,
                           idesc_bf16(128, 64), false);
             });
             relu_out(taddr, act, kActSbo, s);
         }
-        ok &= tc_round_group(&mbar[pipe], phase, bar, issuer, p.wait_polls, [&] {
+        ok &= tc_round_group<kLowered>(&mbar[pipe], phase, bar, issuer, p.wait_polls, [&] {
             mma_chain(taddr, aA, 256, 128, kActSbo, aW + 32768u, 256, 128, 1024, 4,
                       idesc_bf16(128, 16), false);
         });
@@ -1104,8 +1121,9 @@ cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &
                         const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
                         float out_scale, float4 *val, int sm_count, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    cudaError_t ea = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)kInferSmem);
+    const bool lowered = p.wait_polls != kMbarSpin;
+    cudaError_t ea = cudaFuncSetAttribute(lowered ? infer_kernel<true> : infer_kernel<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
     if (ea != cudaSuccess) return ea;
     const uint32_t ntiles = (n + kThreads - 1) / kThreads;
     // one CTA (four pipelines, 16 warps) per SM: two CTAs per SM fit when the
@@ -1113,8 +1131,12 @@ cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &
     // reads of twice the pipelines compete for the same L1)
     const uint32_t ctas = (ntiles + kInferPipes - 1) / kInferPipes;
     const uint32_t grid = std::min<uint32_t>(ctas, (uint32_t)sm_count);
-    infer_kernel<<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, order, n, out_scale,
-                                                                   val);
+    if (lowered)
+        infer_kernel<true><<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, order, n,
+                                                                             out_scale, val);
+    else
+        infer_kernel<false><<<grid, kThreads * kInferPipes, kInferSmem, s>>>(g, p, S, qa, qd, order, n,
+                                                                              out_scale, val);
     note_launch();
     return cudaGetLastError();
 }

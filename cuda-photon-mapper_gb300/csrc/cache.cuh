@@ -81,11 +81,13 @@ cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *
 // same map (for sparse sorted picks, where shared candidate sets do not
 // pay): diffuse queries e / (pi r^2) / pi, volume queries e / (4/3 pi r^3)
 // with the phase function toward wo; with raw set, e and r^2 (-1 when
-// nothing was found).
+// nothing was found). With run_ctr (one device word, nullable) the launch
+// is persistent: as many warps as fit take runs from the counter.
 cudaError_t cache_knn_values_runs(const PScene &S, const MapView &surf, const MapView &vol,
                                   const float4 *qa, const float4 *qd, const uint32_t *sel,
                                   const uint32_t *order, uint32_t n, int run, int k, float radius,
-                                  bool raw, float4 *val, cudaStream_t s);
+                                  bool raw, float4 *val, uint32_t *run_ctr, int sm_count,
+                                  cudaStream_t s);
 // The render's radiance from raw per-query values (flux sum, squared radius
 // or -1): per pixel, in query order, with exactly the arithmetic of the
 // single-kernel render (transmittance factors from the query records), so

@@ -28,6 +28,7 @@ struct CacheState {
     // targets, and their positions in the random order training reads
     uint32_t *skey = nullptr, *sval = nullptr, *skey_tmp = nullptr, *sval_tmp = nullptr;
     uint32_t *shist = nullptr, *sn = nullptr;
+    uint32_t *run_ctr = nullptr;  // the target launch's run counter
     // the order inference takes the render's queries in
     uint32_t *iorder = nullptr;
     uint32_t iorder_cap = 0;
@@ -62,7 +63,7 @@ cudaError_t pick_and_target(PhysicalState *st, CacheState *c, cudaStream_t strea
                                 stream, &ok_keys, &ok_vals));
     CT_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), st->ql.qa, st->ql.qd,
                                  c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt,
-                                 stream));
+                                 c->run_ctr, c->sm_count, stream));
 #undef CT_TRY
     return cudaSuccess;
 }
@@ -83,7 +84,7 @@ void free_cache(CacheState *c) {
     cudaFree(c->p.w_img); cudaFree(c->p.dx); cudaFree(c->p.xt);
     cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum); cudaFree(c->iorder);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
-    cudaFree(c->shist); cudaFree(c->sn);
+    cudaFree(c->shist); cudaFree(c->sn); cudaFree(c->run_ctr);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->tev0) cudaEventDestroy(c->tev0);
@@ -217,6 +218,7 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     PM_TRY_FREE(dalloc(&c->sval_tmp, cfg.train_samples));
     PM_TRY_FREE(dalloc(&c->shist, radix_sort_hist_words(cfg.train_samples)));
     PM_TRY_FREE(dalloc(&c->sn, 1));
+    PM_TRY_FREE(dalloc(&c->run_ctr, 1));
     PM_TRY_FREE(cudaMemcpy(c->sn, &cfg.train_samples, sizeof(uint32_t), cudaMemcpyHostToDevice));
     PM_TRY_FREE(dalloc(&c->scale_sum, 1));
     for (auto &ev : c->ev) PM_TRY_FREE(cudaEventCreate(&ev));

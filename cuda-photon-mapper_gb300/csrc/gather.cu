@@ -233,13 +233,22 @@ template <int S>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     query_knn_run_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
                          const uint32_t *sel, const uint32_t *order, uint32_t n, int run, int k,
-                         float r2cap, bool raw, float4 *out) {
+                         float r2cap, bool raw, float4 *out, uint32_t *run_ctr) {
     __shared__ WarpScratch ws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t first = (blockIdx.x * kWarpsPerBlock + wib) * (uint32_t)run;
-    if (first >= n) return;
-    const uint32_t last = min(first + (uint32_t)run, n);
+    const uint32_t nruns = (n + (uint32_t)run - 1) / (uint32_t)run;
     const uint64_t cap = make_key(r2cap, 0xffffffffu);
+    // with run_ctr, persistent warps take runs from the counter until none
+    // is left; without, warp w of the grid takes run w
+    uint32_t r = blockIdx.x * kWarpsPerBlock + wib;
+    for (;;) {
+    if (run_ctr) {
+        if (lane == 0) r = atomicAdd(run_ctr, 1u);
+        r = __shfl_sync(0xffffffffu, r, 0);
+    }
+    if (r >= nruns) break;
+    const uint32_t first = r * (uint32_t)run;
+    const uint32_t last = min(first + (uint32_t)run, n);
     Knn<S> kn;
     kn.reset(cap, k);
     int prev_kind = -1;  // 0 surface, 1 volume
@@ -281,6 +290,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         warm = found_k;
         prev_kind = kind;
     }
+    if (!run_ctr) break;
+    }  // runs
 }
 
 int slots_for(int k) { return (k + 31) / 32; }
@@ -345,17 +356,35 @@ cudaError_t render_frame(const PScene &S, const MapView &surf, const MapView &vo
 cudaError_t cache_knn_values_runs(const PScene &S, const MapView &surf, const MapView &vol,
                                   const float4 *qa, const float4 *qd, const uint32_t *sel,
                                   const uint32_t *order, uint32_t n, int run, int k, float radius,
-                                  bool raw, float4 *val, cudaStream_t s) {
+                                  bool raw, float4 *val, uint32_t *run_ctr, int sm_count,
+                                  cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const float r2 = radius * radius;
     const uint32_t warps = (n + (uint32_t)run - 1) / (uint32_t)run;
-    const dim3 grid((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
-    switch (slots_for(k)) {
-        case 1: query_knn_run_kernel<1><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
-        case 2: query_knn_run_kernel<2><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
-        case 3: query_knn_run_kernel<3><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
-        default: query_knn_run_kernel<4><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val); break;
+    dim3 grid((warps + kWarpsPerBlock - 1) / kWarpsPerBlock), block(kWarpsPerBlock * 32);
+    if (run_ctr) {
+        cudaError_t e = cudaMemsetAsync(run_ctr, 0, sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
     }
+#define PM_RUN_LAUNCH(SL)                                                                                   \
+    do {                                                                                                    \
+        if (run_ctr) {                                                                                      \
+            int per_sm = 1;                                                                                 \
+            cudaError_t eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, query_knn_run_kernel<SL>, \
+                                                                           kWarpsPerBlock * 32, 0);         \
+            if (eo != cudaSuccess) return eo;                                                               \
+            grid.x = std::min<uint32_t>(grid.x, (uint32_t)std::max(sm_count, 1) * (uint32_t)std::max(per_sm, 1)); \
+        }                                                                                                   \
+        query_knn_run_kernel<SL><<<grid, block, 0, s>>>(S, surf, vol, qa, qd, sel, order, n, run, k, r2, raw, val, \
+                                                        run_ctr);                                           \
+    } while (0)
+    switch (slots_for(k)) {
+        case 1: PM_RUN_LAUNCH(1); break;
+        case 2: PM_RUN_LAUNCH(2); break;
+        case 3: PM_RUN_LAUNCH(3); break;
+        default: PM_RUN_LAUNCH(4); break;
+    }
+#undef PM_RUN_LAUNCH
     note_launch();
     return cudaGetLastError();
 }
