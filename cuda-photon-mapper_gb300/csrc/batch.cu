@@ -140,6 +140,21 @@ struct pm_batch {
         size_t pix_cap = 0, q_cap = 0;
     } q;
     std::vector<uint32_t> nq;  // queries per scene
+    // The frame's estimate pass over every query-list scene at once: their
+    // query records, values, sorted orders and per-pixel scans side by side
+    // ("arena"), one descriptor per scene grouped by k-list width, and one
+    // persistent launch per width.
+    struct Arena {
+        float4 *qa = nullptr, *qd = nullptr, *val = nullptr;
+        uint32_t *ord = nullptr, *off = nullptr;
+        uint32_t *defer = nullptr, *defer_sc = nullptr, *defer_n = nullptr;
+        float *anchor_d = nullptr;
+        TileScene *desc = nullptr;
+        std::vector<size_t> q_off, p_off;  // per scene: first query, first scan word
+        int class_first[5] = {}, class_n[5] = {};
+        uint32_t class_chunks[5] = {};
+        bool on = false;
+    } ar;
 };
 
 namespace {
@@ -165,6 +180,10 @@ void free_batch(pm_batch *b) {
     cudaFree(q.scan_tmp); cudaFree(q.qa); cudaFree(q.qd); cudaFree(q.val); cudaFree(q.key);
     cudaFree(q.ord); cudaFree(q.key_tmp); cudaFree(q.ord_tmp); cudaFree(q.hist); cudaFree(q.anchor_d);
     cudaFree(q.defer_n);
+    auto &ar = b->ar;
+    cudaFree(ar.qa); cudaFree(ar.qd); cudaFree(ar.val); cudaFree(ar.ord); cudaFree(ar.off);
+    cudaFree(ar.defer); cudaFree(ar.defer_sc); cudaFree(ar.defer_n); cudaFree(ar.anchor_d);
+    cudaFree(ar.desc);
     for (auto &s : b->side)
         if (s) cudaStreamDestroy(s);
     if (b->fork) cudaEventDestroy(b->fork);
@@ -247,12 +266,18 @@ std::vector<int> pixel_ids(const pm_batch *b) {
     return v;
 }
 
-// Uploads the per-pixel launch's scene list.
+cudaError_t upload_tile_scenes(pm_batch *b);
+
+// Uploads the per-pixel launch's scene list and the estimate pass's
+// descriptors (both follow the scenes' tunes).
 cudaError_t upload_pixel_scenes(pm_batch *b) {
     const std::vector<int> ids = pixel_ids(b);
     b->n_pixel = (int)ids.size();
-    if (ids.empty()) return cudaSuccess;
-    return upload_render(b, ids, b->render_dev, b->prefix_dev);
+    if (!ids.empty()) {
+        cudaError_t e = upload_render(b, ids, b->render_dev, b->prefix_dev);
+        if (e != cudaSuccess) return e;
+    }
+    return upload_tile_scenes(b);
 }
 
 // The scene's surface / volume queries exist when its map has capacity
@@ -306,6 +331,113 @@ cudaError_t enqueue_query_scene(pm_batch *b, int s, cudaStream_t st) {
     return cudaSuccess;
 }
 
+constexpr int kTileGroups = 4;  // groups of 32 queries per chunk of the estimate pass
+
+// Uploads the estimate pass's scene descriptors: the query-list scenes
+// grouped by k-list width, chunks numbered scene after scene within a width.
+cudaError_t upload_tile_scenes(pm_batch *b) {
+    auto &ar = b->ar;
+    if (!ar.on) return cudaSuccess;
+    std::vector<TileScene> d;
+    for (int c = 1; c <= 4; ++c) {
+        ar.class_first[c] = (int)d.size();
+        uint32_t chunks = 0;
+        for (int s = 0; s < b->n; ++s) {
+            if (!b->tune[s].query_list || b->nq[s] == 0 || slots_for_k(b->cfgs[s].k) != c) continue;
+            const BatchRenderScene r = render_desc(b, s);
+            TileScene t;
+            t.sc = b->scenes_dev + s;
+            t.surf = r.surf;
+            t.vol = r.vol;
+            t.qa = ar.qa + ar.q_off[s];
+            t.qd = ar.qd + ar.q_off[s];
+            t.val = ar.val + ar.q_off[s];
+            t.order = ar.ord + ar.q_off[s];
+            t.n = b->nq[s];
+            t.chunk_begin = chunks;
+            t.k = b->cfgs[s].k;
+            t.r2cap = b->cfgs[s].radius * b->cfgs[s].radius;
+            chunks += tile_chunks(t.n, kTileGroups);
+            d.push_back(t);
+        }
+        ar.class_n[c] = (int)d.size() - ar.class_first[c];
+        ar.class_chunks[c] = chunks;
+    }
+    if (d.empty()) return cudaSuccess;
+    return cudaMemcpy(ar.desc, d.data(), sizeof(TileScene) * d.size(), cudaMemcpyHostToDevice);
+}
+
+// Scene s's query list into the arena: per-pixel counts and scans, the
+// records, then their (map, Morton) order.
+cudaError_t enqueue_arena_queries(pm_batch *b, int s, cudaStream_t st) {
+    auto &q = b->q;
+    auto &ar = b->ar;
+    const BatchRenderScene d = render_desc(b, s);
+    const pm_config &c = b->cfgs[s];
+    const uint32_t npix = (uint32_t)c.width * (uint32_t)c.height;
+    const uint32_t nq = b->nq[s];
+    if (npix == 0) return cudaSuccess;
+    bool vol_on, surf_on;
+    query_flags(b, s, &vol_on, &surf_on);
+    uint32_t *off = ar.off + ar.p_off[s];
+    float4 *qa = ar.qa + ar.q_off[s], *qd = ar.qd + ar.q_off[s];
+    uint32_t *ord = ar.ord + ar.q_off[s];
+    cudaError_t e;
+#define Q_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    Q_TRY(cache_count_queries(d.sc, d.R, vol_on, surf_on, q.cnt, q.scnt, st));
+    Q_TRY(exclusive_scan_u32_large(q.cnt, off, npix, off + npix, q.scan_tmp, st));
+    Q_TRY(exclusive_scan_u32_large(q.scnt, q.soff, npix, q.soff + npix, q.scan_tmp, st));
+    Q_TRY(cache_write_queries(d.sc, d.R, vol_on, surf_on, off, q.soff, qa, qd, q.slist, st));
+    query_gathers_kernel<<<1, 32, 0, st>>>(off + npix, q.soff + npix, b->gathers + 2 * s);
+    note_launch();
+    Q_TRY(cudaGetLastError());
+    if (nq > 0) {
+        CacheGrid box;
+        memset(&box, 0, sizeof(box));
+        const pm_scene &sc = b->scenes[s];
+        for (int a = 0; a < 3; ++a) {
+            const float ext = sc.box_max[a] - sc.box_min[a];
+            const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
+            box.lo[a] = sc.box_min[a] - m;
+            const float size = ext + 2.0f * m;
+            box.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
+        }
+        Q_TRY(cache_sample_keys(box, qa, nullptr, nq, q.key, ord, st));
+        uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
+        Q_TRY(radix_sort_pairs_u32(q.key, ord, q.key_tmp, q.ord_tmp, off + npix, nq, 0, 31, q.hist, st, &ok_keys,
+                                   &ok_vals));
+        if (ok_vals != ord)
+            Q_TRY(cudaMemcpyAsync(ord, ok_vals, sizeof(uint32_t) * nq, cudaMemcpyDeviceToDevice, st));
+    }
+#undef Q_TRY
+    return cudaSuccess;
+}
+
+// The estimate pass of every query-list scene (one persistent launch per
+// k-list width), then each scene's composite.
+cudaError_t enqueue_arena_estimates(pm_batch *b, cudaStream_t st) {
+    auto &ar = b->ar;
+    cudaError_t e;
+    for (int c = 1; c <= 4; ++c) {
+        if (ar.class_n[c] == 0) continue;
+        const TileBuffers buf{ar.anchor_d, ar.defer, ar.defer_n, nullptr};
+        e = knn_values_tiles_multi(ar.desc + ar.class_first[c], ar.class_n[c], ar.class_chunks[c], kTileGroups, c,
+                                   true, buf, ar.defer_sc, b->sm_count, st);
+        if (e != cudaSuccess) return e;
+    }
+    for (int s = 0; s < b->n; ++s) {
+        if (!b->tune[s].query_list) continue;
+        const BatchRenderScene d = render_desc(b, s);
+        const pm_config &c = b->cfgs[s];
+        const uint32_t npix = (uint32_t)c.width * (uint32_t)c.height;
+        if (npix == 0) continue;
+        e = render_composite(d.sc, ar.off + ar.p_off[s], ar.qa + ar.q_off[s], ar.qd + ar.q_off[s],
+                             ar.val + ar.q_off[s], npix, c.exposure, d.rad, d.rgba, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // Counts every scene's queries (they depend on its geometry and camera
 // only) and sizes the query buffers for the largest scene.
 cudaError_t size_query_buffers(pm_batch *b) {
@@ -345,6 +477,31 @@ cudaError_t size_query_buffers(pm_batch *b) {
     Z_TRY(dalloc(&q.anchor_d, tile_chunks((uint32_t)max_q, 4)));
     Z_TRY(dalloc(&q.defer_n, 2));  // deferred count, chunk counter
     q.q_cap = max_q;
+    // the arena of the batched estimate pass: every scene's queries
+    auto &ar = b->ar;
+    size_t q_total = 0, p_total = 0, max_chunks = 1;
+    ar.q_off.assign(b->n, 0);
+    ar.p_off.assign(b->n, 0);
+    for (int s = 0; s < b->n; ++s) {
+        ar.q_off[s] = q_total;
+        ar.p_off[s] = p_total;
+        q_total += b->nq[s];
+        p_total += (size_t)b->cfgs[s].width * b->cfgs[s].height + 1;
+        max_chunks += tile_chunks(b->nq[s], kTileGroups);
+    }
+    q_total = std::max<size_t>(q_total, 1);
+    Z_TRY(dalloc(&ar.qa, q_total));
+    Z_TRY(dalloc(&ar.qd, q_total));
+    Z_TRY(dalloc(&ar.val, q_total));
+    Z_TRY(dalloc(&ar.ord, q_total));
+    Z_TRY(dalloc(&ar.off, p_total));
+    Z_TRY(dalloc(&ar.defer, q_total));
+    Z_TRY(dalloc(&ar.defer_sc, q_total));
+    Z_TRY(dalloc(&ar.defer_n, 2));
+    Z_TRY(dalloc(&ar.anchor_d, max_chunks));
+    Z_TRY(dalloc(&ar.desc, (size_t)b->n));
+    ar.on = true;
+    Z_TRY(upload_tile_scenes(b));
 #undef Z_TRY
     return cudaSuccess;
 }
@@ -414,7 +571,8 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
     }
     if (b->n_pixel > 0) B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n_pixel, b->work, b->sm_count, st));
     for (int s = 0; s < b->n; ++s)
-        if (b->tune[s].query_list) B_TRY(enqueue_query_scene(b, s, st));
+        if (b->tune[s].query_list) B_TRY(enqueue_arena_queries(b, s, st));
+    B_TRY(enqueue_arena_estimates(b, st));
 #undef B_TRY
     return cudaSuccess;
 }

@@ -107,6 +107,29 @@ struct TileBuffers {
     uint32_t *defer_n;
     unsigned long long *stats;
 };
+// One scene of an estimate pass over many scenes (device memory): its
+// scene, maps, query records and values, its queries in (map, Morton)
+// order, their count, the first of its chunks in the launch's numbering,
+// k and the squared gather radius.
+struct TileScene {
+    const pm::PScene *sc;
+    MapView surf, vol;
+    const float4 *qa, *qd;
+    float4 *val;
+    const uint32_t *order;
+    uint32_t n;
+    uint32_t chunk_begin;
+    int k;
+    float r2cap;
+};
+// knn_values_tiles over the scenes of `scenes` (nsc descriptors, chunks
+// numbered scene after scene, total_chunks in all), all with k <= 32 *
+// slots, in three launches (anchors, one persistent shared-candidate launch,
+// deferred queries). buf.anchor_d holds total_chunks words, buf.defer and
+// defer_sc the largest possible number of deferred queries.
+cudaError_t knn_values_tiles_multi(const TileScene *scenes, int nsc, uint32_t total_chunks, int groups,
+                                   int slots, bool raw, const TileBuffers &buf, uint32_t *defer_sc,
+                                   int sm_count, cudaStream_t s);
 // Warps of an estimate pass over n queries, `groups` groups of 32 per warp.
 uint32_t tile_chunks(uint32_t n, int groups);
 // k-NN estimates of the queries in spatial order (order[0..n) indexes qa/qd

@@ -63,22 +63,50 @@ struct TileScratch {
     unsigned long long st[kStCount];  // counters, lane 0
 };
 
-// The launch's parameters, shared by the block.
+// The parameters of the scene a warp is working on (per warp: in a launch
+// over many scenes the warps of one block may serve different scenes).
 struct TileArgs {
     MapView map[2];  // surface, volume
     float4 *out;
-    uint32_t *defer;    // deferred query indices
-    uint32_t *defer_n;  // their count
-    uint64_t cap;       // key bound of the gather radius
+    uint32_t *defer;     // deferred query indices
+    uint32_t *defer_sc;  // their scenes (launches over many scenes; nullable)
+    uint32_t *defer_n;   // their count
+    uint32_t scene;      // the scene's index in such a launch
+    uint64_t cap;        // key bound of the gather radius
     float r2cap, rcap, g;
     int k;
     bool raw;
 };
 
 extern __shared__ __align__(16) unsigned char tile_smem[];
-__shared__ __align__(16) unsigned char tile_args[sizeof(TileArgs)];
+__shared__ __align__(16) unsigned char tile_args[kTileWarps * sizeof(TileArgs)];
 
-__device__ __forceinline__ TileArgs &targs() { return *reinterpret_cast<TileArgs *>(tile_args); }
+__device__ __forceinline__ TileArgs &targs() {
+    return reinterpret_cast<TileArgs *>(tile_args)[threadIdx.x >> 5];
+}
+
+// Lane 0 fills the warp's arguments; the warp then synchronises.
+__device__ __forceinline__ void set_targs(const MapView &surf, const MapView &vol, float4 *out,
+                                          uint32_t *defer, uint32_t *defer_sc, uint32_t *defer_n,
+                                          uint32_t scene, float r2cap, float g, int k, bool raw) {
+    if ((threadIdx.x & 31) == 0) {
+        TileArgs &t = targs();
+        t.map[0] = surf;
+        t.map[1] = vol;
+        t.out = out;
+        t.defer = defer;
+        t.defer_sc = defer_sc;
+        t.defer_n = defer_n;
+        t.scene = scene;
+        t.cap = make_key(r2cap, 0xffffffffu);
+        t.r2cap = r2cap;
+        t.rcap = sqrtf(r2cap);
+        t.g = g;
+        t.k = k;
+        t.raw = raw;
+    }
+    __syncwarp();
+}
 
 __device__ __forceinline__ TileScratch &scratch() {
     return reinterpret_cast<TileScratch *>(tile_smem)[threadIdx.x >> 5];
@@ -159,7 +187,11 @@ __device__ __forceinline__ void defer(const Query &q, unsigned mask) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(targs().defer_n, (uint32_t)__popc(mask));
     base = __shfl_sync(kFull, base, 0);
-    if ((mask >> lane) & 1u) targs().defer[base + __popc(mask & ((1u << lane) - 1u))] = q.out;
+    if ((mask >> lane) & 1u) {
+        const uint32_t at = base + __popc(mask & ((1u << lane) - 1u));
+        targs().defer[at] = q.out;
+        if (targs().defer_sc) targs().defer_sc[at] = targs().scene;
+    }
     count(kStList, (unsigned long long)__popc(mask));
 }
 
@@ -522,41 +554,15 @@ __device__ __forceinline__ void tighten(const Query &q, unsigned mask, float d_l
     }
 }
 
+// One chunk (groups of 32 consecutive queries of the sorted order, from
+// query chunk * 32 * groups) of a scene, with the warp's arguments set.
 template <int S>
-__global__ void __launch_bounds__(kTileWarps * 32, 5)
-    query_knn_tile_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
-                          const uint32_t *order, uint32_t n, const uint32_t *n_dev, int groups,
-                          const float *anchor_d, int k, float r2cap, bool raw, float4 *out,
-                          uint32_t *defer_list, uint32_t *defer_n, uint32_t *chunk_counter,
-                          unsigned long long *stats) {
+__device__ __forceinline__ void tile_chunk(const PScene &Sc, const MapView &surf, const MapView &vol,
+                                           const float4 *qa, const float4 *qd, const uint32_t *order,
+                                           uint32_t n, uint32_t chunk, float anchor, int groups,
+                                           float r2cap, bool raw, float4 *out) {
     const int lane = threadIdx.x & 31;
-    if (n_dev) n = min(n, *n_dev);
-    if (threadIdx.x == 0) {
-        targs().map[0] = surf;
-        targs().map[1] = vol;
-        targs().out = out;
-        targs().defer = defer_list;
-        targs().defer_n = defer_n;
-        targs().cap = make_key(r2cap, 0xffffffffu);
-        targs().r2cap = r2cap;
-        targs().rcap = sqrtf(r2cap);
-        targs().g = Sc.g;
-        targs().k = k;
-        targs().raw = raw;
-    }
-    TileScratch &ts = scratch();
-    if (lane < kStCount) ts.st[lane] = 0;
-    __syncthreads();
-    const uint32_t nchunks = (n + 32u * (uint32_t)groups - 1u) / (32u * (uint32_t)groups);
     const float rcap = sqrtf(r2cap);
-    // persistent warps: each takes the next chunk from the counter until
-    // none is left, so a block's resources are never held by finished warps
-    // waiting on a slow one
-    for (;;) {
-    uint32_t chunk = 0;
-    if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
-    chunk = __shfl_sync(kFull, chunk, 0);
-    if (chunk >= nchunks) break;
     const uint32_t wfirst = chunk * (uint32_t)(32 * groups);
     // exact distances known so far (lane j: one point; kd < 0: none): the
     // anchor, later the previous group
@@ -570,7 +576,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
             kx = a.x;
             ky = a.y;
             kz = a.z;
-            kd = anchor_d[chunk];
+            kd = anchor;
         }
     }
     for (int g = 0; g < groups; ++g) {
@@ -640,7 +646,75 @@ __global__ void __launch_bounds__(kTileWarps * 32, 5)
         kz = q.x.z;
         kd = ((members >> lane) & 1u) ? dnew : -1.0f;
     }
-    }  // chunks
+}
+
+template <int S>
+__global__ void __launch_bounds__(kTileWarps * 32, 5)
+    query_knn_tile_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
+                          const uint32_t *order, uint32_t n, const uint32_t *n_dev, int groups,
+                          const float *anchor_d, int k, float r2cap, bool raw, float4 *out,
+                          uint32_t *defer_list, uint32_t *defer_n, uint32_t *chunk_counter,
+                          unsigned long long *stats) {
+    const int lane = threadIdx.x & 31;
+    if (n_dev) n = min(n, *n_dev);
+    set_targs(surf, vol, out, defer_list, nullptr, defer_n, 0u, r2cap, Sc.g, k, raw);
+    TileScratch &ts = scratch();
+    if (lane < kStCount) ts.st[lane] = 0;
+    __syncwarp();
+    const uint32_t nchunks = (n + 32u * (uint32_t)groups - 1u) / (32u * (uint32_t)groups);
+    // persistent warps: each takes the next chunk from the counter until
+    // none is left, so a block's resources are never held by finished warps
+    // waiting on a slow one
+    for (;;) {
+        uint32_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
+        chunk = __shfl_sync(kFull, chunk, 0);
+        if (chunk >= nchunks) break;
+        tile_chunk<S>(Sc, surf, vol, qa, qd, order, n, chunk, anchor_d[chunk], groups, r2cap, raw, out);
+    }
+    __syncwarp();
+    if (stats && lane < kStCount && ts.st[lane]) atomicAdd(&stats[lane], ts.st[lane]);
+}
+
+// The scene of global chunk c: the last descriptor whose chunk_begin <= c.
+__device__ __forceinline__ int scene_of_chunk(const TileScene *scenes, int nsc, uint32_t c) {
+    int lo = 0, hi = nsc - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (scenes[mid].chunk_begin <= c) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The same pass over the chunks of many scenes (their descriptors in device
+// memory, chunks numbered scene after scene): one persistent launch; a warp
+// loads a scene's arguments when its next chunk belongs to another scene.
+template <int S>
+__global__ void __launch_bounds__(kTileWarps * 32, 5)
+    query_knn_tile_multi_kernel(const TileScene *scenes, int nsc, uint32_t total_chunks, int groups,
+                                const float *anchor_d, bool raw, uint32_t *defer_list,
+                                uint32_t *defer_sc, uint32_t *defer_n, uint32_t *chunk_counter,
+                                unsigned long long *stats) {
+    const int lane = threadIdx.x & 31;
+    TileScratch &ts = scratch();
+    if (lane < kStCount) ts.st[lane] = 0;
+    __syncwarp();
+    int cur = -1;
+    for (;;) {
+        uint32_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
+        chunk = __shfl_sync(kFull, chunk, 0);
+        if (chunk >= total_chunks) break;
+        const int sidx = scene_of_chunk(scenes, nsc, chunk);
+        const TileScene &d = scenes[sidx];
+        if (sidx != cur) {
+            set_targs(d.surf, d.vol, d.val, defer_list, defer_sc, defer_n, (uint32_t)sidx, d.r2cap, d.sc->g,
+                      d.k, raw);
+            cur = sidx;
+        }
+        tile_chunk<S>(*d.sc, d.surf, d.vol, d.qa, d.qd, d.order, d.n, chunk - d.chunk_begin, anchor_d[chunk],
+                      groups, d.r2cap, raw, d.val);
+    }
     __syncwarp();
     if (stats && lane < kStCount && ts.st[lane]) atomicAdd(&stats[lane], ts.st[lane]);
 }
@@ -663,6 +737,52 @@ __global__ void __launch_bounds__(128)
     kn.reset(cap, k);
     knn_search<S>(m, mk3(a.x, a.y, a.z), kn, ws[wib], lane, cap);
     if (lane == 0) anchor_d[chunk] = kn.worst < cap ? sqrtf(key_d2(kn.worst)) : sqrtf(r2cap);
+}
+
+// The anchors of the chunks of many scenes (global chunk numbering).
+template <int S>
+__global__ void __launch_bounds__(128)
+    anchor_multi_kernel(const TileScene *scenes, int nsc, uint32_t total_chunks, int groups,
+                        float *anchor_d) {
+    __shared__ WarpScratch ws[4];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t chunk = blockIdx.x * 4 + wib;
+    if (chunk >= total_chunks) return;
+    const TileScene &d = scenes[scene_of_chunk(scenes, nsc, chunk)];
+    const uint32_t wfirst = (chunk - d.chunk_begin) * (uint32_t)(32 * groups);
+    const float4 a = d.qa[d.order[wfirst + min((uint32_t)kAnchorAt, d.n - 1 - wfirst)]];
+    const MapView &m = __float_as_int(a.w) != kNone ? d.surf : d.vol;
+    const uint64_t cap = make_key(d.r2cap, 0xffffffffu);
+    Knn<S> kn;
+    kn.reset(cap, d.k);
+    knn_search<S>(m, mk3(a.x, a.y, a.z), kn, ws[wib], lane, cap);
+    if (lane == 0) anchor_d[chunk] = kn.worst < cap ? sqrtf(key_d2(kn.worst)) : sqrtf(d.r2cap);
+}
+
+// The deferred queries of many scenes (defer_sc: each one's scene).
+template <int S>
+__global__ void __launch_bounds__(128)
+    deferred_multi_kernel(const TileScene *scenes, const uint32_t *defer_list, const uint32_t *defer_sc,
+                          const uint32_t *defer_n, bool raw) {
+    __shared__ WarpScratch ws[4];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t total = *defer_n;
+    for (uint32_t w = blockIdx.x * 4 + wib; w < total; w += gridDim.x * 4) {
+        const TileScene &d = scenes[defer_sc[w]];
+        const uint64_t cap = make_key(d.r2cap, 0xffffffffu);
+        const Query q = load_query(*d.sc, d.qa, d.qd, defer_list[w]);
+        const MapView &m = q.map == 0 ? d.surf : d.vol;
+        v3 e = mk3(0.f, 0.f, 0.f);
+        int found = 0;
+        float r2 = d.r2cap;
+        if (m.n > 0) {
+            Knn<S> kn;
+            kn.reset(cap, d.k);
+            knn_search<S>(m, q.x, kn, ws[wib], lane, cap);
+            e = flux_sum<S>(kn, m, lane, q.map, q.dirv, d.sc->g, cap, d.r2cap, &found, &r2);
+        }
+        write_estimate(d.val, q.out, e, found, r2, q.map == 0, raw);
+    }
 }
 
 // The deferred queries, one warp each (grid-stride over the list).
@@ -726,6 +846,38 @@ cudaError_t knn_values_tiles(const PScene &S, const MapView &surf, const MapView
         default: PM_TILE_LAUNCH(4); break;
     }
 #undef PM_TILE_LAUNCH
+    note_launches(3);
+    return cudaGetLastError();
+}
+
+cudaError_t knn_values_tiles_multi(const TileScene *scenes, int nsc, uint32_t total_chunks, int groups,
+                                   int slots, bool raw, const TileBuffers &buf, uint32_t *defer_sc,
+                                   int sm_count, cudaStream_t s) {
+    if (total_chunks == 0 || nsc == 0) return cudaSuccess;
+    if (groups < 1 || groups > 4 || slots < 1 || slots > 4) return cudaErrorInvalidValue;
+    const dim3 agrid((total_chunks + kTileWarps - 1) / kTileWarps), block(kTileWarps * 32);
+    const int smem = (int)(kTileWarps * sizeof(TileScratch));
+    const dim3 dgrid(std::max(sm_count, 1) * 8);
+    cudaError_t e = cudaMemsetAsync(buf.defer_n, 0, 2 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    int per_sm = 1;
+#define PM_MULTI_LAUNCH(SL)                                                                              \
+    anchor_multi_kernel<SL><<<agrid, block, 0, s>>>(scenes, nsc, total_chunks, groups, buf.anchor_d);   \
+    e = cudaFuncSetAttribute(query_knn_tile_multi_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
+    if (e != cudaSuccess) return e;                                                                     \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, query_knn_tile_multi_kernel<SL>, kTileWarps * 32, smem); \
+    if (e != cudaSuccess) return e;                                                                     \
+    query_knn_tile_multi_kernel<SL><<<std::min<uint32_t>(agrid.x, (uint32_t)std::max(sm_count, 1) * (uint32_t)std::max(per_sm, 1)), \
+                                      block, smem, s>>>(scenes, nsc, total_chunks, groups, buf.anchor_d, raw, \
+                                                        buf.defer, defer_sc, buf.defer_n, buf.defer_n + 1, buf.stats); \
+    deferred_multi_kernel<SL><<<dgrid, 128, 0, s>>>(scenes, buf.defer, defer_sc, buf.defer_n, raw)
+    switch (slots) {
+        case 1: PM_MULTI_LAUNCH(1); break;
+        case 2: PM_MULTI_LAUNCH(2); break;
+        case 3: PM_MULTI_LAUNCH(3); break;
+        default: PM_MULTI_LAUNCH(4); break;
+    }
+#undef PM_MULTI_LAUNCH
     note_launches(3);
     return cudaGetLastError();
 }
