@@ -654,34 +654,59 @@ __global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph
     }
 }
 
-// The table gradient of n samples from their feature gradients (p.dx):
-// one thread per (sample, level) adds the 8 corners' terms w * dL/dfeature
-// as fixed-point integers. Does nothing once a tensor-core wait of the
-// training kernel has given up (its rows are then incomplete).
-__global__ void __launch_bounds__(256) table_scatter_kernel(CacheGrid g, CacheParams p,
-                                                            const float4 *qa, const uint32_t *sel,
-                                                            uint32_t n) {
+// The table gradient of n samples from their feature gradients (p.dx): a
+// block of kCacheMaxLevels warps takes 32 consecutive samples, warp l their
+// level l (the training order keeps each batch in (map, Morton) order, so
+// the 32 samples are spatial neighbours). Each term w * dL/dfeature is
+// rounded to fixed point and added with an integer atomic. On the coarse
+// levels (resolution <= kScatterGroupRes) neighbouring samples share
+// corners: lanes whose corner is the same table entry (match_any) add their
+// terms in shared memory first and the lowest of them issues the atomics --
+// the same integer sums, fewer atomics on the most contended entries. Does
+// nothing once a tensor-core wait of the training kernel has given up (its
+// rows are then incomplete).
+constexpr int kScatterGroupRes = 111;
+__global__ void __launch_bounds__(kCacheMaxLevels * 32) table_scatter_kernel(CacheGrid g, CacheParams p,
+                                                                          const float4 *qa,
+                                                                          const uint32_t *sel, uint32_t n) {
+    __shared__ longlong2 red[kCacheMaxLevels][32];
     if (*(volatile int *)p.status) return;
-    const size_t T = (size_t)1 << g.log2_t;
-    const size_t total = (size_t)n * kCacheMaxLevels;
-    const float2 *dxf = reinterpret_cast<const float2 *>(p.dx);
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const uint32_t i = (uint32_t)(t / kCacheMaxLevels);
-        const int l = (int)(t % kCacheMaxLevels);
-        if (l >= g.levels) continue;
-        const float2 gr = dxf[t];
-        if (gr.x == 0.0f && gr.y == 0.0f) continue;
-        const QueryPos q = unit_pos(g, qa[sel ? sel[i] : i]);
-        uint32_t idx[8];
-        float w[8];
-        level_corners(g, l, q.px, q.py, q.pz, idx, w);
-        unsigned long long *lv = reinterpret_cast<unsigned long long *>(p.table_grad) + 2 * (size_t)l * T;
+    const int lane = threadIdx.x & 31, l = threadIdx.x >> 5;
+    if (l >= g.levels) return;
+    const uint32_t i = blockIdx.x * 32u + (uint32_t)lane;
+    const bool valid = i < n;
+    const float2 gr = valid ? reinterpret_cast<const float2 *>(p.dx)[(size_t)i * kCacheMaxLevels + l]
+                            : make_float2(0.0f, 0.0f);
+    if (!__any_sync(0xffffffffu, gr.x != 0.0f || gr.y != 0.0f)) return;
+    QueryPos q{0.0f, 0.0f, 0.0f};
+    if (valid) q = unit_pos(g, qa[sel ? sel[i] : i]);
+    uint32_t idx[8];
+    float w[8];
+    level_corners(g, l, q.px, q.py, q.pz, idx, w);
+    unsigned long long *lv = reinterpret_cast<unsigned long long *>(p.table_grad) + 2 * ((size_t)l << g.log2_t);
+    const bool group = g.res[l] <= kScatterGroupRes;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const long long q0 = to_grad_fixed(w[k] * gr.x), q1 = to_grad_fixed(w[k] * gr.y);
-            if (q0) atomicAdd(lv + 2 * idx[k], (unsigned long long)q0);
-            if (q1) atomicAdd(lv + 2 * idx[k] + 1, (unsigned long long)q1);
+    for (int k = 0; k < 8; ++k) {
+        long long s0 = to_grad_fixed(w[k] * gr.x), s1 = to_grad_fixed(w[k] * gr.y);
+        bool lead = true;
+        if (group) {
+            const unsigned peers = __match_any_sync(0xffffffffu, idx[k]);
+            lead = lane == __ffs(peers) - 1;
+            if (peers != (1u << lane)) {
+                red[l][lane] = make_longlong2(s0, s1);
+                __syncwarp(peers);
+                if (lead)
+                    for (unsigned m = peers & (peers - 1u); m; m &= m - 1u) {
+                        const longlong2 o = red[l][__ffs(m) - 1];
+                        s0 += o.x;
+                        s1 += o.y;
+                    }
+                __syncwarp(peers);
+            }
+        }
+        if (lead) {
+            if (s0) atomicAdd(lv + 2 * idx[k], (unsigned long long)s0);
+            if (s1) atomicAdd(lv + 2 * idx[k] + 1, (unsigned long long)s1);
         }
     }
 }
@@ -929,6 +954,33 @@ __global__ void sample_keys_kernel(CacheGrid g, const float4 *qa, const uint32_t
     vals[i] = i;
 }
 
+// The sorted picks' records: pick pos[i] copied to pqa[i], pqd[i]; pord[i] = i.
+__global__ void pick_records_kernel(const uint32_t *pos, const uint32_t *sel, const float4 *qa,
+                                    const float4 *qd, uint32_t n, float4 *pqa, float4 *pqd, uint32_t *pord) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t q = sel[pos[i]];
+    pqa[i] = qa[q];
+    pqd[i] = qd[q];
+    pord[i] = i;
+}
+
+// Sorted pick j -> slot j / nb of batch j % nb (batch b starting at
+// b * (n / nb) + min(b, n % nb)): every batch takes every nb-th pick of the
+// (map, Morton) order.
+__global__ void train_order_kernel(const float4 *pqa, const float4 *pqd, const float4 *pval,
+                                   const uint32_t *pos, const uint32_t *sel, uint32_t n, uint32_t nb,
+                                   float4 *tqa, float4 *tqd, float4 *tgt, uint32_t *tsel) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t b = j % nb;
+    const uint32_t t = b * (n / nb) + min(b, n % nb) + j / nb;
+    tqa[t] = pqa[j];
+    tqd[t] = pqd[j];
+    tgt[t] = pval[j];
+    tsel[t] = sel[pos[j]];
+}
+
 __global__ void iota_kernel(uint32_t *v, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) v[i] = i;
@@ -990,6 +1042,23 @@ cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 
     if (npix == 0) return cudaSuccess;
     composite_exact_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, off, qa, qd, raw, npix, exposure, rad,
                                                               rgba);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_pick_records(const uint32_t *pos, const uint32_t *sel, const float4 *qa, const float4 *qd,
+                               uint32_t n, float4 *pqa, float4 *pqd, uint32_t *pord, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    pick_records_kernel<<<(n + 255) / 256, 256, 0, s>>>(pos, sel, qa, qd, n, pqa, pqd, pord);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_train_order(const float4 *pqa, const float4 *pqd, const float4 *pval,
+                              const uint32_t *pos, const uint32_t *sel, uint32_t n, uint32_t nb,
+                              float4 *tqa, float4 *tqd, float4 *tgt, uint32_t *tsel, cudaStream_t s) {
+    if (n == 0 || nb == 0) return cudaSuccess;
+    train_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(pqa, pqd, pval, pos, sel, n, nb, tqa, tqd, tgt, tsel);
     note_launch();
     return cudaGetLastError();
 }
@@ -1071,9 +1140,7 @@ cudaError_t cache_backward(const CacheGrid &g, const CacheParams &p, const PScen
     wgrad_reduce_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w_part, p.loss_part, (int)grid,
                                                                   p.w_grad, p.loss);
     note_launch();
-    const size_t threads = (size_t)n * kCacheMaxLevels;
-    const uint32_t sgrid = (uint32_t)std::min<size_t>((threads + 255) / 256, (size_t)sm_count * 8);
-    table_scatter_kernel<<<sgrid, 256, 0, s>>>(g, p, qa, sel, n);
+    table_scatter_kernel<<<(n + 31) / 32, kCacheMaxLevels * 32, 0, s>>>(g, p, qa, sel, n);
     note_launch();
     return cudaGetLastError();
 }

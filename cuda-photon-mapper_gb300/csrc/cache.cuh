@@ -100,6 +100,18 @@ cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 
 // grid box; vals[i] = i.
 cudaError_t cache_sample_keys(const CacheGrid &g, const float4 *qa, const uint32_t *sel, uint32_t n,
                               uint32_t *keys, uint32_t *vals, cudaStream_t s);
+// The picks in sorted order (pos[i] the i-th pick, sel[pos[i]] its
+// query): their records into pqa, pqd; pord[i] = i.
+cudaError_t cache_pick_records(const uint32_t *pos, const uint32_t *sel, const float4 *qa, const float4 *qd,
+                               uint32_t n, float4 *pqa, float4 *pqd, uint32_t *pord, cudaStream_t s);
+// The training order of n sorted picks in nb batches: sorted pick j
+// (records pqa/pqd[j], target pval[j], query sel[pos[j]]) to slot j / nb of
+// batch j % nb, batch b holding n / nb + (b < n % nb) samples from
+// b * (n / nb) + min(b, n % nb) -- each batch a spatially stratified
+// sample, in (map, Morton) order within.
+cudaError_t cache_train_order(const float4 *pqa, const float4 *pqd, const float4 *pval,
+                              const uint32_t *pos, const uint32_t *sel, uint32_t n, uint32_t nb,
+                              float4 *tqa, float4 *tqd, float4 *tgt, uint32_t *tsel, cudaStream_t s);
 // v[i] = i for i < n.
 cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s);
 // Training picks from Philox(seed, frame, i): with probability surf_frac

@@ -29,6 +29,12 @@ struct CacheState {
     uint32_t *skey = nullptr, *sval = nullptr, *skey_tmp = nullptr, *sval_tmp = nullptr;
     uint32_t *shist = nullptr, *sn = nullptr;
     uint32_t *run_ctr = nullptr;  // the target launch's run counter
+    // the sorted picks' records, identity order and targets
+    float4 *pqa = nullptr, *pqd = nullptr, *pval = nullptr;
+    uint32_t *pord = nullptr;
+    // training order: batch after batch, each every nb-th sorted pick
+    float4 *tqa = nullptr, *tqd = nullptr;
+    uint32_t *tsel = nullptr;
     // the order inference takes the render's queries in
     uint32_t *iorder = nullptr;
     uint32_t iorder_cap = 0;
@@ -46,11 +52,19 @@ namespace {
 
 constexpr int kTargetRun = 8;  // training targets warm-started in runs of this length
 
-// The frame's training picks c->sel[0..ns) (uniform, stratified between
-// diffuse and volume queries) and their k-NN targets in c->tgt: the picks
-// sorted by (map, Morton code) and estimated in runs of kTargetRun
-// warm-started list searches (picks this sparse are too far apart to share
-// candidate sets), written back in pick order.
+// Training batches of a frame of ns picks: as many as batches of `batch`
+// need, every one a spatially stratified sample (cache_train_order).
+uint32_t batch_count(uint32_t ns, uint32_t batch) { return (ns + batch - 1) / batch; }
+
+// The frame's training picks (uniform, stratified between diffuse and
+// volume queries) and their k-NN targets, in training order: c->tqa, c->tqd
+// the picks' records, c->tgt their targets, c->tsel their queries. The
+// picks are sorted by (map, Morton code), their records gathered in that
+// order, and estimated in runs of kTargetRun warm-started list searches
+// (the volume picks, a few per cent of the volume queries, are too far
+// apart to share candidate sets; measured on the diffuse picks too, the
+// shared-candidate pass was slower than the runs). Then batch b takes every
+// nb-th sorted pick.
 cudaError_t pick_and_target(PhysicalState *st, CacheState *c, cudaStream_t stream) {
     const uint32_t ns = c->cfg.train_samples;
     cudaError_t e;
@@ -61,9 +75,12 @@ cudaError_t pick_and_target(PhysicalState *st, CacheState *c, cudaStream_t strea
     uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
     CT_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31, c->shist,
                                 stream, &ok_keys, &ok_vals));
-    CT_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), st->ql.qa, st->ql.qd,
-                                 c->sel, ok_vals, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->tgt,
-                                 c->run_ctr, c->sm_count, stream));
+    CT_TRY(cache_pick_records(ok_vals, c->sel, st->ql.qa, st->ql.qd, ns, c->pqa, c->pqd, c->pord, stream));
+    CT_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->pqa, c->pqd, nullptr,
+                                 c->pord, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->pval, c->run_ctr,
+                                 c->sm_count, stream));
+    CT_TRY(cache_train_order(c->pqa, c->pqd, c->pval, ok_vals, c->sel, ns, batch_count(ns, c->cfg.batch),
+                             c->tqa, c->tqd, c->tgt, c->tsel, stream));
 #undef CT_TRY
     return cudaSuccess;
 }
@@ -85,6 +102,8 @@ void free_cache(CacheState *c) {
     cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum); cudaFree(c->iorder);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
     cudaFree(c->shist); cudaFree(c->sn); cudaFree(c->run_ctr);
+    cudaFree(c->pqa); cudaFree(c->pqd); cudaFree(c->pval); cudaFree(c->pord);
+    cudaFree(c->tqa); cudaFree(c->tqd); cudaFree(c->tsel);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->tev0) cudaEventDestroy(c->tev0);
@@ -219,6 +238,13 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     PM_TRY_FREE(dalloc(&c->shist, radix_sort_hist_words(cfg.train_samples)));
     PM_TRY_FREE(dalloc(&c->sn, 1));
     PM_TRY_FREE(dalloc(&c->run_ctr, 1));
+    PM_TRY_FREE(dalloc(&c->pqa, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->pqd, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->pval, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->pord, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->tqa, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->tqd, cfg.train_samples));
+    PM_TRY_FREE(dalloc(&c->tsel, cfg.train_samples));
     PM_TRY_FREE(cudaMemcpy(c->sn, &cfg.train_samples, sizeof(uint32_t), cudaMemcpyHostToDevice));
     PM_TRY_FREE(dalloc(&c->scale_sum, 1));
     for (auto &ev : c->ev) PM_TRY_FREE(cudaEventCreate(&ev));
@@ -248,8 +274,8 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
     if (s != PM_OK) return s;
     if (st->ql.nq == 0 || frames == 0) return PM_OK;
     cudaError_t e;
-    const uint32_t ns = c->cfg.train_samples, batch = c->cfg.batch;
-    const uint32_t nb = (ns + batch - 1) / batch;
+    const uint32_t ns = c->cfg.train_samples;
+    const uint32_t nb = batch_count(ns, c->cfg.batch);
     for (int f = 0; f < frames; ++f) {
         PM_TRY(cudaEventRecord(c->tev0, stream));
         PM_TRY(pick_and_target(st, c, stream));
@@ -265,8 +291,9 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
         }
         PM_TRY(cudaMemsetAsync(c->p.loss, 0, sizeof(float), stream));
         for (uint32_t b = 0; b < nb; ++b) {
-            const uint32_t o = b * batch, n = std::min(batch, ns - o);
-            PM_TRY(cache_backward(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, c->sel + o, c->tgt + o, n,
+            // batch b: slots [o, o + n) of the training order
+            const uint32_t o = b * (ns / nb) + std::min(b, ns % nb), n = ns / nb + (b < ns % nb ? 1u : 0u);
+            PM_TRY(cache_backward(c->grid, c->p, st->dscene, c->tqa + o, c->tqd + o, nullptr, c->tgt + o, n,
                                   1.0f / c->target_scale, 1.0f / (3.0f * (float)n), c->cfg.loss_eps,
                                   nullptr, nullptr, c->sm_count, stream));
             float lr = c->cfg.lr;
@@ -515,7 +542,7 @@ pm_status pm_cache_debug_targets(pm_ctx *ctx, float4 *targets, uint32_t *query) 
     PM_TRY(pick_and_target(st, c, 0));
     PM_TRY(cudaDeviceSynchronize());
     if (targets) PM_TRY(cudaMemcpy(targets, c->tgt, sizeof(float4) * ns, cudaMemcpyDeviceToHost));
-    if (query) PM_TRY(cudaMemcpy(query, c->sel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
+    if (query) PM_TRY(cudaMemcpy(query, c->tsel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
     return PM_OK;
 }
 
