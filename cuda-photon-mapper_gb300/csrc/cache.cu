@@ -798,24 +798,64 @@ struct CountSink {
     __device__ void surface(v3, int, v3, float) { ++n; ++ns; }
 };
 
+// The query list keeps each block of 32 consecutive pixels (one warp of
+// the kernels below; the block's queries one contiguous range from
+// off[first pixel]) in sample-major order: the first query of every pixel
+// of the block, then the second ones, ..., pixels in order within a step.
+// The lanes' stores and loads of one step then land side by side, and the
+// order is also the one inference wants (neighbouring rays at similar
+// depths). Query s of lane p sits at
+//   base + sum_q min(c_q, s) + #{q < p : c_q > s}
+// for the block's per-pixel counts c_q. The writer tracks it per lane with
+// the block's counts sorted ascending in shared memory: `base` the first
+// slot of step s, `live` the lanes with more than s queries.
+constexpr int kListWarps = 4;  // warps (pixel blocks) per CTA of the list kernels
 struct WriteSink {
     static constexpr bool kCountOnly = false;
     __device__ void volume_steps(int) {}
     float4 *qa, *qd;
     uint32_t *slist;
-    uint32_t at, sat;
+    uint32_t sat;
+    const uint2 *srt;  // (count, lane) of the block's pixels, ascending
+    uint32_t base, live, lt, s, j;
+    __device__ uint32_t next() {
+        const uint32_t at = base + (uint32_t)__popc(live & lt);
+        base += (uint32_t)__popc(live);
+        ++s;
+        while (j < 32u && srt[j].x <= s) live &= ~(1u << srt[j++].y);
+        return at;
+    }
     __device__ void volume(v3 x, v3 wo, float w) {
+        const uint32_t at = next();
         qa[at] = make_float4(x.x, x.y, x.z, __int_as_float(kNone));
         qd[at] = make_float4(wo.x, wo.y, wo.z, w);
-        ++at;
     }
     __device__ void surface(v3 x, int obj, v3 wo, float w) {
+        const uint32_t at = next();
         slist[sat++] = at;
         qa[at] = make_float4(x.x, x.y, x.z, __int_as_float(obj));
         qd[at] = make_float4(wo.x, wo.y, wo.z, w);
-        ++at;
     }
 };
+
+// Calls f(i) for the list index i of each query of this lane's pixel, in
+// the pixel's own order (s = 0, 1, ...). Warp-synchronous: every lane of
+// the warp calls it, lanes past npix with no queries; the warp's first
+// pixel must be below npix.
+template <typename F>
+__device__ __forceinline__ void for_pixel_queries(const uint32_t *off, uint32_t pix, uint32_t npix, F &&f) {
+    const int lane = threadIdx.x & 31;
+    const bool valid = pix < npix;
+    const uint32_t o = valid ? off[pix] : 0u, c = valid ? off[pix + 1] - o : 0u;
+    uint32_t base = __shfl_sync(0xffffffffu, o, 0);
+    const uint32_t cmax = __reduce_max_sync(0xffffffffu, c);
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t s = 0; s < cmax; ++s) {
+        const unsigned m = __ballot_sync(0xffffffffu, s < c);
+        if (s < c) f(base + (uint32_t)__popc(m & lt));
+        base += (uint32_t)__popc(m);
+    }
+}
 
 __global__ void count_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on, uint32_t *cnt,
                              uint32_t *scnt) {
@@ -827,48 +867,45 @@ __global__ void count_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_o
     scnt[pix] = c.ns;
 }
 
-__global__ void write_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on,
-                             const uint32_t *off, const uint32_t *soff, float4 *qa, float4 *qd,
-                             uint32_t *slist) {
+__global__ void __launch_bounds__(kListWarps * 32)
+    write_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on, const uint32_t *off,
+                 const uint32_t *soff, float4 *qa, float4 *qd, uint32_t *slist) {
+    __shared__ uint2 srt[kListWarps][32];
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= (uint32_t)R.width * (uint32_t)R.height) return;
-    WriteSink w{qa, qd, slist, off[pix], soff[pix]};
-    walk_eye(Sc, R, pix, vol_on, surf_on, w);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (pix - (uint32_t)lane >= npix) return;  // the whole block of 32 pixels
+    const bool valid = pix < npix;
+    const uint32_t c = valid ? off[pix + 1] - off[pix] : 0u;
+    // the block's counts sorted ascending (ties by lane)
+    uint32_t rank = 0;
+    for (int q = 0; q < 32; ++q) {
+        const uint32_t cq = __shfl_sync(0xffffffffu, c, q);
+        rank += (cq < c || (cq == c && q < lane)) ? 1u : 0u;
+    }
+    srt[w][rank] = make_uint2(c, (uint32_t)lane);
+    __syncwarp();
+    WriteSink ws;
+    ws.qa = qa;
+    ws.qd = qd;
+    ws.slist = slist;
+    ws.sat = valid ? soff[pix] : 0u;
+    ws.srt = srt[w];
+    ws.base = __shfl_sync(0xffffffffu, valid ? off[pix] : 0u, 0);
+    ws.live = __ballot_sync(0xffffffffu, c > 0u);
+    ws.lt = (1u << lane) - 1u;
+    ws.s = 0;
+    ws.j = (uint32_t)__popc(__ballot_sync(0xffffffffu, c == 0u));
+    if (valid) walk_eye(Sc, R, pix, vol_on, surf_on, ws);
 }
 
-// The queries of each block of 32 consecutive pixels (one contiguous range
-// of the list) in sample-major order: sample 0 of every pixel of the block,
-// then sample 1, ... -- neighbouring rays at similar depths, whose hash-grid
-// corners coincide on the middle levels, instead of one ray's march.
-__global__ void pixel_block_order_kernel(const uint32_t *off, uint32_t npix, uint32_t *order) {
-    const uint32_t first = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u;
-    if (first >= npix) return;  // whole warps
-    const int lane = threadIdx.x & 31;
-    const uint32_t px = first + (uint32_t)lane;
-    uint32_t o = 0, c = 0;
-    if (px < npix) {
-        o = off[px];
-        c = off[px + 1] - o;
-    }
-    uint32_t base = __shfl_sync(0xffffffffu, o, 0);
-    const uint32_t cmax = __reduce_max_sync(0xffffffffu, c);
-    const unsigned lt = (1u << lane) - 1u;
-    for (uint32_t s = 0; s < cmax; ++s) {
-        const bool act = s < c;
-        const unsigned m = __ballot_sync(0xffffffffu, act);
-        if (act) order[base + __popc(m & lt)] = o + s;
-        base += __popc(m);
-    }
-}
-
-__global__ void composite_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
-                                 const float4 *val, uint32_t npix, float exposure, float4 *rad,
-                                 uchar4 *rgba) {
+__global__ void __launch_bounds__(kListWarps * 32)
+    composite_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
+                     const float4 *val, uint32_t npix, float exposure, float4 *rad, uchar4 *rgba) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
+    if (pix - (threadIdx.x & 31u) >= npix) return;
     v3 L = mk3(0.f, 0.f, 0.f);
-    const uint32_t e = off[pix + 1];
-    for (uint32_t i = off[pix]; i < e; ++i) {
+    for_pixel_queries(off, pix, npix, [&](uint32_t i) {
         const int obj = __float_as_int(qa[i].w);
         const float w = qd[i].w;
         const float4 v = val[i];
@@ -878,7 +915,8 @@ __global__ void composite_kernel(PScene Sc, const uint32_t *off, const float4 *q
         } else {
             L = L + mk3(v.x * w, v.y * w, v.z * w);
         }
-    }
+    });
+    if (pix >= npix) return;
     if (rad) rad[pix] = make_float4(L.x, L.y, L.z, 1.0f);
     if (rgba)
         rgba[pix] = make_uchar4(to_u8_sat((double)(L.x * exposure) * 255.0),
@@ -890,16 +928,15 @@ __global__ void composite_kernel(PScene Sc, const uint32_t *off, const float4 *q
 // operations and order: volume scale = (T * dt) * (1 / (4/3 pi r^3)),
 // L += e * scale; diffuse scale = (T * (1 / (pi r^2))) * (1 / pi),
 // L += albedo * (e * scale).
-__global__ void composite_exact_kernel(PScene Sc, const uint32_t *off, const float4 *qa,
-                                       const float4 *qd, const float4 *raw, uint32_t npix,
-                                       float exposure, float4 *rad, uchar4 *rgba) {
+__global__ void __launch_bounds__(kListWarps * 32)
+    composite_exact_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
+                           const float4 *raw, uint32_t npix, float exposure, float4 *rad, uchar4 *rgba) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
+    if (pix - (threadIdx.x & 31u) >= npix) return;
     v3 L = mk3(0.f, 0.f, 0.f);
-    const uint32_t end = off[pix + 1];
-    for (uint32_t i = off[pix]; i < end; ++i) {
+    for_pixel_queries(off, pix, npix, [&](uint32_t i) {
         const float4 v = raw[i];
-        if (!(v.w >= 0.0f)) continue;
+        if (!(v.w >= 0.0f)) return;
         const float r2 = v.w;
         const v3 e = mk3(v.x, v.y, v.z);
         const float w = qd[i].w;
@@ -912,7 +949,8 @@ __global__ void composite_exact_kernel(PScene Sc, const uint32_t *off, const flo
             const float scale = w * (1.0f / (3.14159265f * r2)) * 0.318309886f;
             L = L + mk3(a.x * (e.x * scale), a.y * (e.y * scale), a.z * (e.z * scale));
         }
-    }
+    });
+    if (pix >= npix) return;
     if (rad) rad[pix] = make_float4(L.x, L.y, L.z, 1.0f);
     if (rgba)
         rgba[pix] = make_uchar4(to_u8_sat((double)(L.x * exposure) * 255.0),
@@ -1012,7 +1050,7 @@ cudaError_t cache_count_queries(const PScene &S, const RenderParams &R, bool vol
                                 uint32_t *cnt, uint32_t *scnt, cudaStream_t s) {
     const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
     if (npix == 0) return cudaSuccess;
-    count_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, R, vol_on, surf_on, cnt, scnt);
+    count_kernel<<<(npix + kListWarps * 32 - 1) / (kListWarps * 32), kListWarps * 32, 0, s>>>(S, R, vol_on, surf_on, cnt, scnt);
     note_launch();
     return cudaGetLastError();
 }
@@ -1022,7 +1060,7 @@ cudaError_t cache_write_queries(const PScene &S, const RenderParams &R, bool vol
                                 uint32_t *slist, cudaStream_t s) {
     const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
     if (npix == 0) return cudaSuccess;
-    write_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, R, vol_on, surf_on, off, soff, qa, qd, slist);
+    write_kernel<<<(npix + kListWarps * 32 - 1) / (kListWarps * 32), kListWarps * 32, 0, s>>>(S, R, vol_on, surf_on, off, soff, qa, qd, slist);
     note_launch();
     return cudaGetLastError();
 }
@@ -1031,7 +1069,7 @@ cudaError_t cache_composite(const PScene &S, const uint32_t *off, const float4 *
                             const float4 *qd, const float4 *val, uint32_t npix, float exposure,
                             float4 *rad, uchar4 *rgba, cudaStream_t s) {
     if (npix == 0) return cudaSuccess;
-    composite_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, off, qa, qd, val, npix, exposure, rad, rgba);
+    composite_kernel<<<(npix + kListWarps * 32 - 1) / (kListWarps * 32), kListWarps * 32, 0, s>>>(S, off, qa, qd, val, npix, exposure, rad, rgba);
     note_launch();
     return cudaGetLastError();
 }
@@ -1040,7 +1078,7 @@ cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 
                              const float4 *qd, const float4 *raw, uint32_t npix, float exposure,
                              float4 *rad, uchar4 *rgba, cudaStream_t s) {
     if (npix == 0) return cudaSuccess;
-    composite_exact_kernel<<<(npix + 127) / 128, 128, 0, s>>>(S, off, qa, qd, raw, npix, exposure, rad,
+    composite_exact_kernel<<<(npix + kListWarps * 32 - 1) / (kListWarps * 32), kListWarps * 32, 0, s>>>(S, off, qa, qd, raw, npix, exposure, rad,
                                                               rgba);
     note_launch();
     return cudaGetLastError();
@@ -1171,15 +1209,6 @@ cudaError_t cache_table_grad_float(const CacheGrid &g, const CacheParams &p, flo
 
 cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s) {
     weight_image_kernel<<<(kCacheWeights + 255) / 256, 256, 0, s>>>(p.w, p.w_img);
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t cache_pixel_block_order(const uint32_t *off, uint32_t npix, uint32_t *order,
-                                    cudaStream_t s) {
-    if (npix == 0) return cudaSuccess;
-    const uint32_t warps = (npix + 31) / 32;
-    pixel_block_order_kernel<<<(warps + 7) / 8, 256, 0, s>>>(off, npix, order);
     note_launch();
     return cudaGetLastError();
 }

@@ -8,7 +8,11 @@
 //   qa = (x, y, z, object id bits; kNone for a volume query)
 //   qd = (wo.x, wo.y, wo.z, w)     wo toward the viewer, w = transmittance (* dt)
 // whose value -- the k-NN estimate or the network's prediction of it -- is
-// summed per pixel in query order: L = sum w * albedo(obj) * value.
+// summed per pixel in query order: L = sum w * albedo(obj) * value. The
+// list holds each block of 32 consecutive pixels in one contiguous range
+// (from off[first pixel], off the exclusive scan of the per-pixel counts),
+// sample-major within it: the first query of each pixel of the block, then
+// the second ones, ... (pixels in order within a step).
 #pragma once
 #include <cuda_fp16.h>
 #include <cstdint>
@@ -151,10 +155,5 @@ cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float
 cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &S,
                         const float4 *qa, const float4 *qd, const uint32_t *order, uint32_t n,
                         float out_scale, float4 *val, int sm_count, cudaStream_t s);
-// order: every query index once, the queries of each block of 32
-// consecutive pixels (off: the per-pixel exclusive scan, npix + 1 entries)
-// kept in the block's range, sample-major within it.
-cudaError_t cache_pixel_block_order(const uint32_t *off, uint32_t npix, uint32_t *order,
-                                    cudaStream_t s);
 
 }  // namespace pm

@@ -35,9 +35,6 @@ struct CacheState {
     // training order: batch after batch, each every nb-th sorted pick
     float4 *tqa = nullptr, *tqd = nullptr;
     uint32_t *tsel = nullptr;
-    // the order inference takes the render's queries in
-    uint32_t *iorder = nullptr;
-    uint32_t iorder_cap = 0;
     float *scale_sum = nullptr;
     float target_scale = 0.0f;  // 0: set from the first training frame
     unsigned long long steps = 0, frames = 0;
@@ -99,7 +96,7 @@ void free_cache(CacheState *c) {
     cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
     cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.loss_part); cudaFree(c->p.status);
     cudaFree(c->p.w_img); cudaFree(c->p.dx); cudaFree(c->p.xt);
-    cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum); cudaFree(c->iorder);
+    cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum);
     cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
     cudaFree(c->shist); cudaFree(c->sn); cudaFree(c->run_ctr);
     cudaFree(c->pqa); cudaFree(c->pqd); cudaFree(c->pval); cudaFree(c->pord);
@@ -336,15 +333,8 @@ pm_status pm_render_cached(pm_ctx *ctx, float4 *radiance, uchar4 *rgba, int sour
     PM_TRY(cudaEventRecord(c->ev[2], stream));
     if (source == 0) {
         const float scale = c->target_scale > 0.0f ? c->target_scale : 1.0f;
-        if (st->ql.nq > c->iorder_cap) {
-            cudaFree(c->iorder);
-            c->iorder = nullptr;
-            c->iorder_cap = 0;
-            PM_TRY(dalloc(&c->iorder, st->ql.qcap));
-            c->iorder_cap = st->ql.qcap;
-        }
-        PM_TRY(cache_pixel_block_order(st->ql.off, npix, c->iorder, stream));
-        PM_TRY(cache_infer(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, c->iorder, st->ql.nq, scale,
+        // list order: pixel blocks sample-major, neighbouring rays at similar depths
+        PM_TRY(cache_infer(c->grid, c->p, st->dscene, st->ql.qa, st->ql.qd, nullptr, st->ql.nq, scale,
                            st->ql.val, c->sm_count, stream));
         PM_TRY(cudaEventRecord(c->ev[3], stream));
         PM_TRY(cache_composite(st->dscene, st->ql.off, st->ql.qa, st->ql.qd, st->ql.val, npix,

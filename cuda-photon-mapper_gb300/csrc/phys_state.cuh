@@ -13,7 +13,7 @@ struct QueryList {
     uint32_t *scnt = nullptr, *soff = nullptr;  // per pixel: diffuse queries (0 or 1), scan
     uint32_t *slist = nullptr;                  // indices of the diffuse queries
     uint32_t *scan_tmp = nullptr;
-    float4 *qa = nullptr, *qd = nullptr;        // query records
+    float4 *qa = nullptr, *qd = nullptr;        // query records, 32-pixel blocks sample-major
     float4 *val = nullptr;                      // per-query values of the last pass
     int val_owner = 0;                          // who wrote val: 0 nobody, 1 pm_render, 2 cache
     uint32_t qcap = 0, nq = 0, nsurf = 0;

@@ -191,12 +191,12 @@ def test_bounded_wait_gives_up_reports_and_recovers(ctx):
 
 
 def test_cached_values_are_the_network_of_each_query(ctx):
-    """pm_render_cached takes the queries pixel block by pixel block (32
-    consecutive pixels, sample-major within a block); every query's value
-    must still land in its own slot: it equals the network output for that
-    query from the training kernel's forward pass (same weights and table),
-    and not the output of its neighbour in the list. 40 x 40 pixels: blocks
-    that straddle image rows and a short last block."""
+    """The query list holds each block of 32 consecutive pixels
+    sample-major, and pm_render_cached runs inference in list order; every
+    query's value must land in its own slot: it equals the network output
+    for that query from the training kernel's forward pass (same weights
+    and table), and not the output of its neighbour in the list. 40 x 40
+    pixels: blocks that straddle image rows and a short last block."""
     sc, cf = small(2, size=(40, 40))
     frame(ctx, sc, cf)
     ctx.cache_enable(log2_table=12, train_samples=1 << 14, batch=1 << 12)
