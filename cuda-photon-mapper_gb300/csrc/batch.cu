@@ -12,18 +12,24 @@
 //   5. per scene and map, on kBuildStreams side streams: records past the
 //      map's size are set to infinity, then the kd-tree is built over the
 //      map's capacity (so every launch size is a host constant)
-//   6. the render: scenes in query-list mode one after another through the
-//      single-scene render's pipeline -- per-pixel query counts and scans,
-//      query records, (map, Morton) sort, the shared-candidate estimate
-//      pass, the exact composite -- on one buffer set sized at creation
-//      for the largest scene (a scene's query count depends only on its
-//      geometry and camera, so it is known then), with every count the
-//      launches need kept on the device; the other scenes in one
-//      persistent launch over their pixels
+//   6. the render: the scenes in per-pixel mode in one persistent launch
+//      over their pixels; each query-list scene's list (per-pixel counts
+//      and scans, records, (map, Morton) sort) into its slice of one arena
+//      sized at creation (a scene's query count depends only on its
+//      geometry and camera), then one persistent shared-candidate estimate
+//      pass over all of them per k-list width, and each scene's exact
+//      composite, every count the launches need kept on the device
+//   7. with per-scene radiance caches (pm_batch_cache_enable) step 6's
+//      estimate pass is replaced, scene by scene right after its list is
+//      built: the scene's training picks and their k-NN targets, its
+//      network's Adam steps (schedule, target scale and frame counter in
+//      device memory, so replayed frames keep training), inference over
+//      every query of the list and the composite
 // A scene's image equals the single-scene render of the same scene bit for
 // bit: the paths, extents and records are the same, and the k-NN sets do
 // not depend on the tree (records at infinity are never within a radius).
 #include "cache.cuh"
+#include "cache_train.cuh"
 #include "gather.cuh"
 #include "kdtree.cuh"
 #include "launch_count.cuh"
@@ -155,12 +161,42 @@ struct pm_batch {
         uint32_t class_chunks[5] = {};
         bool on = false;
     } ar;
+    std::vector<uint32_t> nsurf;  // diffuse queries per scene
+    // per-scene radiance caches (pm_batch_cache_enable): one network per
+    // scene; the frame's picks and the per-step scratch are shared (scenes
+    // train one after another on the frame's stream)
+    struct SceneCache {
+        CacheGrid grid;
+        CacheParams p;                      // scale_dev and sched point into dev
+        float *dev = nullptr;               // [0] target scale, [1..3] Adam {lr, c1, c2}
+        unsigned long long *ctr = nullptr;  // [0] Adam steps, [1] frames
+    };
+    std::vector<SceneCache> caches;
+    pm_cache_config ccfg;
+    bool cache_on = false;
+    TrainScratch cts;
+    CacheParams cstep;  // the shared step scratch (w_part, loss_part, dx, xt)
 };
 
 namespace {
 
+void free_caches(pm_batch *b) {
+    for (auto &c : b->caches) {
+        CacheParams q = c.p;
+        q.parts_cap = 0;  // the step scratch is shared
+        cache_net_free(q);
+        cudaFree(c.dev);
+        cudaFree(c.ctr);
+    }
+    b->caches.clear();
+    train_scratch_free(b->cts);
+    cache_net_free(b->cstep);
+    b->cache_on = false;
+}
+
 void free_batch(pm_batch *b) {
     if (!b) return;
+    free_caches(b);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (auto &m : b->maps) {
@@ -438,6 +474,45 @@ cudaError_t enqueue_arena_estimates(pm_batch *b, cudaStream_t st) {
     return cudaSuccess;
 }
 
+// Scene s's cached frame, right after its query list was built into the
+// arena (the list of its diffuse queries is then in q.slist): the frame's
+// picks and k-NN targets, the Adam steps of its network, inference over
+// every query and the composite.
+cudaError_t enqueue_scene_cache(pm_batch *b, int s, cudaStream_t st) {
+    auto &ar = b->ar;
+    auto &c = b->caches[s];
+    const pm_cache_config &cf = b->ccfg;
+    const BatchRenderScene d = render_desc(b, s);
+    const pm_config &cfg = b->cfgs[s];
+    const uint32_t npix = (uint32_t)cfg.width * (uint32_t)cfg.height, nq = b->nq[s];
+    if (npix == 0 || nq == 0) return cudaSuccess;
+    float4 *qa = ar.qa + ar.q_off[s], *qd = ar.qd + ar.q_off[s], *val = ar.val + ar.q_off[s];
+    const uint32_t *off = ar.off + ar.p_off[s];
+    TrainScratch &t = b->cts;
+    const uint32_t ns = t.ns;
+    cudaError_t e;
+#define S_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    S_TRY(cache_pick_and_target(cf, c.grid, 0, c.ctr + 1, b->dsc[s], d.surf, d.vol, cfg.k, cfg.radius, qa, qd, nq,
+                                b->q.slist, b->nsurf[s], t, b->sm_count, st));
+    S_TRY(cache_scale_init(t.tgt, ns, t.scale_sum, c.dev, st));
+    S_TRY(cudaMemsetAsync(c.p.loss, 0, sizeof(float), st));
+    const uint32_t nb = cache_batch_count(ns, cf.batch);
+    for (uint32_t i = 0; i < nb; ++i) {
+        uint32_t o, n;
+        cache_batch_range(ns, nb, i, &o, &n);
+        // the scales and the learning rate come from c.dev (the host values are unused)
+        S_TRY(cache_backward(c.grid, c.p, b->dsc[s], t.tqa + o, t.tqd + o, nullptr, t.tgt + o, n, 1.0f,
+                             1.0f / (3.0f * (float)n), cf.loss_eps, nullptr, nullptr, b->sm_count, st));
+        S_TRY(cache_schedule(c.dev + 1, c.ctr, cf.lr, cf.lr_min, cf.lr_half_life, cf.beta1, cf.beta2, st));
+        S_TRY(cache_adam(c.grid, c.p, cf.lr, cf.beta1, cf.beta2, cf.eps, 1, st));
+    }
+    S_TRY(cache_count_up(c.ctr + 1, st));
+    S_TRY(cache_infer(c.grid, c.p, b->dsc[s], qa, qd, nullptr, nq, 1.0f, val, b->sm_count, st));
+    S_TRY(cache_composite(d.sc, off, qa, qd, val, npix, cfg.exposure, d.rad, d.rgba, st));
+#undef S_TRY
+    return cudaSuccess;
+}
+
 // Counts every scene's queries (they depend on its geometry and camera
 // only) and sizes the query buffers for the largest scene.
 cudaError_t size_query_buffers(pm_batch *b) {
@@ -454,6 +529,7 @@ cudaError_t size_query_buffers(pm_batch *b) {
     Z_TRY(dalloc(&q.scan_tmp, scan_tile_count((uint32_t)max_pix) + 1));
     q.pix_cap = max_pix;
     b->nq.assign(b->n, 0u);
+    b->nsurf.assign(b->n, 0u);
     size_t max_q = 1;
     for (int s = 0; s < b->n; ++s) {
         const BatchRenderScene d = render_desc(b, s);
@@ -464,6 +540,8 @@ cudaError_t size_query_buffers(pm_batch *b) {
         Z_TRY(cache_count_queries(d.sc, d.R, vol_on, surf_on, q.cnt, q.scnt, 0));
         Z_TRY(exclusive_scan_u32_large(q.cnt, q.off, npix, q.off + npix, q.scan_tmp, 0));
         Z_TRY(cudaMemcpy(&b->nq[s], q.off + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        Z_TRY(exclusive_scan_u32_large(q.scnt, q.soff, npix, q.soff + npix, q.scan_tmp, 0));
+        Z_TRY(cudaMemcpy(&b->nsurf[s], q.soff + npix, sizeof(uint32_t), cudaMemcpyDeviceToHost));
         max_q = std::max(max_q, (size_t)b->nq[s]);
     }
     Z_TRY(dalloc(&q.qa, max_q));
@@ -570,9 +648,12 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
         B_TRY(cudaStreamWaitEvent(st, b->join[k], 0));
     }
     if (b->n_pixel > 0) B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n_pixel, b->work, b->sm_count, st));
-    for (int s = 0; s < b->n; ++s)
-        if (b->tune[s].query_list) B_TRY(enqueue_arena_queries(b, s, st));
-    B_TRY(enqueue_arena_estimates(b, st));
+    for (int s = 0; s < b->n; ++s) {
+        if (!b->tune[s].query_list) continue;
+        B_TRY(enqueue_arena_queries(b, s, st));
+        if (b->cache_on) B_TRY(enqueue_scene_cache(b, s, st));
+    }
+    if (!b->cache_on) B_TRY(enqueue_arena_estimates(b, st));
 #undef B_TRY
     return cudaSuccess;
 }
@@ -821,6 +902,8 @@ pm_status pm_batch_set_tune(pm_batch *b, int scene, const pm_batch_tune *t) {
         t->tile > 64 || (t->collect_max != 32 && t->collect_max != 64 && t->collect_max != 128) ||
         t->merge_min < 1 || t->merge_min > 33 || (t->query_list != 0 && t->query_list != 1))
         return fail(b->ctx, PM_ERR_INVALID, "invalid batch tune");
+    if (b->cache_on && !t->query_list)
+        return fail(b->ctx, PM_ERR_STATE, "per-scene radiance caches need the query-list render");
     DeviceGuard g(b->ctx->device);
     cudaDeviceSynchronize();
     b->tune[scene] = *t;
@@ -836,8 +919,71 @@ pm_status pm_batch_get_tune(pm_batch *b, int scene, pm_batch_tune *t) {
     return PM_OK;
 }
 
+pm_status pm_batch_cache_enable(pm_batch *b, const pm_cache_config *cfg_in) {
+    if (!b) return PM_ERR_INVALID;
+    pm_cache_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else pm_cache_default_config(&cfg);
+    if (!cache_config_ok(cfg)) return fail(b->ctx, PM_ERR_INVALID, "invalid radiance-cache configuration");
+    DeviceGuard g(b->ctx->device);
+    cudaDeviceSynchronize();
+    drop_graph(b);
+    free_caches(b);
+    cudaError_t e;
+#define E_TRY(x) do { e = (x); if (e != cudaSuccess) { free_caches(b); return check_cuda(b->ctx, e, #x); } } while (0)
+    b->ccfg = cfg;
+    E_TRY(train_scratch_alloc(cfg.train_samples, &b->cts));
+    // the shared step scratch: a network without table or weights of its own
+    {
+        CacheParams &q = b->cstep;
+        memset(&q, 0, sizeof(q));
+        q.parts_cap = b->sm_count;
+        E_TRY(dalloc(&q.w_part, (size_t)q.parts_cap * kCacheWeights));
+        E_TRY(dalloc(&q.loss_part, q.parts_cap));
+        q.dx_cap = cfg.batch;
+        E_TRY(dalloc(&q.dx, (size_t)cfg.batch * 8));
+        E_TRY(dalloc(&q.xt, (size_t)cfg.batch * 8));
+    }
+    b->caches.resize(b->n);
+    for (int s = 0; s < b->n; ++s) {
+        auto &c = b->caches[s];
+        cache_grid_init(cfg, &c.grid);
+        cache_grid_box(c.grid, b->scenes[s]);
+        E_TRY(cache_net_alloc(cfg, c.grid, cfg.seed + (uint64_t)s, 0, &c.p));
+        E_TRY(dalloc(&c.dev, 4));
+        E_TRY(dalloc(&c.ctr, 2));
+        E_TRY(cudaMemset(c.dev, 0, sizeof(float) * 4));
+        E_TRY(cudaMemset(c.ctr, 0, sizeof(unsigned long long) * 2));
+        c.p.scale_dev = c.dev;
+        c.p.sched = c.dev + 1;
+        c.p.parts_cap = b->cstep.parts_cap;
+        c.p.w_part = b->cstep.w_part;
+        c.p.loss_part = b->cstep.loss_part;
+        c.p.dx_cap = b->cstep.dx_cap;
+        c.p.dx = b->cstep.dx;
+        c.p.xt = b->cstep.xt;
+        // the cache renders through the query list
+        b->tune[s].query_list = 1;
+    }
+    E_TRY(upload_pixel_scenes(b));
+    E_TRY(cudaDeviceSynchronize());
+#undef E_TRY
+    b->cache_on = true;
+    return PM_OK;
+}
+
+pm_status pm_batch_cache_disable(pm_batch *b) {
+    if (!b) return PM_ERR_INVALID;
+    DeviceGuard g(b->ctx->device);
+    cudaDeviceSynchronize();
+    drop_graph(b);
+    free_caches(b);
+    return PM_OK;
+}
+
 pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t stream) {
     if (!b) return PM_ERR_INVALID;
+    if (b->cache_on) return fail(b->ctx, PM_ERR_STATE, "pm_batch_autotune with per-scene radiance caches on");
     DeviceGuard g(b->ctx->device);
     pm_ctx *ctx = b->ctx;
     cudaError_t e;

@@ -435,7 +435,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int j = 0; j < 16; ++j) gy[j] = 0.0f;
         if (valid) {
             const float4 t4 = val[i];
-            const float t[3] = {t4.x * inv_scale, t4.y * inv_scale, t4.z * inv_scale};
+            const float isc = p.scale_dev ? 1.0f / __ldg(p.scale_dev) : inv_scale;
+            const float t[3] = {t4.x * isc, t4.y * isc, t4.z * isc};
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const float diff = y[c] - t[c];
@@ -609,9 +610,10 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
         });
         float y[16];
         tmem_ld16(taddr, 0, y);
-        if (valid && ok)
-            val[i] = make_float4(fmaxf(y[0], 0.0f) * out_scale, fmaxf(y[1], 0.0f) * out_scale,
-                                 fmaxf(y[2], 0.0f) * out_scale, 0.0f);
+        if (valid && ok) {
+            const float osc = p.scale_dev ? __ldg(p.scale_dev) : out_scale;
+            val[i] = make_float4(fmaxf(y[0], 0.0f) * osc, fmaxf(y[1], 0.0f) * osc, fmaxf(y[2], 0.0f) * osc, 0.0f);
+        }
         if (!ok) abort_s[pipe] = 1;
         asm volatile("tcgen05.fence::before_thread_sync;");
         named_sync(bar, kThreads);
@@ -628,7 +630,12 @@ __global__ void __launch_bounds__(kThreads * kInferPipes)
 
 __global__ void adam_kernel(float *p, float *gr, float *m, float *v, __half2 *ph, uint32_t npairs,
                             float lr, float b1, float b2, float eps, float c1, float c2, bool lazy,
-                            uint4 *w_img) {
+                            uint4 *w_img, const float *sched) {
+    if (sched) {
+        lr = sched[0];
+        c1 = sched[1];
+        c2 = sched[2];
+    }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
         const float2 gg = reinterpret_cast<float2 *>(gr)[i];
         if (lazy && gg.x == 0.0f && gg.y == 0.0f) continue;
@@ -716,7 +723,12 @@ __global__ void __launch_bounds__(kCacheMaxLevels * 32) table_scatter_kernel(Cac
 // and their sums cleared.
 __global__ void adam_table_kernel(float *p, longlong2 *gr, float *m, float *v, __half2 *ph,
                                   uint32_t npairs, float lr, float b1, float b2, float eps, float c1,
-                                  float c2) {
+                                  float c2, const float *sched) {
+    if (sched) {
+        lr = sched[0];
+        c1 = sched[1];
+        c2 = sched[2];
+    }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
         const longlong2 q = gr[i];
         if (q.x == 0 && q.y == 0) continue;
@@ -958,10 +970,12 @@ __global__ void __launch_bounds__(kListWarps * 32)
                                 to_u8_sat((double)(L.z * exposure) * 255.0), 255);
 }
 
-__global__ void select_kernel(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
-                              uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel) {
+__global__ void select_kernel(uint64_t seed, uint32_t frame, const unsigned long long *frame_dev, uint32_t total,
+                              const uint32_t *slist, uint32_t ns_total, uint32_t n, float surf_frac,
+                              uint32_t *sel) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (frame_dev) frame = (uint32_t)*frame_dev;
     const pm_u32x4 r = philox(seed, i, frame, 0x5E1Eu, 0u);
     if (ns_total > 0 && pm_u01(r.v[1]) < surf_frac)
         sel[i] = slist[(uint32_t)(((uint64_t)r.v[0] * ns_total) >> 32)];
@@ -1028,8 +1042,10 @@ __global__ void iota_kernel(uint32_t *v, uint32_t n) {
 // index order, then a fixed reduction tree; the result does not depend on
 // scheduling.
 constexpr int kSumThreads = 1024;
-__global__ void __launch_bounds__(kSumThreads) value_sum_kernel(const float4 *val, uint32_t n, float *sum) {
+__global__ void __launch_bounds__(kSumThreads) value_sum_kernel(const float4 *val, uint32_t n, float *sum,
+                                                               const float *skip_if_set) {
     __shared__ float red[kSumThreads];
+    if (skip_if_set && *skip_if_set > 0.0f) return;
     float acc = 0.0f;
     for (uint32_t i = threadIdx.x; i < n; i += kSumThreads) {
         const float4 v = val[i];
@@ -1042,6 +1058,27 @@ __global__ void __launch_bounds__(kSumThreads) value_sum_kernel(const float4 *va
         __syncthreads();
     }
     if (threadIdx.x == 0) *sum = red[0];
+}
+
+__global__ void count_up_kernel(unsigned long long *c) { ++*c; }
+
+__global__ void scale_init_kernel(const float *sum, uint32_t n, float *scale) {
+    if (*scale > 0.0f) return;
+    const float mean = *sum / (float)n;
+    *scale = mean > 0.0f && isfinite(mean) ? mean : 1.0f;
+}
+
+__global__ void schedule_kernel(float *sched, unsigned long long *step, float lr0, float lr_min, float half_life,
+                                float b1, float b2) {
+    const unsigned long long s0 = *step;
+    float lr = lr0;
+    if (half_life > 0.0f) lr = lr_min + (lr0 - lr_min) * (float)exp2(-(double)s0 / (double)half_life);
+    const unsigned long long s1 = s0 + 1;
+    const float sf = (float)(s1 < (1ull << 30) ? s1 : (1ull << 30));
+    sched[0] = lr;
+    sched[1] = 1.0f / (1.0f - powf(b1, sf));
+    sched[2] = 1.0f / (1.0f - powf(b2, sf));
+    *step = s1;
 }
 
 }  // namespace
@@ -1103,9 +1140,10 @@ cudaError_t cache_train_order(const float4 *pqa, const float4 *pqd, const float4
 
 cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
                          uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel,
-                         cudaStream_t s) {
+                         cudaStream_t s, const unsigned long long *frame_dev) {
     if (n == 0) return cudaSuccess;
-    select_kernel<<<(n + 255) / 256, 256, 0, s>>>(seed, frame, total, slist, ns_total, n, surf_frac, sel);
+    select_kernel<<<(n + 255) / 256, 256, 0, s>>>(seed, frame, frame_dev, total, slist, ns_total, n, surf_frac,
+                                                  sel);
     note_launch();
     return cudaGetLastError();
 }
@@ -1127,7 +1165,29 @@ cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s) {
 
 cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    value_sum_kernel<<<1, kSumThreads, 0, s>>>(val, n, sum);
+    value_sum_kernel<<<1, kSumThreads, 0, s>>>(val, n, sum, nullptr);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_scale_init(const float4 *val, uint32_t n, float *sum, float *scale, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    value_sum_kernel<<<1, kSumThreads, 0, s>>>(val, n, sum, scale);
+    note_launch();
+    scale_init_kernel<<<1, 1, 0, s>>>(sum, n, scale);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_count_up(unsigned long long *c, cudaStream_t s) {
+    count_up_kernel<<<1, 1, 0, s>>>(c);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_schedule(float *sched, unsigned long long *step, float lr0, float lr_min, float half_life,
+                           float beta1, float beta2, cudaStream_t s) {
+    schedule_kernel<<<1, 1, 0, s>>>(sched, step, lr0, lr_min, half_life, beta1, beta2);
     note_launch();
     return cudaGetLastError();
 }
@@ -1190,11 +1250,11 @@ cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float
     const uint32_t tpairs = (uint32_t)(((size_t)g.levels << g.log2_t));
     adam_table_kernel<<<2048, 256, 0, s>>>(p.table, reinterpret_cast<longlong2 *>(p.table_grad),
                                            p.table_m, p.table_v, p.table_h, tpairs, lr, beta1, beta2, eps,
-                                           c1, c2);
+                                           c1, c2, p.sched);
     note_launch();
     adam_kernel<<<(kCacheWeights / 2 + 255) / 256, 256, 0, s>>>(p.w, p.w_grad, p.w_m, p.w_v, nullptr,
                                                                 kCacheWeights / 2, lr, beta1, beta2,
-                                                                eps, c1, c2, false, p.w_img);
+                                                                eps, c1, c2, false, p.w_img, p.sched);
     note_launch();
     return cudaGetLastError();
 }

@@ -65,6 +65,12 @@ struct CacheParams {
     uint32_t dx_cap;       // samples dx and xt hold (a multiple of 128)
     int *status;           // set when a bounded tensor-core wait runs out
     uint32_t wait_polls;   // first bound of every mbarrier wait (kMbarSpin unless lowered for a test)
+    // Device-side training state for frames replayed from a CUDA graph
+    // (nullable; the host values passed to the calls are used otherwise):
+    // the target scale (training divides targets by it, inference
+    // multiplies outputs by it) and the Adam step's {lr, c1, c2}.
+    const float *scale_dev = nullptr;
+    const float *sched = nullptr;
 };
 
 // Per-pixel query counts and diffuse-query counts (0 or 1) (count pass);
@@ -121,9 +127,12 @@ cudaError_t cache_iota(uint32_t *v, uint32_t n, cudaStream_t s);
 // Training picks from Philox(seed, frame, i): with probability surf_frac
 // uniform over the diffuse queries slist[0..ns_total), else uniform over
 // all `total` queries.
+// With frame_dev (nullable), the frame number is read from device memory.
 cudaError_t cache_select(uint64_t seed, uint32_t frame, uint32_t total, const uint32_t *slist,
                          uint32_t ns_total, uint32_t n, float surf_frac, uint32_t *sel,
-                         cudaStream_t s);
+                         cudaStream_t s, const unsigned long long *frame_dev = nullptr);
+// ++*c on the device (a frame counter kept in device memory).
+cudaError_t cache_count_up(unsigned long long *c, cudaStream_t s);
 // *sum = mean over rgb of val[0..n), summed in a fixed order.
 cudaError_t cache_value_sum(const float4 *val, uint32_t n, float *sum, cudaStream_t s);
 
@@ -150,6 +159,16 @@ cudaError_t cache_weight_image(const CacheParams &p, cudaStream_t s);
 // steps and refresh p.w_img.
 cudaError_t cache_adam(const CacheGrid &g, const CacheParams &p, float lr, float beta1,
                        float beta2, float eps, int step, cudaStream_t s);
+// The Adam schedule on the device (one thread): sched = {lr, c1, c2} for
+// the step after *step (lr = lr_min + (lr0 - lr_min) 2^(-step / half_life),
+// or lr0 when half_life <= 0; c1, c2 the bias corrections of the step
+// count after it), and *step advanced.
+cudaError_t cache_schedule(float *sched, unsigned long long *step, float lr0, float lr_min, float half_life,
+                           float beta1, float beta2, cudaStream_t s);
+// *scale, if still 0, set to the mean over rgb of val[0..n) (1 when that is
+// not positive and finite); sum is one word of scratch. Does nothing once
+// the scale is set, so a replayed frame keeps the first frame's scale.
+cudaError_t cache_scale_init(const float4 *val, uint32_t n, float *sum, float *scale, cudaStream_t s);
 // val[i] = max(network(query i), 0) * out_scale for the first n queries,
 // taken in the order order[0..n) (nullable: index order).
 cudaError_t cache_infer(const CacheGrid &g, const CacheParams &p, const PScene &S,

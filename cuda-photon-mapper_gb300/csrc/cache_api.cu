@@ -2,6 +2,7 @@
 // configuration, the per-camera query list, online training frames, cached
 // and k-NN renders through the query list, parameter access and files.
 #include "cache.cuh"
+#include "cache_train.cuh"
 #include "phys_state.cuh"
 #include "pm_ctx.cuh"
 #include "radix_sort.cuh"
@@ -20,22 +21,9 @@ struct CacheState {
     pm::CacheParams p;
     size_t table_floats = 0;
     int sm_count = 148;
-    // the query list itself lives in the physical state (shared with pm_render)
-    // training
-    uint32_t *sel = nullptr;
-    float4 *tgt = nullptr;
-    // the frame's picks sorted by (map, Morton code) for coherent k-NN
-    // targets, and their positions in the random order training reads
-    uint32_t *skey = nullptr, *sval = nullptr, *skey_tmp = nullptr, *sval_tmp = nullptr;
-    uint32_t *shist = nullptr, *sn = nullptr;
-    uint32_t *run_ctr = nullptr;  // the target launch's run counter
-    // the sorted picks' records, identity order and targets
-    float4 *pqa = nullptr, *pqd = nullptr, *pval = nullptr;
-    uint32_t *pord = nullptr;
-    // training order: batch after batch, each every nb-th sorted pick
-    float4 *tqa = nullptr, *tqd = nullptr;
-    uint32_t *tsel = nullptr;
-    float *scale_sum = nullptr;
+    // the query list itself lives in the physical state (shared with pm_render);
+    // the frame's picks and targets
+    pm::TrainScratch ts;
     float target_scale = 0.0f;  // 0: set from the first training frame
     unsigned long long steps = 0, frames = 0;
     cudaEvent_t ev[7] = {};  // queries start/end, values start, values end/composite start, composite end, train mid/end
@@ -45,41 +33,169 @@ struct CacheState {
 };
 
 namespace pm {
-namespace {
 
 constexpr int kTargetRun = 8;  // training targets warm-started in runs of this length
 
-// Training batches of a frame of ns picks: as many as batches of `batch`
-// need, every one a spatially stratified sample (cache_train_order).
-uint32_t batch_count(uint32_t ns, uint32_t batch) { return (ns + batch - 1) / batch; }
+namespace {
+template <typename T>
+cudaError_t talloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, sizeof(T) * count);
+}
+}  // namespace
 
-// The frame's training picks (uniform, stratified between diffuse and
-// volume queries) and their k-NN targets, in training order: c->tqa, c->tqd
-// the picks' records, c->tgt their targets, c->tsel their queries. The
-// picks are sorted by (map, Morton code), their records gathered in that
-// order, and estimated in runs of kTargetRun warm-started list searches
-// (the volume picks, a few per cent of the volume queries, are too far
-// apart to share candidate sets; measured on the diffuse picks too, the
-// shared-candidate pass was slower than the runs). Then batch b takes every
-// nb-th sorted pick.
-cudaError_t pick_and_target(PhysicalState *st, CacheState *c, cudaStream_t stream) {
-    const uint32_t ns = c->cfg.train_samples;
+cudaError_t train_scratch_alloc(uint32_t ns, TrainScratch *t) {
+    cudaError_t e;
+#define TS_TRY(x) do { e = (x); if (e != cudaSuccess) { train_scratch_free(*t); return e; } } while (0)
+    *t = TrainScratch();
+    t->ns = ns;
+    TS_TRY(talloc(&t->sel, ns));
+    TS_TRY(talloc(&t->skey, ns));
+    TS_TRY(talloc(&t->sval, ns));
+    TS_TRY(talloc(&t->skey_tmp, ns));
+    TS_TRY(talloc(&t->sval_tmp, ns));
+    TS_TRY(talloc(&t->shist, radix_sort_hist_words(ns)));
+    TS_TRY(talloc(&t->sn, 1));
+    TS_TRY(talloc(&t->run_ctr, 1));
+    TS_TRY(talloc(&t->pqa, ns));
+    TS_TRY(talloc(&t->pqd, ns));
+    TS_TRY(talloc(&t->pval, ns));
+    TS_TRY(talloc(&t->pord, ns));
+    TS_TRY(talloc(&t->tqa, ns));
+    TS_TRY(talloc(&t->tqd, ns));
+    TS_TRY(talloc(&t->tgt, ns));
+    TS_TRY(talloc(&t->tsel, ns));
+    TS_TRY(talloc(&t->scale_sum, 1));
+    TS_TRY(cudaMemcpy(t->sn, &ns, sizeof(uint32_t), cudaMemcpyHostToDevice));
+#undef TS_TRY
+    return cudaSuccess;
+}
+
+void train_scratch_free(TrainScratch &t) {
+    cudaFree(t.sel); cudaFree(t.skey); cudaFree(t.sval); cudaFree(t.skey_tmp); cudaFree(t.sval_tmp);
+    cudaFree(t.shist); cudaFree(t.sn); cudaFree(t.run_ctr);
+    cudaFree(t.pqa); cudaFree(t.pqd); cudaFree(t.pval); cudaFree(t.pord);
+    cudaFree(t.tqa); cudaFree(t.tqd); cudaFree(t.tgt); cudaFree(t.tsel); cudaFree(t.scale_sum);
+    t = TrainScratch();
+}
+
+bool cache_config_ok(const pm_cache_config &cfg) {
+    return !(cfg.levels < 1 || cfg.levels > kCacheMaxLevels || cfg.log2_table < 8 || cfg.log2_table > 22 ||
+             cfg.base_res < 2 || cfg.max_res < cfg.base_res || cfg.max_res > 65536 ||
+             cfg.train_samples < 1 || cfg.train_samples > (1u << 24) || cfg.batch < 128 ||
+             cfg.batch % 128 != 0 || !(cfg.lr > 0.0f) || !(cfg.beta1 >= 0.0f && cfg.beta1 < 1.0f) ||
+             !(cfg.beta2 >= 0.0f && cfg.beta2 < 1.0f) || !(cfg.eps >= 0.0f) ||
+             !(cfg.lr_min >= 0.0f) || !(cfg.lr_half_life >= 0.0f) || !(cfg.loss_eps > 0.0f) ||
+             !(cfg.surface_fraction >= 0.0f && cfg.surface_fraction <= 1.0f));
+}
+
+void cache_grid_init(const pm_cache_config &cfg, CacheGrid *g) {
+    memset(g, 0, sizeof(*g));
+    g->levels = cfg.levels;
+    g->log2_t = (uint32_t)cfg.log2_table;
+    const double b = cfg.levels > 1 ? std::exp(std::log((double)cfg.max_res / cfg.base_res) / (cfg.levels - 1)) : 1.0;
+    for (int l = 0; l < cfg.levels; ++l) g->res[l] = (int)std::floor(cfg.base_res * std::pow(b, l) + 1e-6);
+    for (int a = 0; a < 3; ++a) {
+        g->lo[a] = 0.0f;
+        g->inv_size[a] = 1.0f;
+    }
+}
+
+void cache_grid_box(CacheGrid &g, const pm_scene &sc) {
+    for (int a = 0; a < 3; ++a) {
+        const float ext = sc.box_max[a] - sc.box_min[a];
+        const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
+        g.lo[a] = sc.box_min[a] - m;
+        const float size = ext + 2.0f * m;
+        g.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
+    }
+}
+
+size_t cache_table_floats(const pm_cache_config &cfg) { return (size_t)cfg.levels << (cfg.log2_table + 1); }
+
+cudaError_t cache_net_alloc(const pm_cache_config &cfg, const CacheGrid &g, uint64_t seed, int parts_cap,
+                            CacheParams *out) {
+    CacheParams p;
+    memset(&p, 0, sizeof(p));
+    const size_t tf = cache_table_floats(cfg);
+    cudaError_t e;
+#define NA_TRY(x) do { e = (x); if (e != cudaSuccess) { cache_net_free(p); return e; } } while (0)
+    NA_TRY(talloc(&p.w, kCacheWeights));
+    NA_TRY(talloc(&p.w_grad, kCacheWeights));
+    NA_TRY(talloc(&p.w_m, kCacheWeights));
+    NA_TRY(talloc(&p.w_v, kCacheWeights));
+    NA_TRY(talloc(&p.table, tf));
+    NA_TRY(talloc(&p.table_grad, tf));
+    NA_TRY(talloc(&p.table_m, tf));
+    NA_TRY(talloc(&p.table_v, tf));
+    NA_TRY(talloc(&p.table_h, tf / 2));
+    NA_TRY(talloc(&p.w_img, kCacheWImageBytes / 16));
+    NA_TRY(talloc(&p.loss, 1));
+    NA_TRY(talloc(&p.status, 1));
+    NA_TRY(cudaMemset(p.status, 0, sizeof(int)));
+    if (parts_cap > 0) {
+        p.parts_cap = parts_cap;
+        NA_TRY(talloc(&p.w_part, (size_t)parts_cap * kCacheWeights));
+        NA_TRY(talloc(&p.loss_part, parts_cap));
+        p.dx_cap = cfg.batch;
+        NA_TRY(talloc(&p.dx, (size_t)cfg.batch * 8));
+        NA_TRY(talloc(&p.xt, (size_t)cfg.batch * 8));
+    }
+    p.wait_polls = kMbarSpin;
+    NA_TRY(cache_init(g, p, seed, 0));
+#undef NA_TRY
+    *out = p;
+    return cudaSuccess;
+}
+
+void cache_net_free(CacheParams &p) {
+    cudaFree(p.w); cudaFree(p.w_grad); cudaFree(p.w_m); cudaFree(p.w_v);
+    cudaFree(p.table); cudaFree(p.table_grad); cudaFree(p.table_m); cudaFree(p.table_v); cudaFree(p.table_h);
+    cudaFree(p.w_img); cudaFree(p.loss); cudaFree(p.status);
+    if (p.parts_cap > 0) {
+        cudaFree(p.w_part); cudaFree(p.loss_part); cudaFree(p.dx); cudaFree(p.xt);
+    }
+    memset(&p, 0, sizeof(p));
+}
+
+uint32_t cache_batch_count(uint32_t ns, uint32_t batch) { return (ns + batch - 1) / batch; }
+
+void cache_batch_range(uint32_t ns, uint32_t nb, uint32_t b, uint32_t *o, uint32_t *n) {
+    *o = b * (ns / nb) + std::min(b, ns % nb);
+    *n = ns / nb + (b < ns % nb ? 1u : 0u);
+}
+
+cudaError_t cache_pick_and_target(const pm_cache_config &cfg, const CacheGrid &grid, uint32_t frame,
+                                  const unsigned long long *frame_dev, const PScene &S, const MapView &surf,
+                                  const MapView &vol, int k, float radius, const float4 *qa, const float4 *qd,
+                                  uint32_t nq, const uint32_t *slist, uint32_t nsurf, TrainScratch &t,
+                                  int sm_count, cudaStream_t stream) {
+    const uint32_t ns = t.ns;
     cudaError_t e;
 #define CT_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
-    CT_TRY(cache_select(c->cfg.seed, (uint32_t)c->frames, st->ql.nq, st->ql.slist, st->ql.nsurf, ns,
-                        c->cfg.surface_fraction, c->sel, stream));
-    CT_TRY(cache_sample_keys(c->grid, st->ql.qa, c->sel, ns, c->skey, c->sval, stream));
+    CT_TRY(cache_select(cfg.seed, frame, nq, slist, nsurf, ns, cfg.surface_fraction, t.sel, stream, frame_dev));
+    CT_TRY(cache_sample_keys(grid, qa, t.sel, ns, t.skey, t.sval, stream));
     uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
-    CT_TRY(radix_sort_pairs_u32(c->skey, c->sval, c->skey_tmp, c->sval_tmp, c->sn, ns, 0, 31, c->shist,
-                                stream, &ok_keys, &ok_vals));
-    CT_TRY(cache_pick_records(ok_vals, c->sel, st->ql.qa, st->ql.qd, ns, c->pqa, c->pqd, c->pord, stream));
-    CT_TRY(cache_knn_values_runs(st->dscene, view_of(st->map[0]), view_of(st->map[1]), c->pqa, c->pqd, nullptr,
-                                 c->pord, ns, kTargetRun, st->cfg.k, st->cfg.radius, false, c->pval, c->run_ctr,
-                                 c->sm_count, stream));
-    CT_TRY(cache_train_order(c->pqa, c->pqd, c->pval, ok_vals, c->sel, ns, batch_count(ns, c->cfg.batch),
-                             c->tqa, c->tqd, c->tgt, c->tsel, stream));
+    CT_TRY(radix_sort_pairs_u32(t.skey, t.sval, t.skey_tmp, t.sval_tmp, t.sn, ns, 0, 31, t.shist, stream, &ok_keys,
+                                &ok_vals));
+    CT_TRY(cache_pick_records(ok_vals, t.sel, qa, qd, ns, t.pqa, t.pqd, t.pord, stream));
+    CT_TRY(cache_knn_values_runs(S, surf, vol, t.pqa, t.pqd, nullptr, t.pord, ns, kTargetRun, k, radius, false,
+                                 t.pval, t.run_ctr, sm_count, stream));
+    CT_TRY(cache_train_order(t.pqa, t.pqd, t.pval, ok_vals, t.sel, ns, cache_batch_count(ns, cfg.batch), t.tqa,
+                             t.tqd, t.tgt, t.tsel, stream));
 #undef CT_TRY
     return cudaSuccess;
+}
+
+namespace {
+
+// The frame's training picks of the installed query list and their k-NN
+// targets, in training order (cache_pick_and_target).
+cudaError_t pick_and_target(PhysicalState *st, CacheState *c, cudaStream_t stream) {
+    return cache_pick_and_target(c->cfg, c->grid, (uint32_t)c->frames, nullptr, st->dscene, view_of(st->map[0]),
+                                 view_of(st->map[1]), st->cfg.k, st->cfg.radius, st->ql.qa, st->ql.qd, st->ql.nq,
+                                 st->ql.slist, st->ql.nsurf, c->ts, c->sm_count, stream);
 }
 
 template <typename T>
@@ -91,31 +207,12 @@ cudaError_t dalloc(T **p, size_t count) {
 
 void free_cache(CacheState *c) {
     if (!c) return;
-    cudaFree(c->p.w); cudaFree(c->p.w_grad); cudaFree(c->p.w_m); cudaFree(c->p.w_v);
-    cudaFree(c->p.w_part);
-    cudaFree(c->p.table); cudaFree(c->p.table_grad); cudaFree(c->p.table_m); cudaFree(c->p.table_v);
-    cudaFree(c->p.table_h); cudaFree(c->p.loss); cudaFree(c->p.loss_part); cudaFree(c->p.status);
-    cudaFree(c->p.w_img); cudaFree(c->p.dx); cudaFree(c->p.xt);
-    cudaFree(c->sel); cudaFree(c->tgt); cudaFree(c->scale_sum);
-    cudaFree(c->skey); cudaFree(c->sval); cudaFree(c->skey_tmp); cudaFree(c->sval_tmp);
-    cudaFree(c->shist); cudaFree(c->sn); cudaFree(c->run_ctr);
-    cudaFree(c->pqa); cudaFree(c->pqd); cudaFree(c->pval); cudaFree(c->pord);
-    cudaFree(c->tqa); cudaFree(c->tqd); cudaFree(c->tsel);
+    cache_net_free(c->p);
+    train_scratch_free(c->ts);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->tev0) cudaEventDestroy(c->tev0);
     delete c;
-}
-
-// World box of the scene (walls included) -> [0,1]^3, with a 1 % margin.
-void set_grid_box(CacheGrid &g, const pm_scene &sc) {
-    for (int a = 0; a < 3; ++a) {
-        const float ext = sc.box_max[a] - sc.box_min[a];
-        const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
-        g.lo[a] = sc.box_min[a] - m;
-        const float size = ext + 2.0f * m;
-        g.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
-    }
 }
 
 // Builds the query list of the installed camera unless it is current
@@ -125,7 +222,7 @@ pm_status ensure_queries(pm_ctx *ctx, PhysicalState *st, CacheState *c, cudaStre
     cudaError_t e = query_list_build(st, force, stream);
     if (e != cudaSuccess) return check_cuda(ctx, e, "query_list_build");
     c->stats.ms_queries = 0.0f;
-    set_grid_box(c->grid, st->scene);
+    cache_grid_box(c->grid, st->scene);
     return PM_OK;
 }
 
@@ -179,14 +276,7 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     pm_cache_config cfg;
     if (cfg_in) cfg = *cfg_in;
     else pm_cache_default_config(&cfg);
-    if (cfg.levels < 1 || cfg.levels > kCacheMaxLevels || cfg.log2_table < 8 || cfg.log2_table > 22 ||
-        cfg.base_res < 2 || cfg.max_res < cfg.base_res || cfg.max_res > 65536 ||
-        cfg.train_samples < 1 || cfg.train_samples > (1u << 24) || cfg.batch < 128 ||
-        cfg.batch % 128 != 0 || !(cfg.lr > 0.0f) || !(cfg.beta1 >= 0.0f && cfg.beta1 < 1.0f) ||
-        !(cfg.beta2 >= 0.0f && cfg.beta2 < 1.0f) || !(cfg.eps >= 0.0f) ||
-        !(cfg.lr_min >= 0.0f) || !(cfg.lr_half_life >= 0.0f) || !(cfg.loss_eps > 0.0f) ||
-        !(cfg.surface_fraction >= 0.0f && cfg.surface_fraction <= 1.0f))
-        return fail(ctx, PM_ERR_INVALID, "invalid radiance-cache configuration");
+    if (!cache_config_ok(cfg)) return fail(ctx, PM_ERR_INVALID, "invalid radiance-cache configuration");
     DeviceGuard g(ctx->device);
     cache_free(ctx);
     CacheState *c = new CacheState();
@@ -195,58 +285,15 @@ pm_status pm_cache_enable(pm_ctx *ctx, const pm_cache_config *cfg_in) {
     memset(&c->stats, 0, sizeof(c->stats));
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
     CacheGrid &gr = c->grid;
-    memset(&gr, 0, sizeof(gr));
-    gr.levels = cfg.levels;
-    gr.log2_t = (uint32_t)cfg.log2_table;
-    const double b = cfg.levels > 1 ? std::exp(std::log((double)cfg.max_res / cfg.base_res) / (cfg.levels - 1)) : 1.0;
-    for (int l = 0; l < cfg.levels; ++l) gr.res[l] = (int)std::floor(cfg.base_res * std::pow(b, l) + 1e-6);
-    for (int a = 0; a < 3; ++a) { gr.lo[a] = 0.0f; gr.inv_size[a] = 1.0f; }
-    if (ctx->phys) set_grid_box(gr, ctx->phys->scene);
-    c->table_floats = (size_t)cfg.levels << (cfg.log2_table + 1);
+    cache_grid_init(cfg, &gr);
+    if (ctx->phys) cache_grid_box(gr, ctx->phys->scene);
+    c->table_floats = cache_table_floats(cfg);
     cudaError_t e;
 #define PM_TRY_FREE(x) do { e = (x); if (e != cudaSuccess) { cache_free(ctx); return check_cuda(ctx, e, #x); } } while (0)
-    CacheParams &p = c->p;
-    PM_TRY_FREE(dalloc(&p.w, kCacheWeights));
-    PM_TRY_FREE(dalloc(&p.w_grad, kCacheWeights));
-    p.parts_cap = c->sm_count;
-    PM_TRY_FREE(dalloc(&p.w_part, (size_t)p.parts_cap * kCacheWeights));
-    PM_TRY_FREE(dalloc(&p.w_m, kCacheWeights));
-    PM_TRY_FREE(dalloc(&p.w_v, kCacheWeights));
-    PM_TRY_FREE(dalloc(&p.table, c->table_floats));
-    PM_TRY_FREE(dalloc(&p.table_grad, c->table_floats));
-    PM_TRY_FREE(dalloc(&p.table_m, c->table_floats));
-    PM_TRY_FREE(dalloc(&p.table_v, c->table_floats));
-    PM_TRY_FREE(dalloc(&p.table_h, c->table_floats / 2));
-    PM_TRY_FREE(dalloc(&p.w_img, kCacheWImageBytes / 16));
-    PM_TRY_FREE(dalloc(&p.loss, 1));
-    PM_TRY_FREE(dalloc(&p.loss_part, p.parts_cap));
-    p.dx_cap = cfg.batch;
-    PM_TRY_FREE(dalloc(&p.dx, (size_t)cfg.batch * 8));
-    PM_TRY_FREE(dalloc(&p.xt, (size_t)cfg.batch * 8));
-    PM_TRY_FREE(dalloc(&p.status, 1));
-    PM_TRY_FREE(cudaMemset(p.status, 0, sizeof(int)));
-    p.wait_polls = kMbarSpin;
-    PM_TRY_FREE(dalloc(&c->sel, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->tgt, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->skey, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->sval, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->skey_tmp, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->sval_tmp, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->shist, radix_sort_hist_words(cfg.train_samples)));
-    PM_TRY_FREE(dalloc(&c->sn, 1));
-    PM_TRY_FREE(dalloc(&c->run_ctr, 1));
-    PM_TRY_FREE(dalloc(&c->pqa, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->pqd, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->pval, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->pord, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->tqa, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->tqd, cfg.train_samples));
-    PM_TRY_FREE(dalloc(&c->tsel, cfg.train_samples));
-    PM_TRY_FREE(cudaMemcpy(c->sn, &cfg.train_samples, sizeof(uint32_t), cudaMemcpyHostToDevice));
-    PM_TRY_FREE(dalloc(&c->scale_sum, 1));
+    PM_TRY_FREE(cache_net_alloc(cfg, gr, cfg.seed, c->sm_count, &c->p));
+    PM_TRY_FREE(train_scratch_alloc(cfg.train_samples, &c->ts));
     for (auto &ev : c->ev) PM_TRY_FREE(cudaEventCreate(&ev));
     PM_TRY_FREE(cudaEventCreate(&c->tev0));
-    PM_TRY_FREE(cache_init(gr, p, cfg.seed, 0));
     PM_TRY_FREE(cudaDeviceSynchronize());
 #undef PM_TRY_FREE
     return PM_OK;
@@ -272,16 +319,16 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
     if (st->ql.nq == 0 || frames == 0) return PM_OK;
     cudaError_t e;
     const uint32_t ns = c->cfg.train_samples;
-    const uint32_t nb = batch_count(ns, c->cfg.batch);
+    const uint32_t nb = cache_batch_count(ns, c->cfg.batch);
     for (int f = 0; f < frames; ++f) {
         PM_TRY(cudaEventRecord(c->tev0, stream));
         PM_TRY(pick_and_target(st, c, stream));
         PM_TRY(cudaEventRecord(c->ev[5], stream));
         if (!(c->target_scale > 0.0f)) {
             float sum = 0.0f;
-            PM_TRY(cudaMemsetAsync(c->scale_sum, 0, sizeof(float), stream));
-            PM_TRY(cache_value_sum(c->tgt, ns, c->scale_sum, stream));
-            PM_TRY(cudaMemcpyAsync(&sum, c->scale_sum, sizeof(float), cudaMemcpyDeviceToHost, stream));
+            PM_TRY(cudaMemsetAsync(c->ts.scale_sum, 0, sizeof(float), stream));
+            PM_TRY(cache_value_sum(c->ts.tgt, ns, c->ts.scale_sum, stream));
+            PM_TRY(cudaMemcpyAsync(&sum, c->ts.scale_sum, sizeof(float), cudaMemcpyDeviceToHost, stream));
             PM_TRY(cudaStreamSynchronize(stream));
             const float mean = sum / (float)ns;
             c->target_scale = mean > 0.0f && std::isfinite(mean) ? mean : 1.0f;
@@ -289,8 +336,9 @@ pm_status pm_cache_train(pm_ctx *ctx, int frames, cudaStream_t stream) {
         PM_TRY(cudaMemsetAsync(c->p.loss, 0, sizeof(float), stream));
         for (uint32_t b = 0; b < nb; ++b) {
             // batch b: slots [o, o + n) of the training order
-            const uint32_t o = b * (ns / nb) + std::min(b, ns % nb), n = ns / nb + (b < ns % nb ? 1u : 0u);
-            PM_TRY(cache_backward(c->grid, c->p, st->dscene, c->tqa + o, c->tqd + o, nullptr, c->tgt + o, n,
+            uint32_t o, n;
+            cache_batch_range(ns, nb, b, &o, &n);
+            PM_TRY(cache_backward(c->grid, c->p, st->dscene, c->ts.tqa + o, c->ts.tqd + o, nullptr, c->ts.tgt + o, n,
                                   1.0f / c->target_scale, 1.0f / (3.0f * (float)n), c->cfg.loss_eps,
                                   nullptr, nullptr, c->sm_count, stream));
             float lr = c->cfg.lr;
@@ -448,7 +496,7 @@ pm_status pm_cache_debug_step(pm_ctx *ctx, const float4 *qa, const float4 *qd, c
     DeviceGuard g(ctx->device);
     CacheState *c = ctx->cache;
     PhysicalState *st = ctx->phys;
-    set_grid_box(c->grid, st->scene);
+    cache_grid_box(c->grid, st->scene);
     cudaError_t e;
     float4 *dqa = nullptr, *dqd = nullptr, *dt = nullptr;
     float *dx = nullptr, *dy = nullptr, *tg = nullptr;
@@ -531,8 +579,8 @@ pm_status pm_cache_debug_targets(pm_ctx *ctx, float4 *targets, uint32_t *query) 
     cudaError_t e;
     PM_TRY(pick_and_target(st, c, 0));
     PM_TRY(cudaDeviceSynchronize());
-    if (targets) PM_TRY(cudaMemcpy(targets, c->tgt, sizeof(float4) * ns, cudaMemcpyDeviceToHost));
-    if (query) PM_TRY(cudaMemcpy(query, c->tsel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
+    if (targets) PM_TRY(cudaMemcpy(targets, c->ts.tgt, sizeof(float4) * ns, cudaMemcpyDeviceToHost));
+    if (query) PM_TRY(cudaMemcpy(query, c->ts.tsel, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
     return PM_OK;
 }
 

@@ -191,6 +191,8 @@ PROTOTYPES = {
     "pm_batch_set_tune": (_i, [_vp, _i, _c.POINTER(BatchTune)]),
     "pm_batch_get_tune": (_i, [_vp, _i, _c.POINTER(BatchTune)]),
     "pm_batch_autotune": (_i, [_vp, _c.c_char_p, _vp]),
+    "pm_batch_cache_enable": (_i, [_vp, _vp]),
+    "pm_batch_cache_disable": (_i, [_vp]),
     "pm_cache_set_wait_limit": (_i, [_vp, _i]),
     "pm_cache_clear_status": (_i, [_vp]),
     "pm_cache_save": (_i, [_vp, _c.c_char_p]),
@@ -605,6 +607,19 @@ class Batch:
     def autotune(self, json_path=None, stream=0):
         self.ctx._check(self.lib.pm_batch_autotune(
             self.h, json_path.encode() if json_path else None, stream), "pm_batch_autotune")
+
+    def cache_enable(self, cfg=None, **overrides):
+        """Per-scene radiance caches (pm_batch_cache_enable); overrides set
+        fields of the default (or given) CacheConfig."""
+        if cfg is None:
+            cfg = cache_default_config()
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        self.ctx._check(self.lib.pm_batch_cache_enable(self.h, _c.byref(cfg)), "pm_batch_cache_enable")
+        return cfg
+
+    def cache_disable(self):
+        self.ctx._check(self.lib.pm_batch_cache_disable(self.h), "pm_batch_cache_disable")
 
 
 def cache_default_config():

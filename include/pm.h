@@ -457,11 +457,12 @@ PM_API pm_status pm_cache_load(pm_ctx *ctx, const char *path);
  * runs a frame of all of them as: one persistent trace launch over every
  * scene's photon paths (counting pass), per-scene record extents without a
  * host round trip, one persistent trace launch (writing pass), per-scene
- * kd-tree builds on side streams, then the render: scenes in query-list
- * mode one after another through pm_render's pipeline (query list, spatial
- * sort, shared candidate sets, composite; buffers sized at creation for the
- * largest scene, counts kept on the device), the others in one persistent
- * launch that hands out pixel chunks of all of them dynamically. Because no
+ * kd-tree builds on side streams, then the render: every query-list scene's
+ * query list and spatial sort into one arena sized at creation (counts kept
+ * on the device), one persistent shared-candidate estimate launch over all
+ * of them per k-list width and per-scene composites; the scenes in
+ * per-pixel mode in one persistent launch that hands out pixel chunks of
+ * all of them dynamically. Because no
  * step reads a count back to the host, the whole frame can be captured as a
  * CUDA graph (pm_batch_capture) and replayed (pm_batch_launch). Every
  * scene's image is bit-identical to a single-scene pm_emit + pm_build +
@@ -503,6 +504,19 @@ PM_API pm_status pm_batch_get_tune(pm_batch *b, int scene, pm_batch_tune *tune);
  * trial and choice to json_path (nullable). Rebuilds the trees it changes;
  * a captured graph is dropped (capture again). */
 PM_API pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t stream);
+/* Per-scene learned radiance caches (NULL config: pm_cache_default_config;
+ * scene i's network starts from seed cfg.seed + i, its grid spans its own
+ * scene box). From the next frame on, each scene's frame trains its network
+ * on cfg.train_samples k-NN targets of its query list (Adam steps of
+ * cfg.batch samples) and then renders every query of the list through the
+ * network instead of the k-NN estimate. The learning-rate schedule, the
+ * target scale and the frame counter live in device memory, so a captured
+ * frame keeps training when it is replayed. Every scene is switched to the
+ * query-list render (pm_batch_set_tune then refuses query_list 0, and
+ * pm_batch_autotune refuses to run); a captured frame is dropped. */
+PM_API pm_status pm_batch_cache_enable(pm_batch *b, const pm_cache_config *cfg);
+/* Frees the caches: frames render through the k-NN estimates again. */
+PM_API pm_status pm_batch_cache_disable(pm_batch *b);
 
 /* Kernels this library has launched since it was loaded (all contexts). */
 PM_API unsigned long long pm_kernel_launches(void);
