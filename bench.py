@@ -17,7 +17,9 @@ the FP32 oracle (`parity_sample`). More workloads ride on the same line:
 `preset2` (the 2M-photon scene, same metric), `cache` (the learned radiance
 cache on the preset-2 scene: online frame and cached render against the k-NN
 render, errors against the k-NN and FP64 renders), `batch` (64 independent
-scenes per frame captured as a CUDA graph) and `legacy` (the reference's own
+scenes per frame captured as a CUDA graph; `batch.cached`: the same batch
+with a radiance cache per scene trained and queried inside the replayed
+frame, its images against the k-NN images) and `legacy` (the reference's own
 voxel frame).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -74,6 +76,11 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched frame")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-cache-warm", type=int, default=96,
+                    help="training frames of the per-scene radiance caches before the timed batch frames "
+                         "(0: skip the cached batch frames)")
+    ap.add_argument("--batch-cache-samples", type=int, default=1 << 20,
+                    help="k-NN training samples per scene and frame of the per-scene caches")
     ap.add_argument("--no-legacy", action="store_true", help="skip the legacy-mode frames")
     ap.add_argument("--resolution", default=None,
                     help="WxH instead of the preset's image size (small profiling cases)")
@@ -445,9 +452,13 @@ def batch_frames(ctx, lib, args, device):
         paths += s.paths_traced
         records += s.map_size[0] + s.map_size[1]
     pixels = sum(c.width * c.height for c in cfgs)
+    cached = None
+    if args.batch_cache_warm > 0:
+        cached = batch_cache_frames(b, cfgs, st, timed, args)
     b.close()
     frame_s = statistics.mean(graph_ms) / 1e3
     return {
+        "cached": cached,
         "workload": "%d scenes per frame: 2..32 seeded spheres, sigma_s U[0, 0.2], photons "
                     "log-U[1e5, 4e6] split between the maps, 256^2/512^2/1024^2 pixels, k in "
                     "{32, 64, 128}, kd-tree per map, march 0.01" % args.batch_scenes,
@@ -459,6 +470,43 @@ def batch_frames(ctx, lib, args, device):
         "knobs": "defaults (leaf 32, query-list render; per-pixel knobs tile 1, collect 128, "
                  "merge 16); pm_batch_autotune picks per k",
         "clocks": clk,
+    }
+
+
+def batch_cache_frames(b, cfgs, st, timed, args):
+    """The same batch with a BF16 radiance cache per scene: each frame trains
+    every scene's network on `batch_cache_samples` k-NN targets of its own
+    query list (Adam steps of 2^17 samples) and renders every query through
+    it, the whole frame one replayed CUDA graph. Error: each scene's cached
+    image against its k-NN image (the same maps and camera) after
+    `batch_cache_warm` training frames."""
+    import numpy as np
+    import photonmap
+    sh = st.cuda_stream
+    knn = [b.read(i)[0] for i in range(b.n)]
+    cc = b.cache_enable(train_samples=args.batch_cache_samples, batch=min(1 << 17, args.batch_cache_samples))
+    b.capture(sh)
+    t0 = time.perf_counter()
+    for _ in range(args.batch_cache_warm):
+        b.launch(sh)
+    st.synchronize()
+    warm_s = time.perf_counter() - t0
+    frame_ms = [timed(lambda: b.launch(sh)) for _ in range(args.batch_steps)]
+    errs = []
+    for i in range(b.n):
+        img = b.read(i)[0][:, :3].astype(np.float64)
+        ref = knn[i][:, :3].astype(np.float64)
+        errs.append(float(np.sqrt(np.mean((img - ref) ** 2)) / max(np.sqrt(np.mean(ref ** 2)), 1e-30)))
+    b.cache_disable()
+    return {
+        "workload": "the batch above with one radiance cache per scene (16-level hash grid, 2^%d entries "
+                    "per level, 4x64 MLP in bf16 on tcgen05): %d k-NN training samples per scene and "
+                    "frame, Adam steps of %d, inference on every query; training, inference and "
+                    "composite inside the replayed frame" % (cc.log2_table, cc.train_samples, cc.batch),
+        "warm_frames": args.batch_cache_warm, "warm_s": warm_s,
+        "frame_ms_graph": statistics.mean(frame_ms),
+        "rel_rmse_vs_knn": {"median": float(np.median(errs)), "mean": float(np.mean(errs)),
+                            "max": float(np.max(errs)), "scenes": len(errs)},
     }
 
 
