@@ -340,7 +340,12 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         while ((1u << node_bits) < nodes) ++node_bits;
         uint64_t *ko = nullptr;
         uint32_t *vo = nullptr;
-        e = radix_sort_pairs_u64(ka, va, kb, vb, a.n_dev, n, 0, 16 + node_bits, a.hist, s, &ko, &vo);
+        // the records are grouped by node already (a node is a fixed range of
+        // positions, a whole number of sort tiles at these levels): sort each
+        // node's range by its 16-bit coordinate alone
+        e = span % kSortTile == 0
+                ? radix_sort_pairs_u64(ka, va, kb, vb, a.n_dev, n, 0, 16, a.hist, s, &ko, &vo, span / kSortTile)
+                : radix_sort_pairs_u64(ka, va, kb, vb, a.n_dev, n, 0, 16 + node_bits, a.hist, s, &ko, &vo);
         if (e != cudaSuccess) return e;
         if (vo != va) {
             uint64_t *tk = ka; ka = kb; kb = tk;
