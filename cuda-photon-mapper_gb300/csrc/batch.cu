@@ -162,6 +162,9 @@ struct pm_batch {
         bool on = false;
     } ar;
     std::vector<uint32_t> nsurf;  // diffuse queries per scene
+    // the radix-sorted levels of every map's tree in shared launches (one
+    // plan per set of leaf sizes; re-planned when a tune changes one)
+    KdMulti kd;
     // per-scene radiance caches (pm_batch_cache_enable): one network per
     // scene; the frame's picks and the per-step scratch are shared (scenes
     // train one after another on the frame's stream)
@@ -197,6 +200,7 @@ void free_caches(pm_batch *b) {
 void free_batch(pm_batch *b) {
     if (!b) return;
     free_caches(b);
+    kd_multi_free(b->kd);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (auto &m : b->maps) {
@@ -585,6 +589,35 @@ cudaError_t size_query_buffers(pm_batch *b) {
 }
 
 // Pads and builds the two trees of scene s on `st` with sort scratch `so`.
+// The build arguments of map m of scene s (sort scratch so; nullable for a
+// plan of the shared levels).
+KdBuildArgs map_args(const pm_batch *b, int s, int m, const pm_batch::Sort *so) {
+    const auto &mp = b->maps[2 * s + m];
+    KdBuildArgs a;
+    a.n = mp.cap;
+    a.n_dev = b->capn + 2 * s + m;
+    const pm_scene &sc = b->scenes[s];
+    a.lo = make_float3(sc.box_min[0], sc.box_min[1], sc.box_min[2]);
+    a.hi = make_float3(sc.box_max[0], sc.box_max[1], sc.box_max[2]);
+    a.box_dev = nullptr;
+    a.pos_in = mp.pos;
+    a.pow_in = mp.pow;
+    a.pos_out = mp.tpos;
+    a.pow_out = mp.tpow;
+    a.dir_out = mp.tdir;
+    a.node_lo = mp.lo;
+    a.node_hi = mp.hi;
+    a.keys = so ? so->keys : nullptr;
+    a.keys_tmp = so ? so->keys_tmp : nullptr;
+    a.vals = so ? so->vals : nullptr;
+    a.vals_tmp = so ? so->vals_tmp : nullptr;
+    a.hist = so ? so->hist : nullptr;
+    a.order_out = nullptr;
+    a.leaf_shift = shift_of(b->tune[s].leaf_size);
+    return a;
+}
+
+// Pads and builds the two trees of scene s on `st` with sort scratch `so`.
 cudaError_t build_scene(pm_batch *b, int s, cudaStream_t st, const pm_batch::Sort &so) {
     for (int m = 0; m < 2; ++m) {
         auto &mp = b->maps[2 * s + m];
@@ -592,29 +625,19 @@ cudaError_t build_scene(pm_batch *b, int s, cudaStream_t st, const pm_batch::Sor
         cudaError_t e = pad_map(mp.pos, mp.pow, b->words + s * kWords + (m == 0 ? W_EXT_S : W_EXT_V),
                                 mp.cap, st);
         if (e != cudaSuccess) return e;
-        KdBuildArgs a;
-        a.n = mp.cap;
-        a.n_dev = b->capn + 2 * s + m;
-        const pm_scene &sc = b->scenes[s];
-        a.lo = make_float3(sc.box_min[0], sc.box_min[1], sc.box_min[2]);
-        a.hi = make_float3(sc.box_max[0], sc.box_max[1], sc.box_max[2]);
-        a.box_dev = nullptr;
-        a.pos_in = mp.pos;
-        a.pow_in = mp.pow;
-        a.pos_out = mp.tpos;
-        a.pow_out = mp.tpow;
-        a.dir_out = mp.tdir;
-        a.node_lo = mp.lo;
-        a.node_hi = mp.hi;
-        a.keys = so.keys; a.keys_tmp = so.keys_tmp;
-        a.vals = so.vals; a.vals_tmp = so.vals_tmp;
-        a.hist = so.hist;
-        a.order_out = nullptr;
-        a.leaf_shift = shift_of(b->tune[s].leaf_size);
-        e = build_tree(a, st);
+        e = build_tree(map_args(b, s, m, &so), st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+// The plan of the shared tree levels for the current leaf sizes.
+cudaError_t plan_trees(pm_batch *b) {
+    kd_multi_free(b->kd);
+    std::vector<KdBuildArgs> args;
+    for (int s = 0; s < b->n; ++s)
+        for (int m = 0; m < 2; ++m) args.push_back(map_args(b, s, m, nullptr));
+    return kd_multi_create(args, &b->kd);
 }
 
 cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
@@ -637,11 +660,22 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
     note_launch();
     B_TRY(cudaGetLastError());
     B_TRY(trace_photons_batch(b->scenes_dev, b->write_dev, b->n, b->sm_count, st));
+    // the trees: records past each map's size to infinity, the radix-sorted
+    // levels of every map in shared launches, then each map's subtree finish,
+    // permutation and boxes on the side streams
+    for (int s = 0; s < b->n; ++s)
+        for (int m = 0; m < 2; ++m) {
+            auto &mp = b->maps[2 * s + m];
+            if (mp.cap == 0) continue;
+            B_TRY(pad_map(mp.pos, mp.pow, b->words + s * kWords + (m == 0 ? W_EXT_S : W_EXT_V), mp.cap, st));
+        }
+    uint32_t *order = nullptr;
+    B_TRY(kd_multi_levels(b->kd, st, &order));
     B_TRY(cudaEventRecord(b->fork, st));
     for (int k = 0; k < kBuildStreams; ++k) B_TRY(cudaStreamWaitEvent(b->side[k], b->fork, 0));
-    for (int s = 0; s < b->n; ++s) {
-        const int k = s % kBuildStreams;
-        B_TRY(build_scene(b, s, b->side[k], b->sort[k]));
+    for (int i = 0; i < b->kd.nmaps; ++i) {
+        const int s = b->kd.index[i] / 2, m = b->kd.index[i] % 2;
+        B_TRY(build_tree_finish(map_args(b, s, m, nullptr), order + b->kd.maps[i].base, b->side[i % kBuildStreams]));
     }
     for (int k = 0; k < kBuildStreams; ++k) {
         B_TRY(cudaEventRecord(b->join[k], b->side[k]));
@@ -794,6 +828,7 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     C_TRY(cudaMemcpy(b->write_dev, wp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
     C_TRY(upload_pixel_scenes(b));
     C_TRY(size_query_buffers(b));
+    C_TRY(plan_trees(b));
     C_TRY(cudaDeviceSynchronize());
 #undef C_TRY
     *out = b;
@@ -909,6 +944,7 @@ pm_status pm_batch_set_tune(pm_batch *b, int scene, const pm_batch_tune *t) {
     b->tune[scene] = *t;
     drop_graph(b);
     cudaError_t e = upload_pixel_scenes(b);
+    if (e == cudaSuccess) e = plan_trees(b);
     if (e != cudaSuccess) return check_cuda(b->ctx, e, "pm_batch_set_tune");
     return PM_OK;
 }
@@ -1106,6 +1142,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
     cudaFree(one_prefix);
     A_TRY(upload_pixel_scenes(b));
     // every scene's trees follow the new leaf sizes from the next frame on
+    A_TRY(plan_trees(b));
     A_TRY(enqueue_frame(b, stream));
     A_TRY(cudaStreamSynchronize(stream));
 #undef A_TRY

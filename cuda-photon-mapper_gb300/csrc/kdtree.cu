@@ -21,6 +21,9 @@
 #include "kdtree.cuh"
 #include "radix_sort.cuh"
 
+#include <algorithm>
+#include <cstring>
+
 namespace pm {
 namespace {
 
@@ -296,6 +299,86 @@ __global__ void top_box_kernel(uint32_t levels, float4 *node_lo, float4 *node_hi
     }
 }
 
+
+// ---- several maps at once (KdMulti) ----
+
+// Pooled position i: the map (build order) and the position within it.
+__device__ __forceinline__ int multi_map(const uint32_t *tile_map, uint32_t i) { return (int)tile_map[i / kSortTile]; }
+
+__global__ void multi_init_kernel(const KdMultiMap *maps, const uint32_t *tile_map, uint32_t total,
+                                  uint32_t *vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    vals[i] = i - maps[multi_map(tile_map, i)].base;
+}
+
+__global__ void multi_root_kernel(const KdMultiMap *maps, int nmaps) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmaps || maps[m].depth == 0) return;
+    maps[m].cell_lo[1] = maps[m].root_lo;
+    maps[m].cell_hi[1] = maps[m].root_hi;
+}
+
+// split_key_kernel over the pooled positions of the maps sorted at `level`;
+// positions past a map's records (the padding of its last tile) get the
+// largest key, so the stable sort keeps them at the end of their node.
+__global__ void split_key_multi_kernel(const KdMultiMap *maps, const uint32_t *tile_map, uint32_t total,
+                                       int level, const uint32_t *order, uint64_t *keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const KdMultiMap &m = maps[multi_map(tile_map, i)];
+    const uint32_t j = i - m.base;
+    if (j >= m.n) {
+        keys[i] = 0xffffu;
+        return;
+    }
+    const uint32_t span = (32u << m.leaf_shift) << (m.depth - level);
+    const uint32_t node = j / span;
+    const uint32_t g = (1u << level) + node;
+    const float4 lo = m.cell_lo[g], hi = m.cell_hi[g];
+    const int ax = longest_axis(lo, hi);
+    const float4 p = m.pos[order[i]];
+    const float c = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+    const float l0 = ax == 0 ? lo.x : (ax == 1 ? lo.y : lo.z);
+    const float l1 = ax == 0 ? hi.x : (ax == 1 ? hi.y : hi.z);
+    const float f = (c - l0) / (l1 - l0) * 65536.0f;
+    const uint32_t qc = !(f > 0.0f) ? 0u : (f >= 65535.0f ? 65535u : (uint32_t)f);
+    keys[i] = ((uint64_t)node << 16) | qc;
+}
+
+// split_cell_kernel over the nodes of every map sorted at `level`
+// (prefix: nmaps + 1 scanned node counts).
+__global__ void split_cell_multi_kernel(const KdMultiMap *maps, int nmaps, const uint32_t *prefix,
+                                        int level, const uint32_t *order) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= prefix[nmaps]) return;
+    int lo_m = 0, hi_m = nmaps - 1;  // the last map whose prefix <= u
+    while (lo_m < hi_m) {
+        const int mid = (lo_m + hi_m + 1) >> 1;
+        if (prefix[mid] <= u) lo_m = mid; else hi_m = mid - 1;
+    }
+    const KdMultiMap &m = maps[lo_m];
+    const uint32_t j = u - prefix[lo_m];
+    const uint32_t span = (32u << m.leaf_shift) << (m.depth - level);
+    const uint32_t g = (1u << level) + j;
+    const float4 lo = m.cell_lo[g], hi = m.cell_hi[g];
+    const uint32_t start = j * span, half = span >> 1;
+    const uint32_t cnt = min(span, m.n - start);
+    float4 llo = lo, lhi = hi, rlo = lo, rhi = hi;
+    if (cnt > half) {
+        const int ax = longest_axis(lo, hi);
+        const float4 p = m.pos[order[m.base + start + half]];
+        const float c = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+        if (ax == 0) { lhi.x = c; rlo.x = c; }
+        else if (ax == 1) { lhi.y = c; rlo.y = c; }
+        else { lhi.z = c; rlo.z = c; }
+    }
+    m.cell_lo[2 * g] = llo;
+    m.cell_hi[2 * g] = lhi;
+    m.cell_lo[2 * g + 1] = rlo;
+    m.cell_hi[2 * g + 1] = rhi;
+}
+
 }  // namespace
 
 int tree_depth(uint32_t n, int leaf_shift) {
@@ -307,6 +390,14 @@ int tree_depth(uint32_t n, int leaf_shift) {
 }
 
 size_t tree_nodes(uint32_t n, int leaf_shift) { return (size_t)2 << tree_depth(n, leaf_shift); }
+
+// The first level finished per subtree in shared memory: nodes of at most
+// kSubtreeMax records.
+int first_finish_level(int D, uint32_t leaf) {
+    int lf = D;
+    while (lf > 0 && ((uint64_t)leaf << (D - (lf - 1))) <= (uint64_t)kSubtreeMax) --lf;
+    return lf;
+}
 
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     const uint32_t n = a.n;
@@ -325,8 +416,7 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
     }
     // levels [lf, D) are finished per subtree in shared memory
     const uint32_t leaf = 32u << a.leaf_shift;
-    int lf = D;
-    while (lf > 0 && ((uint64_t)leaf << (D - (lf - 1))) <= (uint64_t)kSubtreeMax) --lf;
+    const int lf = first_finish_level(D, leaf);
     if (lf == 0 && D > 0) {
         iota_kernel<<<blocks, 256, 0, s>>>(va, n);
         note_launch();
@@ -354,6 +444,17 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         split_cell_kernel<<<(nodes + 255) / 256, 256, 0, s>>>(a.pos_in, va, n, l, span, nodes,
                                                                a.node_lo, a.node_hi); note_launch();
     }
+    return build_tree_finish(a, va, s);
+}
+
+cudaError_t build_tree_finish(const KdBuildArgs &a, uint32_t *va, cudaStream_t s) {
+    const uint32_t n = a.n;
+    if (n == 0) return cudaSuccess;
+    const int D = tree_depth(n, a.leaf_shift);
+    const uint32_t blocks = (n + 255) / 256;
+    const uint32_t leaf = 32u << a.leaf_shift;
+    const int lf = first_finish_level(D, leaf);
+    cudaError_t e;
     if (lf < D) {
         const uint32_t span = leaf << (D - lf);
         const uint32_t nodes = (n + span - 1) / span;
@@ -384,6 +485,139 @@ cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s) {
         e = cudaMemcpyAsync(a.order_out, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return e;
     }
+    return cudaGetLastError();
+}
+
+namespace {
+template <typename T>
+cudaError_t kd_alloc(T **p, size_t count) {
+    *p = nullptr;
+    return cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+}
+}  // namespace
+
+cudaError_t kd_multi_create(const std::vector<KdBuildArgs> &args, KdMulti *k) {
+    *k = KdMulti();
+    std::vector<int> idx;
+    for (int i = 0; i < (int)args.size(); ++i)
+        if (args[i].n > 0) idx.push_back(i);
+    auto lf_of = [&](int i) {
+        const int D = tree_depth(args[i].n, args[i].leaf_shift);
+        return first_finish_level(D, 32u << args[i].leaf_shift);
+    };
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lf_of(a) > lf_of(b); });
+    uint32_t tiles = 0;
+    for (int i : idx) {
+        const KdBuildArgs &a = args[i];
+        KdMultiMap m;
+        memset(&m, 0, sizeof(m));
+        m.pos = a.pos_in;
+        m.cell_lo = a.node_lo;
+        m.cell_hi = a.node_hi;
+        m.root_lo = make_float4(a.lo.x, a.lo.y, a.lo.z, 0.0f);
+        m.root_hi = make_float4(a.hi.x, a.hi.y, a.hi.z, 0.0f);
+        m.n = a.n;
+        m.base = tiles * kSortTile;
+        m.depth = tree_depth(a.n, a.leaf_shift);
+        m.lf = lf_of(i);
+        m.leaf_shift = a.leaf_shift;
+        tiles += (a.n + kSortTile - 1) / kSortTile;
+        k->levels = std::max(k->levels, m.lf);
+        k->maps.push_back(m);
+        k->index.push_back(i);
+    }
+    k->nmaps = (int)k->maps.size();
+    k->total = tiles * kSortTile;
+    const int L = std::max(k->levels, 1);
+    std::vector<uint32_t> tile_map(std::max<uint32_t>(tiles, 1), 0);
+    std::vector<uint2> seg((size_t)L * std::max<uint32_t>(tiles, 1), make_uint2(0, 1));
+    std::vector<uint32_t> prefix((size_t)L * (k->nmaps + 1), 0);
+    std::vector<uint32_t> level_n(L, 0);
+    for (int mi = 0; mi < k->nmaps; ++mi) {
+        const KdMultiMap &m = k->maps[mi];
+        const uint32_t t0 = m.base / kSortTile, nt = (m.n + kSortTile - 1) / kSortTile;
+        for (uint32_t t = 0; t < nt; ++t) tile_map[t0 + t] = (uint32_t)mi;
+    }
+    k->level_tiles.assign(L, 0);
+    k->level_nodes.assign(L, 0);
+    k->level_maps.assign(L, 0);
+    for (int l = 0; l < k->levels; ++l) {
+        uint32_t nodes = 0;
+        for (int mi = 0; mi < k->nmaps; ++mi) {
+            const KdMultiMap &m = k->maps[mi];
+            prefix[(size_t)l * (k->nmaps + 1) + mi] = nodes;
+            if (l >= m.lf) continue;  // maps sorted by lf: the rest are finished
+            const uint32_t span = (32u << m.leaf_shift) << (m.depth - l);
+            const uint32_t t0 = m.base / kSortTile, nt = (m.n + kSortTile - 1) / kSortTile;
+            const uint32_t st = span / kSortTile;  // whole tiles at the sorted levels
+            for (uint32_t t = 0; t < nt; ++t) {
+                const uint32_t first = t / st * st;
+                seg[(size_t)l * tiles + t0 + t] = make_uint2(t0 + first, std::min(st, nt - first));
+            }
+            nodes += (m.n + span - 1) / span;
+            k->level_tiles[l] = t0 + nt;
+            k->level_maps[l] = (uint32_t)(mi + 1);
+        }
+        prefix[(size_t)l * (k->nmaps + 1) + k->nmaps] = nodes;
+        k->level_nodes[l] = nodes;
+        level_n[l] = k->level_tiles[l] * kSortTile;
+    }
+    cudaError_t e;
+#define KM_TRY(x) do { e = (x); if (e != cudaSuccess) { kd_multi_free(*k); return e; } } while (0)
+    KM_TRY(kd_alloc(&k->desc, k->nmaps));
+    KM_TRY(kd_alloc(&k->tile_map, tile_map.size()));
+    KM_TRY(kd_alloc(&k->seg_tab, seg.size()));
+    KM_TRY(kd_alloc(&k->node_prefix, prefix.size()));
+    KM_TRY(kd_alloc(&k->level_n, level_n.size()));
+    KM_TRY(kd_alloc(&k->keys, k->total));
+    KM_TRY(kd_alloc(&k->keys_tmp, k->total));
+    KM_TRY(kd_alloc(&k->vals, k->total));
+    KM_TRY(kd_alloc(&k->vals_tmp, k->total));
+    KM_TRY(kd_alloc(&k->hist, radix_sort_hist_words(k->total)));
+    if (k->nmaps)
+        KM_TRY(cudaMemcpy(k->desc, k->maps.data(), sizeof(KdMultiMap) * k->nmaps, cudaMemcpyHostToDevice));
+    KM_TRY(cudaMemcpy(k->tile_map, tile_map.data(), sizeof(uint32_t) * tile_map.size(), cudaMemcpyHostToDevice));
+    KM_TRY(cudaMemcpy(k->seg_tab, seg.data(), sizeof(uint2) * seg.size(), cudaMemcpyHostToDevice));
+    KM_TRY(cudaMemcpy(k->node_prefix, prefix.data(), sizeof(uint32_t) * prefix.size(), cudaMemcpyHostToDevice));
+    KM_TRY(cudaMemcpy(k->level_n, level_n.data(), sizeof(uint32_t) * level_n.size(), cudaMemcpyHostToDevice));
+#undef KM_TRY
+    return cudaSuccess;
+}
+
+void kd_multi_free(KdMulti &k) {
+    cudaFree(k.desc); cudaFree(k.tile_map); cudaFree(k.seg_tab); cudaFree(k.node_prefix); cudaFree(k.level_n);
+    cudaFree(k.keys); cudaFree(k.keys_tmp); cudaFree(k.vals); cudaFree(k.vals_tmp); cudaFree(k.hist);
+    k = KdMulti();
+}
+
+cudaError_t kd_multi_levels(KdMulti &k, cudaStream_t s, uint32_t **order) {
+    uint64_t *ka = k.keys, *kb = k.keys_tmp;
+    uint32_t *va = k.vals, *vb = k.vals_tmp;
+    *order = va;
+    if (k.nmaps == 0) return cudaSuccess;
+    multi_init_kernel<<<(k.total + 255) / 256, 256, 0, s>>>(k.desc, k.tile_map, k.total, va);
+    note_launch();
+    multi_root_kernel<<<(k.nmaps + 127) / 128, 128, 0, s>>>(k.desc, k.nmaps);
+    note_launch();
+    const uint32_t tiles = k.total / kSortTile;
+    for (int l = 0; l < k.levels; ++l) {
+        const uint32_t n = k.level_tiles[l] * kSortTile;
+        split_key_multi_kernel<<<(n + 255) / 256, 256, 0, s>>>(k.desc, k.tile_map, n, l, va, ka);
+        note_launch();
+        uint64_t *ko = nullptr;
+        uint32_t *vo = nullptr;
+        cudaError_t e = radix_sort_pairs_u64(ka, va, kb, vb, k.level_n + l, n, 0, 16, k.hist, s, &ko, &vo, 0,
+                                             k.seg_tab + (size_t)l * tiles);
+        if (e != cudaSuccess) return e;
+        if (vo != va) {
+            uint64_t *tk = ka; ka = kb; kb = tk;
+            uint32_t *tv = va; va = vb; vb = tv;
+        }
+        split_cell_multi_kernel<<<(k.level_nodes[l] + 255) / 256, 256, 0, s>>>(
+            k.desc, (int)k.level_maps[l], k.node_prefix + (size_t)l * (k.nmaps + 1), l, va);
+        note_launch();
+    }
+    *order = va;
     return cudaGetLastError();
 }
 

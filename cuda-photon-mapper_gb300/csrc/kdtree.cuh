@@ -2,6 +2,8 @@
 #pragma once
 #include "phys_common.cuh"
 
+#include <vector>
+
 namespace pm {
 
 // Depth D of the tree over n records (leaves of 32 << leaf_shift records at
@@ -27,5 +29,42 @@ struct KdBuildArgs {
 };
 
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s);
+// The part of build_tree below the radix-sorted levels -- the subtree
+// finish, the permutation into tree order and the boxes -- for a tree whose
+// record order after those levels is order[0..a.n).
+cudaError_t build_tree_finish(const KdBuildArgs &a, uint32_t *order, cudaStream_t s);
+
+// Several trees built together (a batch's maps): the radix-sorted levels of
+// every map in shared launches over one pooled order, then each map's
+// finish (build_tree_finish). Each tree comes out as build_tree makes it.
+struct KdMultiMap {           // one map, device copy
+    const float4 *pos;        // records in index order
+    float4 *cell_lo, *cell_hi;
+    float4 root_lo, root_hi;  // the root cell
+    uint32_t n;               // records
+    uint32_t base;            // first pooled position (a multiple of the sort tile)
+    int depth, lf, leaf_shift;
+};
+struct KdMulti {
+    int nmaps = 0, levels = 0;          // levels: the most radix-sorted levels of any map
+    std::vector<KdMultiMap> maps;       // in build order: the most sorted levels first
+    std::vector<int> index;             // build order -> the caller's map index
+    KdMultiMap *desc = nullptr;
+    uint32_t *tile_map = nullptr;       // per pooled tile: its map (build order)
+    uint2 *seg_tab = nullptr;           // per level and pooled tile: (node's first tile, node's tiles)
+    uint32_t *node_prefix = nullptr;    // per level: nmaps + 1 scanned node counts of the sorted maps
+    uint32_t *level_n = nullptr;        // per level: pooled positions of the maps sorted at that level
+    std::vector<uint32_t> level_tiles, level_nodes, level_maps;
+    uint32_t total = 0;                 // pooled positions
+    uint64_t *keys = nullptr, *keys_tmp = nullptr;
+    uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
+};
+// Plans the build of the maps args[i] (n, pos_in, node_lo/hi, leaf_shift, lo/hi) and allocates
+// its tables and pooled scratch. Maps with no records are left out.
+cudaError_t kd_multi_create(const std::vector<KdBuildArgs> &args, KdMulti *k);
+void kd_multi_free(KdMulti &k);
+// The shared levels of every map; *order receives the pooled order (map i of
+// the build order at *order + maps[i].base).
+cudaError_t kd_multi_levels(KdMulti &k, cudaStream_t s, uint32_t **order);
 
 }  // namespace pm

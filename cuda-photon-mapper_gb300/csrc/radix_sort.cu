@@ -101,7 +101,12 @@ __global__ void __launch_bounds__(kSortThreads) tile_scan_kernel(const uint32_t 
 // seg consecutive tiles one after another, digit-major inside a segment, so
 // that the scan keeps every segment's items inside the segment (seg >=
 // ntiles: one segment, the plain digit-major order).
-__device__ __forceinline__ uint32_t count_at(uint32_t d, uint32_t t, uint32_t ntiles, uint32_t seg) {
+__device__ __forceinline__ uint32_t count_at(uint32_t d, uint32_t t, uint32_t ntiles, uint32_t seg,
+                                             const uint2 *seg_tab) {
+    if (seg_tab) {  // per tile: (the segment's first tile, its tiles)
+        const uint2 e = seg_tab[t];
+        return e.x * 256u + d * e.y + (t - e.x);
+    }
     const uint32_t t0 = t / seg * seg;
     return t0 * 256u + d * min(seg, ntiles - t0) + (t - t0);
 }
@@ -109,7 +114,8 @@ __device__ __forceinline__ uint32_t count_at(uint32_t d, uint32_t t, uint32_t nt
 template <typename K>
 __global__ void __launch_bounds__(kSortThreads) hist_kernel(const K *keys, const uint32_t *n_dev,
                                                             int shift, uint32_t *hist,
-                                                            uint32_t ntiles, uint32_t seg) {
+                                                            uint32_t ntiles, uint32_t seg,
+                                                            const uint2 *seg_tab) {
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -120,20 +126,21 @@ __global__ void __launch_bounds__(kSortThreads) hist_kernel(const K *keys, const
         if (idx < n) atomicAdd(&h[(uint32_t)(keys[idx] >> shift) & 255u], 1u);
     }
     __syncthreads();
-    hist[count_at(threadIdx.x, blockIdx.x, ntiles, seg)] = h[threadIdx.x];
+    hist[count_at(threadIdx.x, blockIdx.x, ntiles, seg, seg_tab)] = h[threadIdx.x];
 }
 
 template <typename K>
 __global__ void __launch_bounds__(kSortThreads) scatter_kernel(
     const K *keys_in, const uint32_t *vals_in, K *keys_out, uint32_t *vals_out,
-    const uint32_t *n_dev, int shift, const uint32_t *offs, uint32_t ntiles, uint32_t seg) {
+    const uint32_t *n_dev, int shift, const uint32_t *offs, uint32_t ntiles, uint32_t seg,
+    const uint2 *seg_tab) {
     constexpr int kWarps = kSortThreads / 32;
     __shared__ uint32_t run[256];
     __shared__ uint32_t wcnt[kWarps][256];
     const int warp = threadIdx.x >> 5;
     const uint32_t n = *n_dev;
     const uint32_t base = blockIdx.x * kSortTile;
-    run[threadIdx.x] = offs[count_at(threadIdx.x, blockIdx.x, ntiles, seg)];
+    run[threadIdx.x] = offs[count_at(threadIdx.x, blockIdx.x, ntiles, seg, seg_tab)];
     for (int r = 0; r < kSortItems; ++r) {
         const uint32_t idx = base + r * kSortThreads + threadIdx.x;
         if (base + r * kSortThreads >= n) break;  // uniform across the block
@@ -166,7 +173,7 @@ template <typename K>
 cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
                        const uint32_t *n_dev, uint32_t max_n, int begin_bit, int end_bit,
                        uint32_t *hist, cudaStream_t stream, K **out_keys, uint32_t **out_vals,
-                       uint32_t seg_tiles) {
+                       uint32_t seg_tiles, const uint2 *seg_tab) {
     K *kin = keys, *kout = keys_tmp;
     uint32_t *vin = vals, *vout = vals_tmp;
     uint32_t ntiles = (max_n + kSortTile - 1) / kSortTile;
@@ -177,7 +184,8 @@ cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
     const uint32_t hn = 256u * ntiles;
     uint32_t *partials = hist + hn;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        hist_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, n_dev, shift, hist, ntiles, seg); note_launch();
+        hist_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, n_dev, shift, hist, ntiles, seg,
+                                                                        seg_tab); note_launch();
         if (hn <= kSortTile) {
             scan_kernel<<<1, kScanThreads, 0, stream>>>(hist, hist, hn, nullptr); note_launch();
         } else {
@@ -187,7 +195,7 @@ cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
             tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(hist, hist, hn, partials); note_launch();
         }
         scatter_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n_dev, shift,
-                                                               hist, ntiles, seg); note_launch();
+                                                               hist, ntiles, seg, seg_tab); note_launch();
         K *tk = kin; kin = kout; kout = tk;
         uint32_t *tv = vin; vin = vout; vout = tv;
     }
@@ -203,15 +211,16 @@ cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_
                                  int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
                                  uint32_t **out_keys, uint32_t **out_vals) {
     return sort_pairs<uint32_t>(keys, vals, keys_tmp, vals_tmp, n_dev, max_n, begin_bit, end_bit,
-                                hist, stream, out_keys, out_vals, 0u);
+                                hist, stream, out_keys, out_vals, 0u, nullptr);
 }
 
 cudaError_t radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t *keys_tmp,
                                  uint32_t *vals_tmp, const uint32_t *n_dev, uint32_t max_n,
                                  int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
-                                 uint64_t **out_keys, uint32_t **out_vals, uint32_t seg_tiles) {
+                                 uint64_t **out_keys, uint32_t **out_vals, uint32_t seg_tiles,
+                                 const uint2 *seg_tab) {
     return sort_pairs<uint64_t>(keys, vals, keys_tmp, vals_tmp, n_dev, max_n, begin_bit, end_bit,
-                                hist, stream, out_keys, out_vals, seg_tiles);
+                                hist, stream, out_keys, out_vals, seg_tiles, seg_tab);
 }
 
 uint32_t scan_tile_count(uint32_t n) {

@@ -37,11 +37,14 @@ cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_
                                  uint32_t **out_keys, uint32_t **out_vals);
 // With seg_tiles > 0 the items are sorted within segments of seg_tiles x
 // kSortTile consecutive items (each segment keeps its place): a segmented
-// sort in the passes of the segment's own bits.
+// sort in the passes of the segment's own bits. With seg_tab (device, one
+// entry per tile: the first tile of the tile's segment and the segment's
+// tile count) the segments are any runs of whole tiles.
 cudaError_t radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t *keys_tmp,
                                  uint32_t *vals_tmp, const uint32_t *n_dev, uint32_t max_n,
                                  int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
-                                 uint64_t **out_keys, uint32_t **out_vals, uint32_t seg_tiles = 0);
+                                 uint64_t **out_keys, uint32_t **out_vals, uint32_t seg_tiles = 0,
+                                 const uint2 *seg_tab = nullptr);
 
 // Exclusive prefix sum of in[0..n) into out[0..n) with one CTA; the total
 // goes to *total (device). n is a host value here.

@@ -39,7 +39,7 @@ using namespace wknn;
 
 constexpr int kTileWarps = 4;
 constexpr int kAnchorAt = 15;                // the anchor: query 15 of a warp's chunk
-constexpr int kTileCap = 384;                // candidate records per warp (slots fit 16 bits)
+constexpr int kTileCap = 400;                // candidate records per warp (the most at 5 blocks of 4 warps per SM)
 constexpr int kScanSlots = 2;   // candidates per lane per step of the selection scan
 constexpr int kPickSlots = 1;   // band entries per lane per step of the final selection
 constexpr float kRel = 2e-4f;                // relative and absolute margins of the distance bounds
