@@ -1,7 +1,7 @@
 // batch.cu -- many independent scenes per frame behind the pm_batch_* C ABI:
-// persistent multi-scene trace and render launches, per-scene kd builds on
-// side streams, CUDA-graph capture of the whole frame, and the autotuner of
-// the search knobs.
+// persistent multi-scene trace and render launches, the kd-trees of every
+// map in shared launches, CUDA-graph capture of the whole frame, and the
+// autotuner of the search knobs.
 //
 // Frame (all on the caller's stream, no host round trip):
 //   1. zero the per-scene words, path counts and gather counters
@@ -9,9 +9,11 @@
 //   3. per scene and map: scan of the path counts over the whole path cap
 //      (zero beyond the issued paths) -> record extent (records, paths)
 //   4. writing pass: one persistent launch
-//   5. per scene and map, on kBuildStreams side streams: records past the
-//      map's size are set to infinity, then the kd-tree is built over the
-//      map's capacity (so every launch size is a host constant)
+//   5. the kd-trees of every map in shared launches (KdMulti): records past
+//      each map's size set to infinity, the radix-sorted levels of all
+//      maps, then their subtree finishes, permutations and boxes; each tree
+//      is built over its map's capacity (so every launch size is a host
+//      constant)
 //   6. the render: the scenes in per-pixel mode in one persistent launch
 //      over their pixels; each query-list scene's list (per-pixel counts
 //      and scans, records, (map, Morton) sort) into its slice of one arena
@@ -48,7 +50,6 @@
 namespace pm {
 namespace {
 
-constexpr int kBuildStreams = 8;
 constexpr int kWords = 16;  // device words per scene, all reset every frame
 enum {
     W_COUNTER = 0,  // path counter (count pass, then write pass)
@@ -126,9 +127,7 @@ struct pm_batch {
     struct Sort {
         uint64_t *keys = nullptr, *keys_tmp = nullptr;
         uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
-    } sort[kBuildStreams];
-    cudaStream_t side[kBuildStreams] = {};
-    cudaEvent_t fork = nullptr, join[kBuildStreams] = {};
+    } sort;  // the autotuner's per-scene rebuilds
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long graph_kernels = 0;
@@ -212,9 +211,8 @@ void free_batch(pm_batch *b) {
     cudaFree(b->capn); cudaFree(b->gathers); cudaFree(b->work); cudaFree(b->rad); cudaFree(b->rgba);
     cudaFree(b->scenes_dev); cudaFree(b->count_dev); cudaFree(b->write_dev);
     cudaFree(b->render_dev); cudaFree(b->prefix_dev);
-    for (auto &s : b->sort) {
-        cudaFree(s.keys); cudaFree(s.keys_tmp); cudaFree(s.vals); cudaFree(s.vals_tmp); cudaFree(s.hist);
-    }
+    cudaFree(b->sort.keys); cudaFree(b->sort.keys_tmp); cudaFree(b->sort.vals); cudaFree(b->sort.vals_tmp);
+    cudaFree(b->sort.hist);
     auto &q = b->q;
     cudaFree(q.cnt); cudaFree(q.off); cudaFree(q.scnt); cudaFree(q.soff); cudaFree(q.slist);
     cudaFree(q.scan_tmp); cudaFree(q.qa); cudaFree(q.qd); cudaFree(q.val); cudaFree(q.key);
@@ -224,11 +222,6 @@ void free_batch(pm_batch *b) {
     cudaFree(ar.qa); cudaFree(ar.qd); cudaFree(ar.val); cudaFree(ar.ord); cudaFree(ar.off);
     cudaFree(ar.defer); cudaFree(ar.defer_sc); cudaFree(ar.defer_n); cudaFree(ar.anchor_d);
     cudaFree(ar.desc);
-    for (auto &s : b->side)
-        if (s) cudaStreamDestroy(s);
-    if (b->fork) cudaEventDestroy(b->fork);
-    for (auto &e : b->join)
-        if (e) cudaEventDestroy(e);
     delete b;
 }
 
@@ -614,6 +607,7 @@ KdBuildArgs map_args(const pm_batch *b, int s, int m, const pm_batch::Sort *so) 
     a.hist = so ? so->hist : nullptr;
     a.order_out = nullptr;
     a.leaf_shift = shift_of(b->tune[s].leaf_size);
+    a.pad_count = b->words + s * kWords + (m == 0 ? W_EXT_S : W_EXT_V);
     return a;
 }
 
@@ -660,27 +654,12 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
     note_launch();
     B_TRY(cudaGetLastError());
     B_TRY(trace_photons_batch(b->scenes_dev, b->write_dev, b->n, b->sm_count, st));
-    // the trees: records past each map's size to infinity, the radix-sorted
-    // levels of every map in shared launches, then each map's subtree finish,
-    // permutation and boxes on the side streams
-    for (int s = 0; s < b->n; ++s)
-        for (int m = 0; m < 2; ++m) {
-            auto &mp = b->maps[2 * s + m];
-            if (mp.cap == 0) continue;
-            B_TRY(pad_map(mp.pos, mp.pow, b->words + s * kWords + (m == 0 ? W_EXT_S : W_EXT_V), mp.cap, st));
-        }
+    // the trees of every map in shared launches: records past each map's
+    // size to infinity, the radix-sorted levels, then the subtree finishes,
+    // the permutations into tree order and the boxes
     uint32_t *order = nullptr;
     B_TRY(kd_multi_levels(b->kd, st, &order));
-    B_TRY(cudaEventRecord(b->fork, st));
-    for (int k = 0; k < kBuildStreams; ++k) B_TRY(cudaStreamWaitEvent(b->side[k], b->fork, 0));
-    for (int i = 0; i < b->kd.nmaps; ++i) {
-        const int s = b->kd.index[i] / 2, m = b->kd.index[i] % 2;
-        B_TRY(build_tree_finish(map_args(b, s, m, nullptr), order + b->kd.maps[i].base, b->side[i % kBuildStreams]));
-    }
-    for (int k = 0; k < kBuildStreams; ++k) {
-        B_TRY(cudaEventRecord(b->join[k], b->side[k]));
-        B_TRY(cudaStreamWaitEvent(st, b->join[k], 0));
-    }
+    B_TRY(kd_multi_finish(b->kd, order, st));
     if (b->n_pixel > 0) B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n_pixel, b->work, b->sm_count, st));
     for (int s = 0; s < b->n; ++s) {
         if (!b->tune[s].query_list) continue;
@@ -777,16 +756,11 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     C_TRY(dalloc(&b->write_dev, n));
     C_TRY(dalloc(&b->render_dev, n));
     C_TRY(dalloc(&b->prefix_dev, (size_t)n + 1));
-    for (auto &so : b->sort) {
-        C_TRY(dalloc(&so.keys, max_map));
-        C_TRY(dalloc(&so.keys_tmp, max_map));
-        C_TRY(dalloc(&so.vals, max_map));
-        C_TRY(dalloc(&so.vals_tmp, max_map));
-        C_TRY(dalloc(&so.hist, radix_sort_hist_words(max_map)));
-    }
-    for (auto &st : b->side) C_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    C_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-    for (auto &ev : b->join) C_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    C_TRY(dalloc(&b->sort.keys, max_map));
+    C_TRY(dalloc(&b->sort.keys_tmp, max_map));
+    C_TRY(dalloc(&b->sort.vals, max_map));
+    C_TRY(dalloc(&b->sort.vals_tmp, max_map));
+    C_TRY(dalloc(&b->sort.hist, radix_sort_hist_words(max_map)));
     // static per-scene parameters
     std::vector<uint32_t> capn(2 * (size_t)n);
     std::vector<TraceParams> cp(n), wp(n);
@@ -1075,7 +1049,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
         for (int li = 0; li < 3; ++li) {
             b->tune[rep].leaf_size = leaves[li];
             b->tune[rep].query_list = 0;
-            A_TRY(build_scene(b, rep, stream, b->sort[0]));
+            A_TRY(build_scene(b, rep, stream, b->sort));
             for (int ti = 0; ti < 4; ++ti) {
                 b->tune[rep].tile = tiles[ti];
                 b->tune[rep].collect_max = 128;
@@ -1091,7 +1065,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
             }
         }
         b->tune[rep] = best;
-        A_TRY(build_scene(b, rep, stream, b->sort[0]));
+        A_TRY(build_scene(b, rep, stream, b->sort));
         for (int ci = 0; ci < 3; ++ci)
             for (int mi = 0; mi < 3; ++mi) {
                 b->tune[rep].collect_max = collects[ci];
@@ -1111,7 +1085,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
             b->tune[rep] = pixel_best;
             b->tune[rep].leaf_size = leaves[li];
             b->tune[rep].query_list = 1;
-            A_TRY(build_scene(b, rep, stream, b->sort[0]));
+            A_TRY(build_scene(b, rep, stream, b->sort));
             float ms;
             A_TRY(time_scene(rep, &ms));
             char buf[160];
@@ -1125,7 +1099,7 @@ pm_status pm_batch_autotune(pm_batch *b, const char *json_path, cudaStream_t str
         int members = 0;
         for (int s = 0; s < b->n; ++s)
             if (b->cfgs[s].k == kc) { b->tune[s] = best; ++members; }
-        A_TRY(build_scene(b, rep, stream, b->sort[0]));
+        A_TRY(build_scene(b, rep, stream, b->sort));
         char head[400];
         snprintf(head, sizeof(head), "%s{\"k\": %d, \"scenes\": %d, \"probe_scene\": %d, \"pixels\": %llu, "
                  "\"choice\": {\"leaf_size\": %d, \"tile\": %d, \"collect_max\": %d, \"merge_min\": %d, "

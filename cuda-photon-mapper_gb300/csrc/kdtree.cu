@@ -114,13 +114,13 @@ struct SubtreeScratch {
     float4 clo[2][2 * kSubtreeNodes], chi[2][2 * kSubtreeNodes];
 };
 
-__global__ void __launch_bounds__(kSubtreeThreads)
-    subtree_finish_kernel(const float4 *__restrict__ pos, uint32_t *order, uint32_t n, int l0, int D,
-                          uint32_t span0, const float4 *__restrict__ cell_lo,
-                          const float4 *__restrict__ cell_hi) {
-    extern __shared__ __align__(16) unsigned char subtree_smem[];
+extern __shared__ __align__(16) unsigned char subtree_smem[];
+
+// Subtree j of a tree (the node j at level l0); one CTA.
+__device__ __forceinline__ void subtree_finish(const float4 *__restrict__ pos, uint32_t *order, uint32_t n, int l0,
+                                               int D, uint32_t span0, const float4 *__restrict__ cell_lo,
+                                               const float4 *__restrict__ cell_hi, uint32_t j) {
     SubtreeScratch &ss = *reinterpret_cast<SubtreeScratch *>(subtree_smem);
-    const uint32_t j = blockIdx.x;
     const uint32_t start = j * span0;
     if (start >= n) return;
     const int cnt = (int)min(span0, n - start);
@@ -220,16 +220,21 @@ __global__ void __launch_bounds__(kSubtreeThreads)
     for (int t = tid; t < cnt; t += blockDim.x) order[start + t] = ss.idx[t];
 }
 
+__global__ void __launch_bounds__(kSubtreeThreads)
+    subtree_finish_kernel(const float4 *__restrict__ pos, uint32_t *order, uint32_t n, int l0, int D,
+                          uint32_t span0, const float4 *__restrict__ cell_lo,
+                          const float4 *__restrict__ cell_hi) {
+    subtree_finish(pos, order, n, l0, D, span0, cell_lo, cell_hi, blockIdx.x);
+}
+
 __global__ void iota_kernel(uint32_t *v, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) v[i] = i;
 }
 
-__global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
-                               const float4 *__restrict__ pos_in, const float4 *__restrict__ pow_in,
-                               float4 *pos_out, float4 *pow_out, float4 *dir_out) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void permute_one(const uint32_t *__restrict__ order, uint32_t i,
+                                            const float4 *__restrict__ pos_in, const float4 *__restrict__ pow_in,
+                                            float4 *pos_out, float4 *pow_out, float4 *dir_out) {
     uint32_t s = order[i];
     pos_out[i] = pos_in[s];
     if (pow_in) {
@@ -242,13 +247,18 @@ __global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
     }
 }
 
+__global__ void permute_kernel(const uint32_t *__restrict__ order, uint32_t n,
+                               const float4 *__restrict__ pos_in, const float4 *__restrict__ pow_in,
+                               float4 *pos_out, float4 *pow_out, float4 *dir_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) permute_one(order, i, pos_in, pow_in, pos_out, pow_out, dir_out);
+}
+
 // One warp per leaf slot: box of its (up to) 32 << leaf_shift records.
-__global__ void leaf_box_kernel(const float4 *__restrict__ pos, uint32_t n, uint32_t first_leaf,
-                                uint32_t leaf_slots, int leaf_shift, float4 *node_lo,
-                                float4 *node_hi) {
-    uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Leaf slot `warp` of a tree: one warp.
+__device__ __forceinline__ void leaf_box(const float4 *__restrict__ pos, uint32_t n, uint32_t first_leaf,
+                                         int leaf_shift, float4 *node_lo, float4 *node_hi, uint32_t warp) {
     int lane = threadIdx.x & 31;
-    if (warp >= leaf_slots) return;
     const float inf = __int_as_float(0x7f800000);
     float lx = inf, ly = inf, lz = inf, hx = -inf, hy = -inf, hz = -inf;
     for (int c = 0; c < (1 << leaf_shift); ++c) {
@@ -274,6 +284,13 @@ __global__ void leaf_box_kernel(const float4 *__restrict__ pos, uint32_t n, uint
     }
 }
 
+__global__ void leaf_box_kernel(const float4 *__restrict__ pos, uint32_t n, uint32_t first_leaf,
+                                uint32_t leaf_slots, int leaf_shift, float4 *node_lo,
+                                float4 *node_hi) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp < leaf_slots) leaf_box(pos, n, first_leaf, leaf_shift, node_lo, node_hi, warp);
+}
+
 __global__ void inner_box_kernel(uint32_t first, uint32_t count, float4 *node_lo, float4 *node_hi) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
@@ -285,7 +302,7 @@ __global__ void inner_box_kernel(uint32_t first, uint32_t count, float4 *node_lo
 }
 
 // Small levels: one CTA walks the top of the tree level by level.
-__global__ void top_box_kernel(uint32_t levels, float4 *node_lo, float4 *node_hi) {
+__device__ __forceinline__ void top_box(uint32_t levels, float4 *node_lo, float4 *node_hi) {
     for (int l = (int)levels - 1; l >= 0; --l) {
         uint32_t first = 1u << l;
         for (uint32_t i = threadIdx.x; i < first; i += blockDim.x) {
@@ -297,6 +314,10 @@ __global__ void top_box_kernel(uint32_t levels, float4 *node_lo, float4 *node_hi
         }
         __syncthreads();
     }
+}
+
+__global__ void top_box_kernel(uint32_t levels, float4 *node_lo, float4 *node_hi) {
+    top_box(levels, node_lo, node_hi);
 }
 
 
@@ -379,6 +400,69 @@ __global__ void split_cell_multi_kernel(const KdMultiMap *maps, int nmaps, const
     m.cell_hi[2 * g + 1] = rhi;
 }
 
+
+// The last map m with prefix[m] <= u (prefix: nmaps + 1 scanned counts).
+__device__ __forceinline__ int map_at(const uint32_t *prefix, int nmaps, uint32_t u) {
+    int lo = 0, hi = nmaps - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void multi_pad_kernel(const KdMultiMap *maps, const uint32_t *tile_map, uint32_t total) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const KdMultiMap &m = maps[multi_map(tile_map, i)];
+    const uint32_t j = i - m.base;
+    if (!m.pad_count || j >= m.n || j < *m.pad_count) return;
+    const float inf = __int_as_float(0x7f800000);
+    m.pad_pos[j] = make_float4(inf, inf, inf, __uint_as_float(j));
+    m.pad_pow[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void __launch_bounds__(kSubtreeThreads)
+    multi_subtree_kernel(const KdMultiMap *maps, int nmaps, const uint32_t *prefix, uint32_t *order) {
+    const KdMultiMap &m = maps[map_at(prefix, nmaps, blockIdx.x)];
+    const uint32_t span0 = (32u << m.leaf_shift) << (m.depth - m.lf);
+    subtree_finish(m.pos, order + m.base, m.n, m.lf, m.depth, span0, m.cell_lo, m.cell_hi,
+                   blockIdx.x - prefix[map_at(prefix, nmaps, blockIdx.x)]);
+}
+
+__global__ void multi_permute_kernel(const KdMultiMap *maps, const uint32_t *tile_map, uint32_t total,
+                                     const uint32_t *order) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const KdMultiMap &m = maps[multi_map(tile_map, i)];
+    const uint32_t j = i - m.base;
+    if (j < m.n) permute_one(order + m.base, j, m.pos, m.pow, m.pos_out, m.pow_out, m.dir_out);
+}
+
+__global__ void multi_leaf_kernel(const KdMultiMap *maps, int nmaps, const uint32_t *prefix) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= prefix[nmaps]) return;  // whole warps
+    const int mi = map_at(prefix, nmaps, w);
+    const KdMultiMap &m = maps[mi];
+    leaf_box(m.pos_out, m.n, 1u << m.depth, m.leaf_shift, m.cell_lo, m.cell_hi, w - prefix[mi]);
+}
+
+__global__ void multi_inner_kernel(const KdMultiMap *maps, int nmaps, const uint32_t *prefix, int level) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= prefix[nmaps]) return;
+    const int mi = map_at(prefix, nmaps, u);
+    const KdMultiMap &m = maps[mi];
+    const uint32_t nd = (1u << level) + (u - prefix[mi]);
+    const float4 a = m.cell_lo[2 * nd], b = m.cell_lo[2 * nd + 1];
+    const float4 c = m.cell_hi[2 * nd], d = m.cell_hi[2 * nd + 1];
+    m.cell_lo[nd] = make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+    m.cell_hi[nd] = make_float4(fmaxf(c.x, d.x), fmaxf(c.y, d.y), fmaxf(c.z, d.z), 0.0f);
+}
+
+__global__ void multi_top_kernel(const KdMultiMap *maps) {
+    const KdMultiMap &m = maps[blockIdx.x];
+    top_box((uint32_t)min(m.depth, 10), m.cell_lo, m.cell_hi);
+}
 }  // namespace
 
 int tree_depth(uint32_t n, int leaf_shift) {
@@ -521,6 +605,14 @@ cudaError_t kd_multi_create(const std::vector<KdBuildArgs> &args, KdMulti *k) {
         m.depth = tree_depth(a.n, a.leaf_shift);
         m.lf = lf_of(i);
         m.leaf_shift = a.leaf_shift;
+        m.pad_pos = const_cast<float4 *>(a.pos_in);
+        m.pad_pow = const_cast<float4 *>(a.pow_in);
+        m.pow = a.pow_in;
+        m.pos_out = a.pos_out;
+        m.pow_out = a.pow_out;
+        m.dir_out = a.dir_out;
+        m.pad_count = a.pad_count;
+        if (a.pad_count) k->pad = true;
         tiles += (a.n + kSortTile - 1) / kSortTile;
         k->levels = std::max(k->levels, m.lf);
         k->maps.push_back(m);
@@ -562,8 +654,41 @@ cudaError_t kd_multi_create(const std::vector<KdBuildArgs> &args, KdMulti *k) {
         k->level_nodes[l] = nodes;
         level_n[l] = k->level_tiles[l] * kSortTile;
     }
+    // the finish tables: subtrees, leaf slots, inner nodes of levels 10 ..
+    const int nm1 = k->nmaps + 1;
+    for (const KdMultiMap &m : k->maps) k->max_depth = std::max(k->max_depth, m.depth);
+    const int inner_levels = std::max(k->max_depth - 10, 0);
+    std::vector<uint32_t> fin((size_t)(2 + inner_levels) * nm1, 0);
+    k->inner_nodes.assign(inner_levels, 0);
+    uint32_t subs = 0, leaves = 0;
+    std::vector<uint32_t> inner(inner_levels, 0);
+    for (int mi = 0; mi < k->nmaps; ++mi) {
+        const KdMultiMap &m = k->maps[mi];
+        fin[mi] = subs;
+        fin[nm1 + mi] = leaves;
+        if (m.lf < m.depth) {
+            const uint32_t span0 = (32u << m.leaf_shift) << (m.depth - m.lf);
+            subs += (m.n + span0 - 1) / span0;
+        }
+        leaves += 1u << m.depth;
+        for (int l = 10; l < m.depth; ++l) {
+            fin[(size_t)(2 + l - 10) * nm1 + mi] = inner[l - 10];
+            inner[l - 10] += 1u << l;
+        }
+        for (int l = std::max(m.depth, 10); l < k->max_depth; ++l) fin[(size_t)(2 + l - 10) * nm1 + mi] = inner[l - 10];
+    }
+    fin[k->nmaps] = subs;
+    fin[nm1 + k->nmaps] = leaves;
+    for (int l = 0; l < inner_levels; ++l) {
+        fin[(size_t)(2 + l) * nm1 + k->nmaps] = inner[l];
+        k->inner_nodes[l] = inner[l];
+    }
+    k->subtrees = subs;
+    k->leaves = leaves;
     cudaError_t e;
 #define KM_TRY(x) do { e = (x); if (e != cudaSuccess) { kd_multi_free(*k); return e; } } while (0)
+    KM_TRY(kd_alloc(&k->fin_prefix, fin.size()));
+    KM_TRY(cudaMemcpy(k->fin_prefix, fin.data(), sizeof(uint32_t) * fin.size(), cudaMemcpyHostToDevice));
     KM_TRY(kd_alloc(&k->desc, k->nmaps));
     KM_TRY(kd_alloc(&k->tile_map, tile_map.size()));
     KM_TRY(kd_alloc(&k->seg_tab, seg.size()));
@@ -587,6 +712,7 @@ cudaError_t kd_multi_create(const std::vector<KdBuildArgs> &args, KdMulti *k) {
 void kd_multi_free(KdMulti &k) {
     cudaFree(k.desc); cudaFree(k.tile_map); cudaFree(k.seg_tab); cudaFree(k.node_prefix); cudaFree(k.level_n);
     cudaFree(k.keys); cudaFree(k.keys_tmp); cudaFree(k.vals); cudaFree(k.vals_tmp); cudaFree(k.hist);
+    cudaFree(k.fin_prefix);
     k = KdMulti();
 }
 
@@ -595,6 +721,10 @@ cudaError_t kd_multi_levels(KdMulti &k, cudaStream_t s, uint32_t **order) {
     uint32_t *va = k.vals, *vb = k.vals_tmp;
     *order = va;
     if (k.nmaps == 0) return cudaSuccess;
+    if (k.pad) {
+        multi_pad_kernel<<<(k.total + 255) / 256, 256, 0, s>>>(k.desc, k.tile_map, k.total);
+        note_launch();
+    }
     multi_init_kernel<<<(k.total + 255) / 256, 256, 0, s>>>(k.desc, k.tile_map, k.total, va);
     note_launch();
     multi_root_kernel<<<(k.nmaps + 127) / 128, 128, 0, s>>>(k.desc, k.nmaps);
@@ -618,6 +748,34 @@ cudaError_t kd_multi_levels(KdMulti &k, cudaStream_t s, uint32_t **order) {
         note_launch();
     }
     *order = va;
+    return cudaGetLastError();
+}
+
+cudaError_t kd_multi_finish(KdMulti &k, uint32_t *order, cudaStream_t s) {
+    if (k.nmaps == 0) return cudaSuccess;
+    const int nm1 = k.nmaps + 1;
+    cudaError_t e;
+    if (k.subtrees > 0) {
+        const int smem = (int)sizeof(SubtreeScratch);
+        e = cudaFuncSetAttribute(multi_subtree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        multi_subtree_kernel<<<k.subtrees, kSubtreeThreads, smem, s>>>(k.desc, k.nmaps, k.fin_prefix, order);
+        note_launch();
+    }
+    multi_permute_kernel<<<(k.total + 255) / 256, 256, 0, s>>>(k.desc, k.tile_map, k.total, order);
+    note_launch();
+    multi_leaf_kernel<<<(uint32_t)(((uint64_t)k.leaves * 32 + 255) / 256), 256, 0, s>>>(k.desc, k.nmaps,
+                                                                                          k.fin_prefix + nm1);
+    note_launch();
+    for (int l = k.max_depth - 1; l >= 10; --l) {
+        const uint32_t cnt = k.inner_nodes[l - 10];
+        if (cnt == 0) continue;
+        multi_inner_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(k.desc, k.nmaps, k.fin_prefix + (size_t)(2 + l - 10) * nm1,
+                                                             l);
+        note_launch();
+    }
+    multi_top_kernel<<<k.nmaps, 1024, 0, s>>>(k.desc);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -26,6 +26,9 @@ struct KdBuildArgs {
     uint32_t *hist;                  // radix_sort_hist_words(n)
     uint32_t *order_out;             // nullable: tree position -> record index
     int leaf_shift = 0;              // leaves of 32 << leaf_shift records
+    // multi build only (nullable): the records from *pad_count to n are set
+    // to infinity (position) and zero (power) before the build
+    const uint32_t *pad_count = nullptr;
 };
 
 cudaError_t build_tree(const KdBuildArgs &a, cudaStream_t s);
@@ -39,6 +42,10 @@ cudaError_t build_tree_finish(const KdBuildArgs &a, uint32_t *order, cudaStream_
 // finish (build_tree_finish). Each tree comes out as build_tree makes it.
 struct KdMultiMap {           // one map, device copy
     const float4 *pos;        // records in index order
+    float4 *pad_pos, *pad_pow;     // the same arrays, written by the padding
+    const float4 *pow;
+    float4 *pos_out, *pow_out, *dir_out;  // tree order
+    const uint32_t *pad_count;     // nullable
     float4 *cell_lo, *cell_hi;
     float4 root_lo, root_hi;  // the root cell
     uint32_t n;               // records
@@ -55,6 +62,13 @@ struct KdMulti {
     uint32_t *node_prefix = nullptr;    // per level: nmaps + 1 scanned node counts of the sorted maps
     uint32_t *level_n = nullptr;        // per level: pooled positions of the maps sorted at that level
     std::vector<uint32_t> level_tiles, level_nodes, level_maps;
+    // the finish of every map at once: scanned per-map counts of subtrees,
+    // leaf slots and (per level from 10 up) inner nodes
+    uint32_t *fin_prefix = nullptr;     // subtrees, leaves, then one row per inner level
+    uint32_t subtrees = 0, leaves = 0;
+    int max_depth = 0;
+    std::vector<uint32_t> inner_nodes;  // per level 10 .. max_depth - 1
+    bool pad = false;                   // some map pads its records
     uint32_t total = 0;                 // pooled positions
     uint64_t *keys = nullptr, *keys_tmp = nullptr;
     uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
@@ -63,8 +77,10 @@ struct KdMulti {
 // its tables and pooled scratch. Maps with no records are left out.
 cudaError_t kd_multi_create(const std::vector<KdBuildArgs> &args, KdMulti *k);
 void kd_multi_free(KdMulti &k);
-// The shared levels of every map; *order receives the pooled order (map i of
-// the build order at *order + maps[i].base).
+// The padding and the shared levels of every map; *order receives the
+// pooled order (map i of the build order at *order + maps[i].base).
 cudaError_t kd_multi_levels(KdMulti &k, cudaStream_t s, uint32_t **order);
+// Every map's finish (build_tree_finish) in shared launches.
+cudaError_t kd_multi_finish(KdMulti &k, uint32_t *order, cudaStream_t s);
 
 }  // namespace pm
