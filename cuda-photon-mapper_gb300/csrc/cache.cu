@@ -220,9 +220,11 @@ __device__ void encode_row(unsigned char *act, uint32_t sbo, int row, const Cach
                 const __half2 *lv = tab + (size_t)l * T;
 #pragma unroll
                 for (int k = 0; k < 8; ++k) {
+                    // fused (the library builds with contraction off): the
+                    // encoding has no bit-exact counterpart to match
                     const float2 h = __half22float2(__ldg(lv + idx[k]));
-                    f0 += w[k] * h.x;
-                    f1 += w[k] * h.y;
+                    f0 = __fmaf_rn(w[k], h.x, f0);
+                    f1 = __fmaf_rn(w[k], h.y, f1);
                 }
             }
             v[2 * j] = f0;
