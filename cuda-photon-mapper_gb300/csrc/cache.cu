@@ -207,7 +207,7 @@ __device__ void encode_row(unsigned char *act, uint32_t sbo, int row, const Cach
     }
     const QueryPos q = unit_pos(g, a);
     const size_t T = (size_t)1 << g.log2_t;
-#pragma unroll 1
+#pragma unroll
     for (int c = 0; c < 4; ++c) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
