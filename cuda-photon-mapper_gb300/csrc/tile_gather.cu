@@ -39,7 +39,12 @@ using namespace wknn;
 
 constexpr int kTileWarps = 4;
 constexpr int kAnchorAt = 15;                // the anchor: query 15 of a warp's chunk
-constexpr int kTileCap = 400;                // candidate records per warp (the most at 5 blocks of 4 warps per SM)
+// Residency before capacity: 7 blocks of 4 warps per SM (the registers capped
+// at 72, a few spilled) with candidate sets of 272 records measured faster
+// than 5 blocks with 400 (more groups halve, but more warps hide the
+// latency of every phase).
+constexpr int kTileBlocks = 7;
+constexpr int kTileCap = 272;                // candidate records per warp (fits 7 blocks' shared memory)
 constexpr int kScanSlots = 2;   // candidates per lane per step of the selection scan
 constexpr int kPickSlots = 1;   // band entries per lane per step of the final selection
 constexpr float kRel = 2e-4f;                // relative and absolute margins of the distance bounds
@@ -649,7 +654,7 @@ __device__ __forceinline__ void tile_chunk(const PScene &Sc, const MapView &surf
 }
 
 template <int S>
-__global__ void __launch_bounds__(kTileWarps * 32, 5)
+__global__ void __launch_bounds__(kTileWarps * 32, kTileBlocks)
     query_knn_tile_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
                           const uint32_t *order, uint32_t n, const uint32_t *n_dev, int groups,
                           const float *anchor_d, int k, float r2cap, bool raw, float4 *out,
@@ -690,7 +695,7 @@ __device__ __forceinline__ int scene_of_chunk(const TileScene *scenes, int nsc, 
 // memory, chunks numbered scene after scene): one persistent launch; a warp
 // loads a scene's arguments when its next chunk belongs to another scene.
 template <int S>
-__global__ void __launch_bounds__(kTileWarps * 32, 5)
+__global__ void __launch_bounds__(kTileWarps * 32, kTileBlocks)
     query_knn_tile_multi_kernel(const TileScene *scenes, int nsc, uint32_t total_chunks, int groups,
                                 const float *anchor_d, bool raw, uint32_t *defer_list,
                                 uint32_t *defer_sc, uint32_t *defer_n, uint32_t *chunk_counter,
