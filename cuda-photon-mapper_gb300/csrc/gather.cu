@@ -229,8 +229,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
 // out[order[j]]: the exact estimate query_knn_kernel computes, or with raw
 // set the flux sum and the squared radius (-1 when nothing was found), from
 // which the render's own arithmetic finishes the estimate.
+// 9 blocks of 4 warps per SM (registers capped): the residency that measured
+// fastest (7 by registers alone, 12 spilled too much).
 template <int S>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 9)
     query_knn_run_kernel(PScene Sc, MapView surf, MapView vol, const float4 *qa, const float4 *qd,
                          const uint32_t *sel, const uint32_t *order, uint32_t n, int run, int k,
                          float r2cap, bool raw, float4 *out, uint32_t *run_ctr) {
