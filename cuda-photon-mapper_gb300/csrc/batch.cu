@@ -87,6 +87,89 @@ __global__ void query_gathers_kernel(const uint32_t *off_total, const uint32_t *
     }
 }
 
+// The same for every scene of the batched list launches.
+__global__ void list_gathers_kernel(const ListScene *ls, const int *ids, int n, unsigned long long *gathers) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int s = ids[j];
+    const ListScene &d = ls[s];
+    const uint32_t all = d.off[d.npix], surf = d.soff[d.npix];
+    gathers[2 * s] = surf;
+    gathers[2 * s + 1] = (unsigned long long)all - surf;
+}
+
+// Segments of whole sort tiles laid out one after another in a pool (a
+// scene's path counts of one map, its per-pixel counts, its query slice),
+// cut into runs of at most kRunMax items that one segmented scan or sort
+// handles. tab holds, per tile of the pool, its segment's first tile
+// (counted from the run's first tile) and the segment's tile count.
+constexpr size_t kRunMax = (size_t)1 << 31;
+struct SegRuns {
+    struct Run {
+        size_t first;
+        uint32_t n;
+    };
+    std::vector<Run> runs;
+    uint2 *tab = nullptr;
+    uint32_t *n_dev = nullptr;  // per run: its item count
+    uint32_t max_n = 0;
+};
+
+void seg_runs_free(SegRuns &r) {
+    cudaFree(r.tab);
+    cudaFree(r.n_dev);
+    r = SegRuns();
+}
+
+// Lays out segments of seg_items[i] items, each rounded up to whole tiles:
+// first[i] its first item; *total the pool's items.
+cudaError_t seg_runs_build(const std::vector<size_t> &seg_items, SegRuns *r, std::vector<size_t> *first,
+                           size_t *total) {
+    seg_runs_free(*r);
+    std::vector<uint2> tab;
+    first->assign(seg_items.size(), 0);
+    size_t pos = 0, run_first = 0, run_n = 0;
+    for (size_t i = 0; i < seg_items.size(); ++i) {
+        const size_t tiles = (seg_items[i] + kSortTile - 1) / kSortTile, items = tiles * kSortTile;
+        if (items > kRunMax) return cudaErrorInvalidValue;
+        if (run_n + items > kRunMax) {
+            r->runs.push_back({run_first, (uint32_t)run_n});
+            run_first = pos;
+            run_n = 0;
+        }
+        (*first)[i] = pos;
+        const uint32_t t0 = (uint32_t)(run_n / kSortTile);
+        for (size_t k = 0; k < tiles; ++k) tab.push_back(make_uint2(t0, (uint32_t)tiles));
+        run_n += items;
+        pos += items;
+    }
+    if (run_n > 0) r->runs.push_back({run_first, (uint32_t)run_n});
+    *total = pos;
+    std::vector<uint32_t> ns;
+    for (const auto &run : r->runs) {
+        ns.push_back(run.n);
+        r->max_n = std::max(r->max_n, run.n);
+    }
+    cudaError_t e = dalloc(&r->tab, tab.size());
+    if (e == cudaSuccess && !tab.empty())
+        e = cudaMemcpy(r->tab, tab.data(), sizeof(uint2) * tab.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = dalloc(&r->n_dev, ns.size());
+    if (e == cudaSuccess && !ns.empty())
+        e = cudaMemcpy(r->n_dev, ns.data(), sizeof(uint32_t) * ns.size(), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// Segmented exclusive scans of every run of a pool: out[i] counts in[]
+// from the first item of i's segment.
+cudaError_t scan_runs(const SegRuns &r, const uint32_t *in, uint32_t *out, uint32_t *tmp, cudaStream_t st) {
+    for (const auto &run : r.runs) {
+        cudaError_t e = exclusive_scan_u32_segmented(in + run.first, out + run.first, run.n,
+                                                     r.tab + run.first / kSortTile, tmp, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 }  // namespace
 }  // namespace pm
 
@@ -108,11 +191,15 @@ struct pm_batch {
     };
     std::vector<Map> maps;             // 2 per scene
     std::vector<uint32_t> path_cap;    // per scene
-    std::vector<size_t> cnt_off;       // offset of scene s's counts in the pools
+    std::vector<size_t> cnt_off;       // per map (2 per scene): first word of its counts in the pools
     std::vector<size_t> pix_off;       // offset of scene s's pixels in the image pools
     std::vector<pm_batch_tune> tune;
-    uint32_t *cnt = nullptr, *off = nullptr;  // pools: per scene [cnt_s | cnt_v] over the path cap
+    // pools: per scene and map the per-path record counts over the path cap
+    // and their scan, each map a segment of whole tiles
+    uint32_t *cnt = nullptr, *off = nullptr;
     size_t cnt_words = 0;
+    SegRuns cnt_runs;
+    ExtentJob *ext_jobs = nullptr;     // 2 per scene
     uint32_t *scan_tmp = nullptr;
     uint32_t *words = nullptr;         // kWords per scene
     uint32_t *capn = nullptr;          // 2 per scene: map capacities (device n of the builds)
@@ -145,17 +232,33 @@ struct pm_batch {
         size_t pix_cap = 0, q_cap = 0;
     } q;
     std::vector<uint32_t> nq;  // queries per scene
-    // The frame's estimate pass over every query-list scene at once: their
-    // query records, values, sorted orders and per-pixel scans side by side
-    // ("arena"), one descriptor per scene grouped by k-list width, and one
-    // persistent launch per width.
+    // The query lists of every query-list scene side by side ("arena"): a
+    // pool of per-pixel words (counts, scans, diffuse-query lists; npix + 1
+    // per scene) and a pool of query slots (records, values, sorted order),
+    // each scene a segment of whole sort tiles, so that one launch sequence
+    // counts, scans, writes and sorts all scenes' lists. Then one
+    // descriptor per scene grouped by k-list width and one persistent
+    // estimate launch per width, and one composite launch.
     struct Arena {
         float4 *qa = nullptr, *qd = nullptr, *val = nullptr;
         uint32_t *ord = nullptr, *off = nullptr;
+        uint32_t *cnt = nullptr, *scnt = nullptr, *soff = nullptr, *slist = nullptr;  // pixel pool
         uint32_t *defer = nullptr, *defer_sc = nullptr, *defer_n = nullptr;
         float *anchor_d = nullptr;
         TileScene *desc = nullptr;
-        std::vector<size_t> q_off, p_off;  // per scene: first query, first scan word
+        std::vector<size_t> q_off, p_off;  // per scene: first query slot, first pixel word
+        size_t q_total = 0, p_total = 0;
+        SegRuns q_runs, p_runs;
+        int *tile_scene = nullptr;         // per tile of the query pool: its scene
+        uint32_t *scan_tmp = nullptr, *hist = nullptr;
+        // the scenes of the batched list launches: descriptors of every
+        // scene, the ids of those in the query-list render and their
+        // 128-pixel block prefix
+        ListScene *lists = nullptr;
+        int *list_ids = nullptr;
+        uint32_t *list_blk = nullptr;
+        int n_list = 0;
+        uint32_t list_blocks = 0;
         int class_first[5] = {}, class_n[5] = {};
         uint32_t class_chunks[5] = {};
         bool on = false;
@@ -208,6 +311,8 @@ void free_batch(pm_batch *b) {
     }
     for (float *h : b->het) cudaFree(h);
     cudaFree(b->cnt); cudaFree(b->off); cudaFree(b->scan_tmp); cudaFree(b->words);
+    seg_runs_free(b->cnt_runs);
+    cudaFree(b->ext_jobs);
     cudaFree(b->capn); cudaFree(b->gathers); cudaFree(b->work); cudaFree(b->rad); cudaFree(b->rgba);
     cudaFree(b->scenes_dev); cudaFree(b->count_dev); cudaFree(b->write_dev);
     cudaFree(b->render_dev); cudaFree(b->prefix_dev);
@@ -222,6 +327,11 @@ void free_batch(pm_batch *b) {
     cudaFree(ar.qa); cudaFree(ar.qd); cudaFree(ar.val); cudaFree(ar.ord); cudaFree(ar.off);
     cudaFree(ar.defer); cudaFree(ar.defer_sc); cudaFree(ar.defer_n); cudaFree(ar.anchor_d);
     cudaFree(ar.desc);
+    cudaFree(ar.cnt); cudaFree(ar.scnt); cudaFree(ar.soff); cudaFree(ar.slist);
+    seg_runs_free(ar.q_runs);
+    seg_runs_free(ar.p_runs);
+    cudaFree(ar.tile_scene); cudaFree(ar.scan_tmp); cudaFree(ar.hist);
+    cudaFree(ar.lists); cudaFree(ar.list_ids); cudaFree(ar.list_blk);
     delete b;
 }
 
@@ -366,11 +476,73 @@ cudaError_t enqueue_query_scene(pm_batch *b, int s, cudaStream_t st) {
 
 constexpr int kTileGroups = 4;  // groups of 32 queries per chunk of the estimate pass
 
-// Uploads the estimate pass's scene descriptors: the query-list scenes
-// grouped by k-list width, chunks numbered scene after scene within a width.
+// The sort box of scene s's queries: the scene box with a 1 % margin.
+CacheGrid sort_box(const pm_batch *b, int s) {
+    CacheGrid box;
+    memset(&box, 0, sizeof(box));
+    const pm_scene &sc = b->scenes[s];
+    for (int a = 0; a < 3; ++a) {
+        const float ext = sc.box_max[a] - sc.box_min[a];
+        const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
+        box.lo[a] = sc.box_min[a] - m;
+        const float size = ext + 2.0f * m;
+        box.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
+    }
+    return box;
+}
+
+// Uploads the list launches' scene descriptors (every scene; on for the
+// query-list scenes with pixels, whose ids and block prefix follow) and
+// the estimate pass's: the query-list scenes grouped by k-list width,
+// chunks numbered scene after scene within a width.
 cudaError_t upload_tile_scenes(pm_batch *b) {
     auto &ar = b->ar;
     if (!ar.on) return cudaSuccess;
+    {
+        std::vector<ListScene> ls(b->n);
+        std::vector<int> ids;
+        std::vector<uint32_t> blk(1, 0u);
+        for (int s = 0; s < b->n; ++s) {
+            const BatchRenderScene r = render_desc(b, s);
+            ListScene &l = ls[s];
+            memset(&l, 0, sizeof(l));
+            const pm_config &c = b->cfgs[s];
+            l.sc = r.sc;
+            l.R = r.R;
+            l.npix = (uint32_t)c.width * (uint32_t)c.height;
+            bool vol_on, surf_on;
+            query_flags(b, s, &vol_on, &surf_on);
+            l.vol_on = vol_on;
+            l.surf_on = surf_on;
+            l.on = b->tune[s].query_list && l.npix > 0;
+            l.nq = b->nq[s];
+            l.q_first = ar.q_off[s];
+            l.box = sort_box(b, s);
+            l.cnt = ar.cnt + ar.p_off[s];
+            l.scnt = ar.scnt + ar.p_off[s];
+            l.off = ar.off + ar.p_off[s];
+            l.soff = ar.soff + ar.p_off[s];
+            l.qa = ar.qa + ar.q_off[s];
+            l.qd = ar.qd + ar.q_off[s];
+            l.slist = ar.slist + ar.p_off[s];
+            l.raw = ar.val + ar.q_off[s];
+            l.exposure = c.exposure;
+            l.rad = r.rad;
+            l.rgba = r.rgba;
+            if (l.on) {
+                ids.push_back(s);
+                blk.push_back(blk.back() + (l.npix + kListBlock - 1) / kListBlock);
+            }
+        }
+        ar.n_list = (int)ids.size();
+        ar.list_blocks = blk.back();
+        cudaError_t e = cudaMemcpy(ar.lists, ls.data(), sizeof(ListScene) * ls.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && !ids.empty())
+            e = cudaMemcpy(ar.list_ids, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(ar.list_blk, blk.data(), sizeof(uint32_t) * blk.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+    }
     std::vector<TileScene> d;
     for (int c = 1; c <= 4; ++c) {
         ar.class_first[c] = (int)d.size();
@@ -400,54 +572,41 @@ cudaError_t upload_tile_scenes(pm_batch *b) {
     return cudaMemcpy(ar.desc, d.data(), sizeof(TileScene) * d.size(), cudaMemcpyHostToDevice);
 }
 
-// Scene s's query list into the arena: per-pixel counts and scans, the
-// records, then their (map, Morton) order.
-cudaError_t enqueue_arena_queries(pm_batch *b, int s, cudaStream_t st) {
-    auto &q = b->q;
+// The query lists of every query-list scene into the arena: per-pixel
+// counts, their scans restarted at each scene, the records, the gather
+// counters, then each scene's (map, Morton) order by one segmented sort
+// (the sort keys and their second buffer live in the value array, the
+// second index buffer in the deferred-query list: both are free until the
+// estimate pass).
+cudaError_t enqueue_lists(pm_batch *b, cudaStream_t st) {
     auto &ar = b->ar;
-    const BatchRenderScene d = render_desc(b, s);
-    const pm_config &c = b->cfgs[s];
-    const uint32_t npix = (uint32_t)c.width * (uint32_t)c.height;
-    const uint32_t nq = b->nq[s];
-    if (npix == 0) return cudaSuccess;
-    bool vol_on, surf_on;
-    query_flags(b, s, &vol_on, &surf_on);
-    uint32_t *off = ar.off + ar.p_off[s];
-    float4 *qa = ar.qa + ar.q_off[s], *qd = ar.qd + ar.q_off[s];
-    uint32_t *ord = ar.ord + ar.q_off[s];
     cudaError_t e;
 #define Q_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
-    Q_TRY(cache_count_queries(d.sc, d.R, vol_on, surf_on, q.cnt, q.scnt, st));
-    Q_TRY(exclusive_scan_u32_large(q.cnt, off, npix, off + npix, q.scan_tmp, st));
-    Q_TRY(exclusive_scan_u32_large(q.scnt, q.soff, npix, q.soff + npix, q.scan_tmp, st));
-    Q_TRY(cache_write_queries(d.sc, d.R, vol_on, surf_on, off, q.soff, qa, qd, q.slist, st));
-    query_gathers_kernel<<<1, 32, 0, st>>>(off + npix, q.soff + npix, b->gathers + 2 * s);
+    Q_TRY(list_count_multi(ar.lists, ar.list_ids, ar.list_blk, ar.n_list, ar.list_blocks, st));
+    Q_TRY(scan_runs(ar.p_runs, ar.cnt, ar.off, ar.scan_tmp, st));
+    Q_TRY(scan_runs(ar.p_runs, ar.scnt, ar.soff, ar.scan_tmp, st));
+    Q_TRY(list_write_multi(ar.lists, ar.list_ids, ar.list_blk, ar.n_list, ar.list_blocks, st));
+    list_gathers_kernel<<<(ar.n_list + 127) / 128, 128, 0, st>>>(ar.lists, ar.list_ids, ar.n_list, b->gathers);
     note_launch();
     Q_TRY(cudaGetLastError());
-    if (nq > 0) {
-        CacheGrid box;
-        memset(&box, 0, sizeof(box));
-        const pm_scene &sc = b->scenes[s];
-        for (int a = 0; a < 3; ++a) {
-            const float ext = sc.box_max[a] - sc.box_min[a];
-            const float m = 0.01f * (ext > 0.0f ? ext : 1.0f);
-            box.lo[a] = sc.box_min[a] - m;
-            const float size = ext + 2.0f * m;
-            box.inv_size[a] = size > 0.0f ? 1.0f / size : 1.0f;
-        }
-        Q_TRY(cache_sample_keys(box, qa, nullptr, nq, q.key, ord, st));
+    uint32_t *keys = reinterpret_cast<uint32_t *>(ar.val), *keys_tmp = keys + ar.q_total;
+    for (size_t r = 0; r < ar.q_runs.runs.size(); ++r) {
+        const auto &run = ar.q_runs.runs[r];
+        Q_TRY(list_keys_multi(ar.lists, ar.tile_scene, run.first, run.n, keys + run.first, ar.ord + run.first, st));
         uint32_t *ok_keys = nullptr, *ok_vals = nullptr;
-        Q_TRY(radix_sort_pairs_u32(q.key, ord, q.key_tmp, q.ord_tmp, off + npix, nq, 0, 31, q.hist, st, &ok_keys,
-                                   &ok_vals));
-        if (ok_vals != ord)
-            Q_TRY(cudaMemcpyAsync(ord, ok_vals, sizeof(uint32_t) * nq, cudaMemcpyDeviceToDevice, st));
+        Q_TRY(radix_sort_pairs_u32(keys + run.first, ar.ord + run.first, keys_tmp + run.first, ar.defer + run.first,
+                                   ar.q_runs.n_dev + r, run.n, 0, 31, ar.hist, st, &ok_keys, &ok_vals, 0,
+                                   ar.q_runs.tab + run.first / kSortTile));
+        if (ok_vals != ar.ord + run.first)
+            Q_TRY(cudaMemcpyAsync(ar.ord + run.first, ok_vals, sizeof(uint32_t) * run.n, cudaMemcpyDeviceToDevice,
+                                  st));
     }
 #undef Q_TRY
     return cudaSuccess;
 }
 
 // The estimate pass of every query-list scene (one persistent launch per
-// k-list width), then each scene's composite.
+// k-list width), then the composite of all of them.
 cudaError_t enqueue_arena_estimates(pm_batch *b, cudaStream_t st) {
     auto &ar = b->ar;
     cudaError_t e;
@@ -458,23 +617,12 @@ cudaError_t enqueue_arena_estimates(pm_batch *b, cudaStream_t st) {
                                    true, buf, ar.defer_sc, b->sm_count, st);
         if (e != cudaSuccess) return e;
     }
-    for (int s = 0; s < b->n; ++s) {
-        if (!b->tune[s].query_list) continue;
-        const BatchRenderScene d = render_desc(b, s);
-        const pm_config &c = b->cfgs[s];
-        const uint32_t npix = (uint32_t)c.width * (uint32_t)c.height;
-        if (npix == 0) continue;
-        e = render_composite(d.sc, ar.off + ar.p_off[s], ar.qa + ar.q_off[s], ar.qd + ar.q_off[s],
-                             ar.val + ar.q_off[s], npix, c.exposure, d.rad, d.rgba, st);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    return list_composite_multi(ar.lists, ar.list_ids, ar.list_blk, ar.n_list, ar.list_blocks, st);
 }
 
-// Scene s's cached frame, right after its query list was built into the
-// arena (the list of its diffuse queries is then in q.slist): the frame's
-// picks and k-NN targets, the Adam steps of its network, inference over
-// every query and the composite.
+// Scene s's cached frame, after the query lists were built into the
+// arena: the frame's picks and k-NN targets, the Adam steps of its
+// network, inference over every query and the composite.
 cudaError_t enqueue_scene_cache(pm_batch *b, int s, cudaStream_t st) {
     auto &ar = b->ar;
     auto &c = b->caches[s];
@@ -490,7 +638,7 @@ cudaError_t enqueue_scene_cache(pm_batch *b, int s, cudaStream_t st) {
     cudaError_t e;
 #define S_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
     S_TRY(cache_pick_and_target(cf, c.grid, 0, c.ctr + 1, b->dsc[s], d.surf, d.vol, cfg.k, cfg.radius, qa, qd, nq,
-                                b->q.slist, b->nsurf[s], t, b->sm_count, st));
+                                ar.slist + ar.p_off[s], b->nsurf[s], t, b->sm_count, st));
     S_TRY(cache_scale_init(t.tgt, ns, t.scale_sum, c.dev, st));
     S_TRY(cudaMemsetAsync(c.p.loss, 0, sizeof(float), st));
     const uint32_t nb = cache_batch_count(ns, cf.batch);
@@ -552,29 +700,50 @@ cudaError_t size_query_buffers(pm_batch *b) {
     Z_TRY(dalloc(&q.anchor_d, tile_chunks((uint32_t)max_q, 4)));
     Z_TRY(dalloc(&q.defer_n, 2));  // deferred count, chunk counter
     q.q_cap = max_q;
-    // the arena of the batched estimate pass: every scene's queries
+    // the arena: every scene's pixel words and query slots, each a
+    // segment of whole sort tiles
     auto &ar = b->ar;
-    size_t q_total = 0, p_total = 0, max_chunks = 1;
-    ar.q_off.assign(b->n, 0);
-    ar.p_off.assign(b->n, 0);
+    size_t max_chunks = 1;
+    std::vector<size_t> q_items(b->n), p_items(b->n);
     for (int s = 0; s < b->n; ++s) {
-        ar.q_off[s] = q_total;
-        ar.p_off[s] = p_total;
-        q_total += b->nq[s];
-        p_total += (size_t)b->cfgs[s].width * b->cfgs[s].height + 1;
+        q_items[s] = b->nq[s];
+        p_items[s] = (size_t)b->cfgs[s].width * b->cfgs[s].height + 1;
         max_chunks += tile_chunks(b->nq[s], kTileGroups);
     }
-    q_total = std::max<size_t>(q_total, 1);
+    Z_TRY(seg_runs_build(q_items, &ar.q_runs, &ar.q_off, &ar.q_total));
+    Z_TRY(seg_runs_build(p_items, &ar.p_runs, &ar.p_off, &ar.p_total));
+    const size_t q_total = std::max<size_t>(ar.q_total, 1), p_total = ar.p_total;
     Z_TRY(dalloc(&ar.qa, q_total));
     Z_TRY(dalloc(&ar.qd, q_total));
     Z_TRY(dalloc(&ar.val, q_total));
     Z_TRY(dalloc(&ar.ord, q_total));
     Z_TRY(dalloc(&ar.off, p_total));
+    Z_TRY(dalloc(&ar.cnt, p_total));
+    Z_TRY(dalloc(&ar.scnt, p_total));
+    Z_TRY(dalloc(&ar.soff, p_total));
+    Z_TRY(dalloc(&ar.slist, p_total));
+    // counts past each scene's pixels (and of scenes outside the list
+    // render) stay 0
+    Z_TRY(cudaMemset(ar.cnt, 0, sizeof(uint32_t) * p_total));
+    Z_TRY(cudaMemset(ar.scnt, 0, sizeof(uint32_t) * p_total));
     Z_TRY(dalloc(&ar.defer, q_total));
     Z_TRY(dalloc(&ar.defer_sc, q_total));
     Z_TRY(dalloc(&ar.defer_n, 2));
     Z_TRY(dalloc(&ar.anchor_d, max_chunks));
     Z_TRY(dalloc(&ar.desc, (size_t)b->n));
+    Z_TRY(dalloc(&ar.lists, (size_t)b->n));
+    Z_TRY(dalloc(&ar.list_ids, (size_t)b->n));
+    Z_TRY(dalloc(&ar.list_blk, (size_t)b->n + 1));
+    Z_TRY(dalloc(&ar.scan_tmp, scan_tile_count(std::max(ar.p_runs.max_n, 1u)) + 1));
+    Z_TRY(dalloc(&ar.hist, radix_sort_hist_words(std::max(ar.q_runs.max_n, 1u))));
+    {
+        std::vector<int> ts(std::max<size_t>(ar.q_total / kSortTile, 1), -1);
+        for (int s = 0; s < b->n; ++s)
+            for (size_t t = ar.q_off[s] / kSortTile; t < (ar.q_off[s] + q_items[s] + kSortTile - 1) / kSortTile; ++t)
+                ts[t] = s;
+        Z_TRY(dalloc(&ar.tile_scene, ts.size()));
+        Z_TRY(cudaMemcpy(ar.tile_scene, ts.data(), sizeof(int) * ts.size(), cudaMemcpyHostToDevice));
+    }
     ar.on = true;
     Z_TRY(upload_tile_scenes(b));
 #undef Z_TRY
@@ -641,15 +810,10 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
     B_TRY(cudaMemsetAsync(b->cnt, 0, sizeof(uint32_t) * b->cnt_words, st));
     B_TRY(cudaMemsetAsync(b->gathers, 0, sizeof(unsigned long long) * 2 * b->n, st));
     B_TRY(trace_photons_batch(b->scenes_dev, b->count_dev, b->n, b->sm_count, st));
-    for (int s = 0; s < b->n; ++s) {
-        uint32_t *w = b->words + s * kWords;
-        const uint32_t cap = b->path_cap[s];
-        const size_t o = b->cnt_off[s];
-        B_TRY(map_extent_dev(cap, w + W_COUNTER, b->cnt + o, b->off + o, w + W_TOTAL_S, b->scan_tmp,
-                             b->cfgs[s].surface_photons, w + W_EXT_S, st));
-        B_TRY(map_extent_dev(cap, w + W_COUNTER, b->cnt + o + cap, b->off + o + cap, w + W_TOTAL_V,
-                             b->scan_tmp, b->cfgs[s].volume_photons, w + W_EXT_V, st));
-    }
+    // every map's record extent: the scans of all path counts, then one
+    // search per map
+    B_TRY(scan_runs(b->cnt_runs, b->cnt, b->off, b->scan_tmp, st));
+    B_TRY(map_extents_multi(b->ext_jobs, 2 * b->n, st));
     reset_counters_kernel<<<(b->n + 127) / 128, 128, 0, st>>>(b->words, b->n);
     note_launch();
     B_TRY(cudaGetLastError());
@@ -661,12 +825,15 @@ cudaError_t enqueue_frame(pm_batch *b, cudaStream_t st) {
     B_TRY(kd_multi_levels(b->kd, st, &order));
     B_TRY(kd_multi_finish(b->kd, order, st));
     if (b->n_pixel > 0) B_TRY(render_batch(b->render_dev, b->prefix_dev, b->n_pixel, b->work, b->sm_count, st));
-    for (int s = 0; s < b->n; ++s) {
-        if (!b->tune[s].query_list) continue;
-        B_TRY(enqueue_arena_queries(b, s, st));
-        if (b->cache_on) B_TRY(enqueue_scene_cache(b, s, st));
+    if (b->ar.n_list > 0) {
+        B_TRY(enqueue_lists(b, st));
+        if (b->cache_on) {
+            for (int s = 0; s < b->n; ++s)
+                if (b->tune[s].query_list) B_TRY(enqueue_scene_cache(b, s, st));
+        } else {
+            B_TRY(enqueue_arena_estimates(b, st));
+        }
     }
-    if (!b->cache_on) B_TRY(enqueue_arena_estimates(b, st));
 #undef B_TRY
     return cudaSuccess;
 }
@@ -705,8 +872,9 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     b->tune.resize(n);
     cudaError_t e = cudaSuccess;
 #define C_TRY(x) do { e = (x); if (e != cudaSuccess) { free_batch(b); return check_cuda(ctx, e, #x); } } while (0)
-    size_t cnt_words = 0, pix = 0;
-    uint32_t max_cap = 0, max_map = 1;
+    size_t pix = 0;
+    uint32_t max_map = 1;
+    std::vector<size_t> map_counts;  // per map: path cap (one segment of the count pools each)
     for (int s = 0; s < n; ++s) {
         const pm_config &c = cfgs[s];
         b->tune[s] = pm_batch_tune{c.leaf_size, 1, 128, 16, 1};
@@ -715,9 +883,8 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
         cap = std::max<uint64_t>(cap, 1024);
         if (cap > (1ull << 30)) { free_batch(b); return fail(ctx, PM_ERR_LIMIT, "path cap above 2^30"); }
         b->path_cap.push_back((uint32_t)cap);
-        b->cnt_off.push_back(cnt_words);
-        cnt_words += 2 * cap;
-        max_cap = std::max(max_cap, (uint32_t)cap);
+        map_counts.push_back(cap);
+        map_counts.push_back(cap);
         b->pix_off.push_back(pix);
         pix += (size_t)c.width * (size_t)c.height;
         const uint32_t targets[2] = {c.surface_photons, c.volume_photons};
@@ -741,10 +908,11 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
         }
         b->dsc.push_back(to_device_scene(scenes[s], b->het[s]));
     }
-    b->cnt_words = cnt_words;
-    C_TRY(dalloc(&b->cnt, cnt_words));
-    C_TRY(dalloc(&b->off, cnt_words));
-    C_TRY(dalloc(&b->scan_tmp, scan_tile_count(max_cap) + 1));
+    C_TRY(seg_runs_build(map_counts, &b->cnt_runs, &b->cnt_off, &b->cnt_words));
+    C_TRY(dalloc(&b->cnt, b->cnt_words));
+    C_TRY(dalloc(&b->off, b->cnt_words));
+    C_TRY(dalloc(&b->scan_tmp, scan_tile_count(b->cnt_runs.max_n) + 1));
+    C_TRY(dalloc(&b->ext_jobs, 2 * (size_t)n));
     C_TRY(dalloc(&b->words, (size_t)kWords * n));
     C_TRY(dalloc(&b->capn, 2 * (size_t)n));
     C_TRY(dalloc(&b->gathers, 2 * (size_t)n));
@@ -764,13 +932,25 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     // static per-scene parameters
     std::vector<uint32_t> capn(2 * (size_t)n);
     std::vector<TraceParams> cp(n), wp(n);
+    std::vector<ExtentJob> jobs(2 * (size_t)n);
     for (int s = 0; s < n; ++s) {
         const pm_config &c = cfgs[s];
         capn[2 * s] = b->maps[2 * s].cap;
         capn[2 * s + 1] = b->maps[2 * s + 1].cap;
         uint32_t *w = b->words + s * kWords;
-        const size_t o = b->cnt_off[s];
+        const size_t os = b->cnt_off[2 * s], ov = b->cnt_off[2 * s + 1];
         const uint32_t cap = b->path_cap[s];
+        for (int m = 0; m < 2; ++m) {
+            ExtentJob &j = jobs[2 * s + m];
+            const size_t o = m == 0 ? os : ov;
+            j.cnt = b->cnt + o;
+            j.off = b->off + o;
+            j.cap = cap;
+            j.target = m == 0 ? c.surface_photons : c.volume_photons;
+            j.issued = w + W_COUNTER;
+            j.total = w + (m == 0 ? W_TOTAL_S : W_TOTAL_V);
+            j.extent = w + (m == 0 ? W_EXT_S : W_EXT_V);
+        }
         TraceParams P;
         memset(&P, 0, sizeof(P));
         P.seed = c.seed;
@@ -783,12 +963,12 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
         P.path_counter = w + W_COUNTER;
         P.stored_s = w + W_STORED_S;
         P.stored_v = w + W_STORED_V;
-        P.cnt_s = b->cnt + o;
-        P.cnt_v = b->cnt + o + cap;
+        P.cnt_s = b->cnt + os;
+        P.cnt_v = b->cnt + ov;
         cp[s] = P;
         P.store = 1;
-        P.off_s = b->off + o;
-        P.off_v = b->off + o + cap;
+        P.off_s = b->off + os;
+        P.off_v = b->off + ov;
         P.ext_s = w + W_EXT_S;
         P.ext_v = w + W_EXT_V;
         P.power = scenes[s].light_power;
@@ -800,6 +980,7 @@ pm_status pm_batch_create(pm_ctx *ctx, int n, const pm_scene *scenes, const pm_c
     C_TRY(cudaMemcpy(b->scenes_dev, b->dsc.data(), sizeof(PScene) * n, cudaMemcpyHostToDevice));
     C_TRY(cudaMemcpy(b->count_dev, cp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
     C_TRY(cudaMemcpy(b->write_dev, wp.data(), sizeof(TraceParams) * n, cudaMemcpyHostToDevice));
+    C_TRY(cudaMemcpy(b->ext_jobs, jobs.data(), sizeof(ExtentJob) * jobs.size(), cudaMemcpyHostToDevice));
     C_TRY(upload_pixel_scenes(b));
     C_TRY(size_query_buffers(b));
     C_TRY(plan_trees(b));

@@ -28,6 +28,7 @@
 #include "cache.cuh"
 #include "eye_path.cuh"
 #include "launch_count.cuh"
+#include "radix_sort.cuh"
 #include "tc.cuh"
 
 #include <cuda_bf16.h>
@@ -824,12 +825,14 @@ struct CountSink {
 // the block's counts sorted ascending in shared memory: `base` the first
 // slot of step s, `live` the lanes with more than s queries.
 constexpr int kListWarps = 4;  // warps (pixel blocks) per CTA of the list kernels
+static_assert(kListWarps * 32 == (int)kListBlock, "one CTA of the list kernels covers kListBlock pixels");
 struct WriteSink {
     static constexpr bool kCountOnly = false;
     __device__ void volume_steps(int) {}
     float4 *qa, *qd;
     uint32_t *slist;
     uint32_t sat;
+    uint32_t cap;      // slots of the list: records past it are dropped
     const uint2 *srt;  // (count, lane) of the block's pixels, ascending
     uint32_t base, live, lt, s, j;
     __device__ uint32_t next() {
@@ -841,11 +844,13 @@ struct WriteSink {
     }
     __device__ void volume(v3 x, v3 wo, float w) {
         const uint32_t at = next();
+        if (at >= cap) return;
         qa[at] = make_float4(x.x, x.y, x.z, __int_as_float(kNone));
         qd[at] = make_float4(wo.x, wo.y, wo.z, w);
     }
     __device__ void surface(v3 x, int obj, v3 wo, float w) {
         const uint32_t at = next();
+        if (at >= cap) return;
         slist[sat++] = at;
         qa[at] = make_float4(x.x, x.y, x.z, __int_as_float(obj));
         qd[at] = make_float4(wo.x, wo.y, wo.z, w);
@@ -881,14 +886,14 @@ __global__ void count_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_o
     scnt[pix] = c.ns;
 }
 
-__global__ void __launch_bounds__(kListWarps * 32)
-    write_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on, const uint32_t *off,
-                 const uint32_t *soff, float4 *qa, float4 *qd, uint32_t *slist) {
-    __shared__ uint2 srt[kListWarps][32];
-    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (pix - (uint32_t)lane >= npix) return;  // the whole block of 32 pixels
+// The records of the warp's block of 32 pixels (pix this lane's; the
+// block's first pixel below npix), srt the warp's 32 entries of shared
+// memory.
+__device__ __forceinline__ void write_block(const PScene &Sc, const RenderParams &R, bool vol_on, bool surf_on,
+                                            const uint32_t *off, const uint32_t *soff, float4 *qa, float4 *qd,
+                                            uint32_t *slist, uint32_t cap, uint32_t pix, uint32_t npix,
+                                            uint2 *srt) {
+    const int lane = threadIdx.x & 31;
     const bool valid = pix < npix;
     const uint32_t c = valid ? off[pix + 1] - off[pix] : 0u;
     // the block's counts sorted ascending (ties by lane)
@@ -897,20 +902,31 @@ __global__ void __launch_bounds__(kListWarps * 32)
         const uint32_t cq = __shfl_sync(0xffffffffu, c, q);
         rank += (cq < c || (cq == c && q < lane)) ? 1u : 0u;
     }
-    srt[w][rank] = make_uint2(c, (uint32_t)lane);
+    srt[rank] = make_uint2(c, (uint32_t)lane);
     __syncwarp();
     WriteSink ws;
     ws.qa = qa;
     ws.qd = qd;
     ws.slist = slist;
     ws.sat = valid ? soff[pix] : 0u;
-    ws.srt = srt[w];
+    ws.cap = cap;
+    ws.srt = srt;
     ws.base = __shfl_sync(0xffffffffu, valid ? off[pix] : 0u, 0);
     ws.live = __ballot_sync(0xffffffffu, c > 0u);
     ws.lt = (1u << lane) - 1u;
     ws.s = 0;
     ws.j = (uint32_t)__popc(__ballot_sync(0xffffffffu, c == 0u));
     if (valid) walk_eye(Sc, R, pix, vol_on, surf_on, ws);
+}
+
+__global__ void __launch_bounds__(kListWarps * 32)
+    write_kernel(PScene Sc, RenderParams R, bool vol_on, bool surf_on, const uint32_t *off,
+                 const uint32_t *soff, float4 *qa, float4 *qd, uint32_t *slist) {
+    __shared__ uint2 srt[kListWarps][32];
+    const uint32_t npix = (uint32_t)R.width * (uint32_t)R.height;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix - (threadIdx.x & 31u) >= npix) return;  // the whole block of 32 pixels
+    write_block(Sc, R, vol_on, surf_on, off, soff, qa, qd, slist, 0xffffffffu, pix, npix, srt[threadIdx.x >> 5]);
 }
 
 __global__ void __launch_bounds__(kListWarps * 32)
@@ -942,11 +958,9 @@ __global__ void __launch_bounds__(kListWarps * 32)
 // operations and order: volume scale = (T * dt) * (1 / (4/3 pi r^3)),
 // L += e * scale; diffuse scale = (T * (1 / (pi r^2))) * (1 / pi),
 // L += albedo * (e * scale).
-__global__ void __launch_bounds__(kListWarps * 32)
-    composite_exact_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
-                           const float4 *raw, uint32_t npix, float exposure, float4 *rad, uchar4 *rgba) {
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix - (threadIdx.x & 31u) >= npix) return;
+__device__ __forceinline__ void composite_exact_pixel(const PScene &Sc, const uint32_t *off, const float4 *qa,
+                                                      const float4 *qd, const float4 *raw, uint32_t pix,
+                                                      uint32_t npix, float exposure, float4 *rad, uchar4 *rgba) {
     v3 L = mk3(0.f, 0.f, 0.f);
     for_pixel_queries(off, pix, npix, [&](uint32_t i) {
         const float4 v = raw[i];
@@ -972,6 +986,67 @@ __global__ void __launch_bounds__(kListWarps * 32)
                                 to_u8_sat((double)(L.z * exposure) * 255.0), 255);
 }
 
+__global__ void __launch_bounds__(kListWarps * 32)
+    composite_exact_kernel(PScene Sc, const uint32_t *off, const float4 *qa, const float4 *qd,
+                           const float4 *raw, uint32_t npix, float exposure, float4 *rad, uchar4 *rgba) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix - (threadIdx.x & 31u) >= npix) return;
+    composite_exact_pixel(Sc, off, qa, qd, raw, pix, npix, exposure, rad, rgba);
+}
+
+// The block's scene of a batched list launch staged in shared memory (the
+// last j with blk[j] <= blockIdx.x: scenes without pixels have no blocks);
+// returns the block's index within its scene.
+__device__ uint32_t stage_list_scene(const ListScene *ls, const int *ids, const uint32_t *blk, int n,
+                                     ListScene &cur) {
+    __shared__ int sj;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (blk[mid] <= blockIdx.x) lo = mid; else hi = mid;
+        }
+        sj = lo;
+    }
+    __syncthreads();
+    const int j = sj;
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&ls[ids[j]]);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(&cur);
+    for (int i = threadIdx.x; i < (int)(sizeof(ListScene) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    return blockIdx.x - blk[j];
+}
+
+__global__ void __launch_bounds__(kListWarps * 32)
+    list_count_multi_kernel(const ListScene *ls, const int *ids, const uint32_t *blk, int n) {
+    __shared__ ListScene cur;
+    const uint32_t pix = stage_list_scene(ls, ids, blk, n, cur) * blockDim.x + threadIdx.x;
+    if (pix >= cur.npix) return;
+    CountSink c;
+    walk_eye(cur.sc, cur.R, pix, cur.vol_on != 0, cur.surf_on != 0, c);
+    cur.cnt[pix] = c.n;
+    cur.scnt[pix] = c.ns;
+}
+
+__global__ void __launch_bounds__(kListWarps * 32)
+    list_write_multi_kernel(const ListScene *ls, const int *ids, const uint32_t *blk, int n) {
+    __shared__ ListScene cur;
+    __shared__ uint2 srt[kListWarps][32];
+    const uint32_t pix = stage_list_scene(ls, ids, blk, n, cur) * blockDim.x + threadIdx.x;
+    if (pix - (threadIdx.x & 31u) >= cur.npix) return;
+    write_block(cur.sc, cur.R, cur.vol_on != 0, cur.surf_on != 0, cur.off, cur.soff, cur.qa, cur.qd, cur.slist,
+                cur.nq, pix, cur.npix, srt[threadIdx.x >> 5]);
+}
+
+__global__ void __launch_bounds__(kListWarps * 32)
+    list_composite_multi_kernel(const ListScene *ls, const int *ids, const uint32_t *blk, int n) {
+    __shared__ ListScene cur;
+    const uint32_t pix = stage_list_scene(ls, ids, blk, n, cur) * blockDim.x + threadIdx.x;
+    if (pix - (threadIdx.x & 31u) >= cur.npix) return;
+    composite_exact_pixel(cur.sc, cur.off, cur.qa, cur.qd, cur.raw, pix, cur.npix, cur.exposure, cur.rad,
+                          cur.rgba);
+}
+
 __global__ void select_kernel(uint64_t seed, uint32_t frame, const unsigned long long *frame_dev, uint32_t total,
                               const uint32_t *slist, uint32_t ns_total, uint32_t n, float surf_frac,
                               uint32_t *sel) {
@@ -994,18 +1069,40 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
     return v;
 }
 
-__global__ void sample_keys_kernel(CacheGrid g, const float4 *qa, const uint32_t *sel, uint32_t n,
-                                   uint32_t *keys, uint32_t *vals) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 a = qa[sel ? sel[i] : i];
+__device__ __forceinline__ uint32_t query_key(const CacheGrid &g, float4 a) {
     const QueryPos q = unit_pos(g, a);
     const uint32_t x = min((uint32_t)(q.px * 1024.0f), 1023u);
     const uint32_t y = min((uint32_t)(q.py * 1024.0f), 1023u);
     const uint32_t z = min((uint32_t)(q.pz * 1024.0f), 1023u);
     const uint32_t vol = __float_as_int(a.w) == kNone ? 1u : 0u;
-    keys[i] = (vol << 30) | (spread10(x) << 2) | (spread10(y) << 1) | spread10(z);
+    return (vol << 30) | (spread10(x) << 2) | (spread10(y) << 1) | spread10(z);
+}
+
+__global__ void sample_keys_kernel(CacheGrid g, const float4 *qa, const uint32_t *sel, uint32_t n,
+                                   uint32_t *keys, uint32_t *vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = query_key(g, qa[sel ? sel[i] : i]);
     vals[i] = i;
+}
+
+__global__ void list_keys_kernel(const ListScene *ls, const int *tile_scene, size_t first, uint32_t n,
+                                 uint32_t *keys, uint32_t *vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t g = first + i;
+    const int sc = tile_scene[g / kSortTile];
+    uint32_t key = 0xffffffffu, val = 0xffffffffu;
+    if (sc >= 0) {
+        const ListScene &d = ls[sc];
+        const size_t loc = g - d.q_first;
+        if (d.on && loc < d.nq) {
+            key = query_key(d.box, d.qa[loc]);
+            val = (uint32_t)loc;
+        }
+    }
+    keys[i] = key;
+    vals[i] = val;
 }
 
 // The sorted picks' records: pick pos[i] copied to pqa[i], pqd[i]; pord[i] = i.
@@ -1119,6 +1216,38 @@ cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 
     if (npix == 0) return cudaSuccess;
     composite_exact_kernel<<<(npix + kListWarps * 32 - 1) / (kListWarps * 32), kListWarps * 32, 0, s>>>(S, off, qa, qd, raw, npix, exposure, rad,
                                                               rgba);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t list_count_multi(const ListScene *ls, const int *ids, const uint32_t *blk, int n, uint32_t blocks,
+                             cudaStream_t s) {
+    if (n <= 0 || blocks == 0) return cudaSuccess;
+    list_count_multi_kernel<<<blocks, kListWarps * 32, 0, s>>>(ls, ids, blk, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t list_write_multi(const ListScene *ls, const int *ids, const uint32_t *blk, int n, uint32_t blocks,
+                             cudaStream_t s) {
+    if (n <= 0 || blocks == 0) return cudaSuccess;
+    list_write_multi_kernel<<<blocks, kListWarps * 32, 0, s>>>(ls, ids, blk, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t list_composite_multi(const ListScene *ls, const int *ids, const uint32_t *blk, int n,
+                                 uint32_t blocks, cudaStream_t s) {
+    if (n <= 0 || blocks == 0) return cudaSuccess;
+    list_composite_multi_kernel<<<blocks, kListWarps * 32, 0, s>>>(ls, ids, blk, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t list_keys_multi(const ListScene *ls, const int *tile_scene, size_t first, uint32_t n, uint32_t *keys,
+                            uint32_t *vals, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    list_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(ls, tile_scene, first, n, keys, vals);
     note_launch();
     return cudaGetLastError();
 }

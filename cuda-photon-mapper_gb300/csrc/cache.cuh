@@ -110,6 +110,48 @@ cudaError_t render_composite(const PScene &S, const uint32_t *off, const float4 
 // grid box; vals[i] = i.
 cudaError_t cache_sample_keys(const CacheGrid &g, const float4 *qa, const uint32_t *sel, uint32_t n,
                               uint32_t *keys, uint32_t *vals, cudaStream_t s);
+
+// One scene of the batched query-list launches (device array entry): its
+// geometry, camera and query kinds, and its slices of the batch's pools.
+// The per-pixel arrays hold npix + 1 entries (the last count stays 0, so
+// the last offset is the scene's total); the query slice holds nq slots.
+struct ListScene {
+    PScene sc;
+    RenderParams R;
+    uint32_t npix;
+    int vol_on, surf_on;
+    int on;                    // in the query-list render this frame
+    uint32_t nq;               // queries of the slice (counted when the batch was made)
+    size_t q_first;            // the slice's first slot in the query pool
+    CacheGrid box;             // the sort box (lo, inv_size)
+    uint32_t *cnt, *scnt;      // per pixel: queries, diffuse queries
+    uint32_t *off, *soff;      // their scans, restarted at the scene's first pixel
+    float4 *qa, *qd;           // the query slice
+    uint32_t *slist;           // the slice's diffuse queries (at most one per pixel)
+    const float4 *raw;         // the slice's k-NN estimates (flux sum, r^2)
+    float exposure;
+    float4 *rad;
+    uchar4 *rgba;
+};
+constexpr uint32_t kListBlock = 128;  // pixels per CTA of the batched list launches
+// The count, write and exact-composite passes above over the scenes
+// ls[ids[0..n)] in one launch each: blk (device, n + 1 entries) is the
+// exclusive scan of the scenes' blocks of kListBlock pixels, blocks its
+// total.
+// A scene's records never leave its slice: a query past nq is dropped.
+cudaError_t list_count_multi(const ListScene *ls, const int *ids, const uint32_t *blk, int n, uint32_t blocks,
+                             cudaStream_t s);
+cudaError_t list_write_multi(const ListScene *ls, const int *ids, const uint32_t *blk, int n, uint32_t blocks,
+                             cudaStream_t s);
+cudaError_t list_composite_multi(const ListScene *ls, const int *ids, const uint32_t *blk, int n,
+                                 uint32_t blocks, cudaStream_t s);
+// Sort keys of the query pool's slots [first, first + n): slot g of scene
+// s = tile_scene[g / kSortTile] (-1: none) gets cache_sample_keys' key of
+// its query and value g - q_first while it lies below the scene's nq and
+// the scene is on; every other slot key 0xffffffff (after all real keys)
+// and value 0xffffffff.
+cudaError_t list_keys_multi(const ListScene *ls, const int *tile_scene, size_t first, uint32_t n, uint32_t *keys,
+                            uint32_t *vals, cudaStream_t s);
 // The picks in sorted order (pos[i] the i-th pick, sel[pos[i]] its
 // query): their records into pqa, pqd; pord[i] = i.
 cudaError_t cache_pick_records(const uint32_t *pos, const uint32_t *sel, const float4 *qa, const float4 *qd,

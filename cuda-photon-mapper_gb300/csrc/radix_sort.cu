@@ -74,9 +74,13 @@ __global__ void __launch_bounds__(kSortThreads) tile_sum_kernel(const uint32_t *
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
+// With seg_tab (per tile: the first tile of its segment, the segment's
+// tiles) each segment's scan starts at 0: the tile's offset less that of
+// its segment's first tile.
 __global__ void __launch_bounds__(kSortThreads) tile_scan_kernel(const uint32_t *in, uint32_t *out,
                                                                  uint32_t n,
-                                                                 const uint32_t *offs) {
+                                                                 const uint32_t *offs,
+                                                                 const uint2 *seg_tab) {
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t total;
     const uint32_t base = blockIdx.x * kSortTile + threadIdx.x * kSortItems;
@@ -89,6 +93,7 @@ __global__ void __launch_bounds__(kSortThreads) tile_scan_kernel(const uint32_t 
         s += v[i];
     }
     uint32_t run = block_exclusive_scan(s, warp_sums, &total) + offs[blockIdx.x];
+    if (seg_tab) run -= offs[seg_tab[blockIdx.x].x];
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         uint32_t idx = base + i;
@@ -180,19 +185,21 @@ cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
     if (ntiles == 0) ntiles = 1;
     const uint32_t seg = seg_tiles ? seg_tiles : ntiles;
     // The digit-count scan runs in three multi-CTA steps once the histogram
-    // outgrows a few tiles; its tile partials live past the histogram.
+    // outgrows a few tiles (always for pooled segments, so that a pool's
+    // launch sequence does not depend on its size); its tile partials live
+    // past the histogram.
     const uint32_t hn = 256u * ntiles;
     uint32_t *partials = hist + hn;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
         hist_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, n_dev, shift, hist, ntiles, seg,
                                                                         seg_tab); note_launch();
-        if (hn <= kSortTile) {
+        if (hn <= kSortTile && !seg_tab) {
             scan_kernel<<<1, kScanThreads, 0, stream>>>(hist, hist, hn, nullptr); note_launch();
         } else {
             const uint32_t tiles = scan_tile_count(hn);
             tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(hist, hn, partials); note_launch();
             scan_kernel<<<1, kScanThreads, 0, stream>>>(partials, partials, tiles, nullptr); note_launch();
-            tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(hist, hist, hn, partials); note_launch();
+            tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(hist, hist, hn, partials, nullptr); note_launch();
         }
         scatter_kernel<K><<<ntiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n_dev, shift,
                                                                hist, ntiles, seg, seg_tab); note_launch();
@@ -209,9 +216,10 @@ cudaError_t sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
 cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp,
                                  uint32_t *vals_tmp, const uint32_t *n_dev, uint32_t max_n,
                                  int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
-                                 uint32_t **out_keys, uint32_t **out_vals) {
+                                 uint32_t **out_keys, uint32_t **out_vals, uint32_t seg_tiles,
+                                 const uint2 *seg_tab) {
     return sort_pairs<uint32_t>(keys, vals, keys_tmp, vals_tmp, n_dev, max_n, begin_bit, end_bit,
-                                hist, stream, out_keys, out_vals, 0u, nullptr);
+                                hist, stream, out_keys, out_vals, seg_tiles, seg_tab);
 }
 
 cudaError_t radix_sort_pairs_u64(uint64_t *keys, uint32_t *vals, uint64_t *keys_tmp,
@@ -234,7 +242,17 @@ cudaError_t exclusive_scan_u32_large(const uint32_t *in, uint32_t *out, uint32_t
     uint32_t tiles = scan_tile_count(n);
     tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(in, n, tmp); note_launch();
     scan_kernel<<<1, kScanThreads, 0, stream>>>(tmp, tmp, tiles, total); note_launch();
-    tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(in, out, n, tmp); note_launch();
+    tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(in, out, n, tmp, nullptr); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t exclusive_scan_u32_segmented(const uint32_t *in, uint32_t *out, uint32_t n, const uint2 *seg_tab,
+                                         uint32_t *tmp, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t tiles = scan_tile_count(n);
+    tile_sum_kernel<<<tiles, kSortThreads, 0, stream>>>(in, n, tmp); note_launch();
+    scan_kernel<<<1, kScanThreads, 0, stream>>>(tmp, tmp, tiles, nullptr); note_launch();
+    tile_scan_kernel<<<tiles, kSortThreads, 0, stream>>>(in, out, n, tmp, seg_tab); note_launch();
     return cudaGetLastError();
 }
 

@@ -34,7 +34,8 @@ inline size_t radix_sort_hist_words(uint32_t max_n) {
 cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_tmp,
                                  uint32_t *vals_tmp, const uint32_t *n_dev, uint32_t max_n,
                                  int begin_bit, int end_bit, uint32_t *hist, cudaStream_t stream,
-                                 uint32_t **out_keys, uint32_t **out_vals);
+                                 uint32_t **out_keys, uint32_t **out_vals, uint32_t seg_tiles = 0,
+                                 const uint2 *seg_tab = nullptr);
 // With seg_tiles > 0 the items are sorted within segments of seg_tiles x
 // kSortTile consecutive items (each segment keeps its place): a segmented
 // sort in the passes of the segment's own bits. With seg_tab (device, one
@@ -57,5 +58,12 @@ cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, ui
 uint32_t scan_tile_count(uint32_t n);
 cudaError_t exclusive_scan_u32_large(const uint32_t *in, uint32_t *out, uint32_t n,
                                      uint32_t *total, uint32_t *tmp, cudaStream_t stream);
+// The same scan restarted at every segment: the segments are runs of whole
+// tiles of kSortTile items, seg_tab (device) gives per tile its segment's
+// first tile and tile count, and out[i] sums in[] from the segment's first
+// item up to i (exclusive). tmp: scan_tile_count(n) words. Three launches
+// for any number of segments.
+cudaError_t exclusive_scan_u32_segmented(const uint32_t *in, uint32_t *out, uint32_t n, const uint2 *seg_tab,
+                                         uint32_t *tmp, cudaStream_t stream);
 
 }  // namespace pm

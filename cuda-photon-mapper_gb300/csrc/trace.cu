@@ -293,11 +293,8 @@ __global__ void __launch_bounds__(128) trace_batch_kernel(const PScene *scenes,
 }
 
 // Smallest path count whose records reach the target (or all issued paths).
-__global__ void map_extent_kernel(const uint32_t *off, const uint32_t *cnt, uint32_t issued,
-                                  const uint32_t *issued_dev, const uint32_t *total_p,
-                                  uint32_t target, uint32_t *extent) {
-    if (issued_dev) issued = min(*issued_dev, issued);
-    uint32_t total = *total_p;
+__device__ void find_extent(const uint32_t *off, const uint32_t *cnt, uint32_t issued, uint32_t total,
+                            uint32_t target, uint32_t *extent) {
     if (target == 0) {
         extent[0] = 0;
         extent[1] = 0;
@@ -315,6 +312,27 @@ __global__ void map_extent_kernel(const uint32_t *off, const uint32_t *cnt, uint
     }
     extent[0] = target;
     extent[1] = lo + 1;
+}
+
+__global__ void map_extent_kernel(const uint32_t *off, const uint32_t *cnt, uint32_t issued,
+                                  const uint32_t *issued_dev, const uint32_t *total_p,
+                                  uint32_t target, uint32_t *extent) {
+    if (issued_dev) issued = min(*issued_dev, issued);
+    find_extent(off, cnt, issued, *total_p, target, extent);
+}
+
+__global__ void map_extents_kernel(const ExtentJob *jobs, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ExtentJob j = jobs[i];
+    if (j.cap == 0) {
+        j.extent[0] = 0;
+        j.extent[1] = 0;
+        return;
+    }
+    const uint32_t total = j.off[j.cap - 1] + j.cnt[j.cap - 1];
+    *j.total = total;
+    find_extent(j.off, j.cnt, min(*j.issued, j.cap), total, j.target, j.extent);
 }
 
 constexpr uint32_t kNeedTile = 1024;
@@ -407,6 +425,12 @@ cudaError_t map_extent_dev(uint32_t cap, const uint32_t *issued_dev, const uint3
     cudaError_t e = exclusive_scan_u32_large(cnt, off, cap, total, scan_tmp, s);
     if (e != cudaSuccess) return e;
     map_extent_kernel<<<1, 1, 0, s>>>(off, cnt, cap, issued_dev, total, target, extent); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t map_extents_multi(const ExtentJob *jobs, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    map_extents_kernel<<<(n + 127) / 128, 128, 0, s>>>(jobs, n); note_launch();
     return cudaGetLastError();
 }
 

@@ -45,6 +45,16 @@ cudaError_t map_extent(uint32_t issued, const uint32_t *cnt, uint32_t *off, uint
 cudaError_t map_extent_dev(uint32_t cap, const uint32_t *issued_dev, const uint32_t *cnt,
                            uint32_t *off, uint32_t *total, uint32_t *scan_tmp, uint32_t target,
                            uint32_t *extent, cudaStream_t s);
+// map_extent_dev of many maps in one launch, their counts already scanned
+// (off[i] the counts of paths before i, e.g. by a segmented scan of a pool).
+struct ExtentJob {
+    const uint32_t *cnt, *off;  // the map's per-path counts and their scan, over cap paths
+    uint32_t cap, target;
+    const uint32_t *issued;     // paths the counting pass issued (device)
+    uint32_t *total;            // out: records of all cap paths
+    uint32_t *extent;           // out: records, paths
+};
+cudaError_t map_extents_multi(const ExtentJob *jobs, int n, cudaStream_t s);
 // The ids below `issued` of the paths that hold a record of a map (id <
 // ext_s[1] with cnt_s > 0, or id < ext_v[1] with cnt_v > 0), in increasing
 // order, into list[0 .. *list_n): per-tile counts, a scan of them, then each

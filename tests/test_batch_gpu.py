@@ -89,6 +89,29 @@ def test_graph_replay_equals_eager_frame(ctx):
     b.close()
 
 
+def test_frame_launches_do_not_grow_with_scenes(ctx):
+    """Every stage of the frame runs over all scenes in shared launches: a
+    batch of the same two scenes three times over replays exactly as many
+    kernels per frame as the two scenes alone, and each copy renders like
+    the original."""
+    scenes, cfgs = small_batch(2)
+    counts, imgs = [], []
+    for rep in (1, 3):
+        b = photonmap.Batch(ctx, scenes * rep, cfgs * rep)
+        stream = torch.cuda.Stream()
+        b.capture(stream.cuda_stream)
+        l0 = ctx.lib.pm_kernel_launches()
+        b.launch(stream.cuda_stream)
+        stream.synchronize()
+        counts.append(ctx.lib.pm_kernel_launches() - l0)
+        imgs.append(batch_images(b, cfgs * rep))
+        b.close()
+    print("kernels per replayed frame, 2 and 6 scenes:", counts)
+    assert counts[0] == counts[1], counts
+    for i in range(6):
+        np.testing.assert_array_equal(bits(imgs[1][i]), bits(imgs[0][i % 2]), err_msg="copy %d" % i)
+
+
 def test_search_knobs_do_not_change_images(ctx):
     scenes, cfgs = small_batch(4)
     b = photonmap.Batch(ctx, scenes, cfgs)
