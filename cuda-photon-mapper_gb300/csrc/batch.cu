@@ -6,8 +6,9 @@
 // Frame (all on the caller's stream, no host round trip):
 //   1. zero the per-scene words, path counts and gather counters
 //   2. counting pass: one persistent launch over every scene's paths
-//   3. per scene and map: scan of the path counts over the whole path cap
-//      (zero beyond the issued paths) -> record extent (records, paths)
+//   3. every map's record extent (records, paths): one segmented scan of
+//      all maps' path counts (each map a tile-aligned segment over its
+//      path cap, zero beyond the issued paths), then one search per map
 //   4. writing pass: one persistent launch
 //   5. the kd-trees of every map in shared launches (KdMulti): records past
 //      each map's size set to infinity, the radix-sorted levels of all
@@ -15,14 +16,17 @@
 //      is built over its map's capacity (so every launch size is a host
 //      constant)
 //   6. the render: the scenes in per-pixel mode in one persistent launch
-//      over their pixels; each query-list scene's list (per-pixel counts
-//      and scans, records, (map, Morton) sort) into its slice of one arena
-//      sized at creation (a scene's query count depends only on its
-//      geometry and camera), then one persistent shared-candidate estimate
-//      pass over all of them per k-list width, and each scene's exact
-//      composite, every count the launches need kept on the device
+//      over their pixels; the query lists of all query-list scenes in one
+//      arena sized at creation (a scene's query count depends only on its
+//      geometry and camera; each scene's pixel words and query slots are
+//      tile-aligned segments of two pools): one count launch, segmented
+//      scans, one write launch, one segmented (map, Morton) sort; then one
+//      persistent shared-candidate estimate pass over all of them per
+//      k-list width and one exact composite launch, every count the
+//      launches need kept on the device. The frame's launch count does not
+//      grow with the number of scenes.
 //   7. with per-scene radiance caches (pm_batch_cache_enable) step 6's
-//      estimate pass is replaced, scene by scene right after its list is
+//      estimate pass is replaced, scene by scene after the lists are
 //      built: the scene's training picks and their k-NN targets, its
 //      network's Adam steps (schedule, target scale and frame counter in
 //      device memory, so replayed frames keep training), inference over
