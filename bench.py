@@ -136,8 +136,11 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic(preset):
-    """DRAM bytes per k-NN estimate launch from the committed ncu summary, if any."""
+def load_traffic(preset, args):
+    """DRAM bytes per k-NN estimate launch from the committed ncu summary of
+    the preset's full-size frame, if any (none at another resolution)."""
+    if args.resolution:
+        return None
     p = os.path.join(ROOT, "profiles", "query_knn_tile_kernel_preset%d_traffic.txt" % preset)
     try:
         for line in open(p):
@@ -801,7 +804,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(npix * (16 + 4)),
                 "steps": args.e2e_steps},
         "roofline": estimate_roofline(head, args.steps, cfg.k, peak, peak_kind,
-                                      load_traffic(args.preset)),
+                                      load_traffic(args.preset, args)),
         "gpu_launches": int(launches),
         "clocks": head["clocks"],
     }
@@ -838,7 +841,7 @@ def run_ours(args):
             "value": g2 / (sum(sec["frame_ms"]) / 1e3), "unit": "gathers/s",
             "ms_per_step": statistics.mean(sec["frame_ms"]), "steps": steps2,
             "phases": phases_of(sec, steps2),
-            "roofline": estimate_roofline(sec, steps2, cf2.k, peak, peak_kind, load_traffic(p2)),
+            "roofline": estimate_roofline(sec, steps2, cf2.k, peak, peak_kind, load_traffic(p2, args)),
             "clocks": sec["clocks"],
         }
         fp64_2 = None
