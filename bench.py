@@ -414,11 +414,11 @@ def batch_frames(ctx, lib, args, device):
     """The batched workload: `batch_scenes` independent scenes (2..32
     spheres, sigma_s in [0, 0.2], 1e5..4e6 photons, 256^2..1024^2 pixels,
     k of 32/64/128) per frame -- one persistent trace launch per pass over
-    all scenes, the radix-sorted tree levels of all maps in shared launches
-    and each map's tree finish on side streams, every scene's query list in
-    one arena and one persistent estimate launch per k-list width --
-    captured as a CUDA graph and replayed. One eager frame is timed beside
-    the replays."""
+    all scenes, the record extents, tree levels and tree finishes of all
+    maps in shared launches, every scene's query list built by shared
+    launches into one arena, one persistent estimate launch per k-list
+    width and one composite launch -- captured as a CUDA graph and
+    replayed. One eager frame is timed beside the replays."""
     import torch
     import photonmap
     pairs = [photonmap.batch_scene(i) for i in range(args.batch_scenes)]
