@@ -715,6 +715,23 @@ def estimate_roofline(r, steps, k, peak, peak_kind, traffic):
                        "on the render stream)"}
 
 
+def frame_roofline(r, steps, k, peak, peak_kind):
+    """The whole frame against HBM by the frame formula: 32 B per stored
+    record (emission), 116 B per record of each map's kd build (positions
+    read, keys and indices written, the permutation's key and index read
+    and written, the 32 B records read and written) and 32 B x k + 16 B per
+    k-NN gather (the k records and the value written), over the frame's
+    CUDA-event time."""
+    records = float(sum(r["map_sizes"]))
+    q_per_frame = (r["surf"] + r["vol"]) / steps
+    alg_bytes = 32.0 * records + 116.0 * records + q_per_frame * (32.0 * k + 16.0)
+    achieved = alg_bytes / (statistics.mean(r["frame_ms"]) / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind, "algorithmic_bytes_per_frame": alg_bytes,
+            "formula": "32 B x stored records + 116 B x records (kd build per map) + gathers x "
+                       "(32 B x k + 16 B), over the frame's CUDA-event time"}
+
+
 def host_maps(ctx):
     """The context's two photon maps copied to the host as oracle maps."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -805,6 +822,7 @@ def run_ours(args):
                 "steps": args.e2e_steps},
         "roofline": estimate_roofline(head, args.steps, cfg.k, peak, peak_kind,
                                       load_traffic(args.preset, args)),
+        "frame_roofline": frame_roofline(head, args.steps, cfg.k, peak, peak_kind),
         "gpu_launches": int(launches),
         "clocks": head["clocks"],
     }
@@ -842,6 +860,7 @@ def run_ours(args):
             "ms_per_step": statistics.mean(sec["frame_ms"]), "steps": steps2,
             "phases": phases_of(sec, steps2),
             "roofline": estimate_roofline(sec, steps2, cf2.k, peak, peak_kind, load_traffic(p2, args)),
+            "frame_roofline": frame_roofline(sec, steps2, cf2.k, peak, peak_kind),
             "clocks": sec["clocks"],
         }
         fp64_2 = None
