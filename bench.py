@@ -13,7 +13,10 @@ Prints one JSON line. `value` is k-NN gathers (surface + volume radiance
 estimates) per second of whole-frame device time; photon throughput and the
 per-phase times are reported beside it, with the relative RMSE of sampled
 pixels against the FP64 oracle render (`fp64`) and their bit-equality with
-the FP32 oracle (`parity_sample`). More workloads ride on the same line:
+the FP32 oracle (`parity_sample`). `roofline` is the k-NN estimate pass
+against the measured HBM bandwidth (with the full-size DRAM traffic per
+launch from the committed ncu summary) and `frame_roofline` the whole frame
+by the frame byte formula. More workloads ride on the same line:
 `preset2` (the 2M-photon scene, same metric), `cache` (the learned radiance
 cache on the preset-2 scene: online frame and cached render against the k-NN
 render, errors against the k-NN and FP64 renders), `batch` (64 independent
