@@ -339,7 +339,7 @@ def cache_ab(ctx, lib, stream, rad, flush, args, cfg, knn_render_ms, bf16_peak, 
     `cache_warm_frames` online training frames, each timed step is one online
     frame (2^20 k-NN training samples + their Adam steps, then the cached
     render of every query). Error is the relative RMSE of the cached image
-    against the k-NN render of the same frame (the cache's judge)."""
+    against the k-NN render of the same frame (the yardstick the cache is trained toward)."""
     import numpy as np
     import torch
     sh = stream.cuda_stream

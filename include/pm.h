@@ -365,7 +365,7 @@ PM_API pm_status pm_phys_viewer_display(pm_phys_viewer *v, float4 *radiance, uch
  * tensor cores with fp32 accumulation. pm_cache_train fits it online to
  * k-NN estimates at random queries of the current frame; pm_render_cached
  * sums the network's predictions per pixel (source 0) or, as its fallback
- * and judge, the k-NN estimates of every query (source 1, equal to
+ * and yardstick, the k-NN estimates of every query (source 1, equal to
  * pm_render up to summation rounding). The cache lives in the context and
  * survives pm_set_scene. */
 typedef struct pm_cache_config {
