@@ -454,16 +454,20 @@ PM_API pm_status pm_cache_load(pm_ctx *ctx, const char *path);
 /* ---- 7. batched scenes ---------------------------------------------------------
  * No counterpart in the reference, which renders one scene. A batch holds
  * many independent scenes (own maps, trees, images, k and resolution) and
- * runs a frame of all of them as: one persistent trace launch over every
- * scene's photon paths (counting pass), per-scene record extents without a
- * host round trip, one persistent trace launch (writing pass), per-scene
- * kd-tree builds on side streams, then the render: every query-list scene's
- * query list and spatial sort into one arena sized at creation (counts kept
- * on the device), one persistent shared-candidate estimate launch over all
- * of them per k-list width and per-scene composites; the scenes in
- * per-pixel mode in one persistent launch that hands out pixel chunks of
- * all of them dynamically. Because no
- * step reads a count back to the host, the whole frame can be captured as a
+ * runs a frame of all of them in shared launches:
+ *  - one persistent trace launch over every scene's photon paths (counting
+ *    pass);
+ *  - every map's record extent from one segmented scan of all path counts;
+ *  - one persistent trace launch (writing pass);
+ *  - the kd-trees of all maps, level by level and finish by finish;
+ *  - the render. Every query-list scene's query list (counts, scans,
+ *    records, spatial sort) is built into one arena sized at creation, with
+ *    every count kept on the device. Then one persistent shared-candidate
+ *    estimate launch per k-list width and one composite launch. The scenes
+ *    in per-pixel mode go through one persistent launch that hands out
+ *    pixel chunks of all of them dynamically.
+ * The number of launches does not grow with the number of scenes. No step
+ * reads a count back to the host, so the whole frame can be captured as a
  * CUDA graph (pm_batch_capture) and replayed (pm_batch_launch). Every
  * scene's image is bit-identical to a single-scene pm_emit + pm_build +
  * pm_render with the same scene, config and path cap. */
