@@ -224,8 +224,9 @@ struct pm_batch {
     unsigned long long graph_kernels = 0;
     bool ran = false;
     int n_pixel = 0;  // scenes in the persistent per-pixel launch
-    // query-list mode: one buffer set for the scenes rendered one after
-    // another, sized for the largest
+    // one scene's query list at a time, sized for the largest scene: the
+    // autotuner's timed single-scene query-list renders and the creation
+    // count of every scene's queries
     struct Queries {
         uint32_t *cnt = nullptr, *off = nullptr, *scnt = nullptr, *soff = nullptr, *slist = nullptr;
         uint32_t *scan_tmp = nullptr;
